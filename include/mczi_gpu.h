@@ -1,0 +1,139 @@
+/*
+ * mczi_gpu.h -- C ABI of libmczi_gpu, the GB300 (sm_103a) implementation of
+ * the MC / ZI k-mer hot path.
+ *
+ * Conventions
+ *  - Every call returns an int32_t status: MCZI_OK (0) or a negative code; the
+ *    message of the last failure is available from mczi_last_error(ctx).  No
+ *    C++ exception and no abort crosses this boundary.
+ *  - The library owns device memory; the caller owns host buffers.  Results
+ *    are kept in the context until the next run and copied out with the
+ *    *_copy calls (call with NULL pointers or query the size first).
+ *  - One context is bound to one CUDA device, one stream and one host thread
+ *    at a time; several contexts may coexist.
+ *  - There is no CPU fallback: if the device or the kernels are unavailable
+ *    the call fails with MCZI_ERR_DEVICE.
+ *
+ * Reference interfaces (paths inside the MCZI project) each entry replaces
+ * are cited on the declarations.
+ */
+#ifndef MCZI_GPU_H
+#define MCZI_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCZI_OK 0
+#define MCZI_ERR_INVALID_CONFIG (-1) /* the reference's `ensure!` failures, same messages */
+#define MCZI_ERR_IO (-2)             /* file open/read/write failure */
+#define MCZI_ERR_OOM (-3)            /* not enough free HBM for the request */
+#define MCZI_ERR_DEVICE (-4)         /* CUDA error or kernels unavailable */
+#define MCZI_ERR_TIMEOUT (-5)        /* a bounded device-side wait gave up */
+#define MCZI_ERR_STATE (-6)          /* call out of order (e.g. no result yet) */
+
+#define MCZI_MODE_ABUNDANCE 0 /* count every occurrence */
+#define MCZI_MODE_PRESENCE 1  /* fof: count each dataset (input) at most once */
+
+/* CounterConfig{k, minimizer, threshold, partition_count}, src/lib.rs:48-53.
+ * partition_count only shapes the reference's temporary files; it is
+ * validated (> 0) and otherwise has no effect on results, as in MC. */
+typedef struct {
+  uint32_t k;
+  uint32_t minimizer;
+  uint64_t threshold;
+  uint32_t partition_count;
+} mczi_counter_config;
+
+/* One FASTA/FASTQ input held in host memory (already decompressed). */
+typedef struct {
+  const uint8_t* data;
+  uint64_t len;
+} mczi_input;
+
+typedef struct mczi_ctx mczi_ctx;
+
+/* Opens a context on CUDA device `device`. */
+int32_t mczi_open(int32_t device, mczi_ctx** out);
+int32_t mczi_close(mczi_ctx* ctx);
+const char* mczi_last_error(const mczi_ctx* ctx);
+/* Makes the context enqueue its work on `cuda_stream` (a cudaStream_t; NULL
+ * restores the context's own stream). */
+int32_t mczi_set_stream(mczi_ctx* ctx, void* cuda_stream);
+
+/* Validation exactly as MC: validate_config (src/lib.rs:110-116, shape checks
+ * :119-139) for mode 0, validate_dataset_presence_config (:141-152) for mode 1. */
+int32_t mczi_validate_config(mczi_ctx* ctx, const mczi_counter_config* cfg, int32_t mode);
+
+/* ---------------------------------------------------------------- MC */
+
+/* count_inputs (src/lib.rs:278) / count_datasets (src/lib.rs:289): counts the
+ * canonical k-mers of `inputs` and keeps those with count > threshold.
+ * Mode 0 counts occurrences (exact counts); mode 1 counts the inputs
+ * (datasets) containing each k-mer (fof, k <= 32).  Inputs that do not start
+ * with a FASTA/FASTQ record are skipped with an MC_WARN line, like
+ * src/lib.rs:3371-3392.  *n_records receives the number of kept k-mers. */
+int32_t mczi_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int32_t mode, const mczi_input* inputs,
+                   size_t n_inputs, uint64_t* n_records);
+
+/* Split form of mczi_count for callers that keep the inputs resident:
+ * mczi_stage copies the inputs to HBM (host->device), mczi_count_staged runs
+ * the device pipeline on the staged bytes. */
+int32_t mczi_stage(mczi_ctx* ctx, const mczi_input* inputs, size_t n_inputs);
+int32_t mczi_count_staged(mczi_ctx* ctx, const mczi_counter_config* cfg, int32_t mode, uint64_t* n_records);
+
+/* Copies the kept records of the last count.  key_hi may be NULL for k <= 32.
+ * sorted != 0 sorts by canonical k-mer (the order of count_inputs). */
+int32_t mczi_result_copy(mczi_ctx* ctx, uint64_t* key_lo, uint64_t* key_hi, uint64_t* counts, uint64_t cap,
+                         int32_t sorted);
+
+/* KFF file of the last count (src/lib.rs:1633-1670, 3071-3121): count bytes 1
+ * (mode 0, k <= 32, counts saturated at min(x+1, 255)), 8 (mode 0, k > 32) or
+ * 4 (mode 1), as MC's count_inputs_to_kff_path / count_datasets_to_kff_path. */
+int32_t mczi_result_write_kff(mczi_ctx* ctx, const char* path);
+/* Greedy simplitig FASTA of the last count (src/lib.rs:1469-1533), as
+ * count_inputs_to_fasta_path / count_datasets_to_fasta_path. */
+int32_t mczi_result_write_fasta(mczi_ctx* ctx, const char* path);
+
+/* Path-based drop-ins for the MC library entry points (plain FASTA/FASTQ files;
+ * compressed inputs are decompressed by the caller):
+ *   count_inputs_to_kff_path   src/lib.rs:457
+ *   count_inputs_to_fasta_path src/lib.rs:427
+ *   count_datasets_to_kff_path src/lib.rs:509
+ *   count_datasets_to_fasta_path src/lib.rs:442  */
+int32_t mczi_count_inputs_to_kff_path(mczi_ctx* ctx, const char* const* inputs, size_t n_inputs,
+                                      const mczi_counter_config* cfg, const char* output_path);
+int32_t mczi_count_inputs_to_fasta_path(mczi_ctx* ctx, const char* const* inputs, size_t n_inputs,
+                                        const mczi_counter_config* cfg, const char* output_path);
+int32_t mczi_count_datasets_to_kff_path(mczi_ctx* ctx, const char* const* inputs, size_t n_inputs,
+                                        const mczi_counter_config* cfg, const char* output_path);
+int32_t mczi_count_datasets_to_fasta_path(mczi_ctx* ctx, const char* const* inputs, size_t n_inputs,
+                                          const mczi_counter_config* cfg, const char* output_path);
+
+/* Per-phase device times (ms) of the last run, measured with CUDA events on
+ * the context's stream: [0] pack, [1] minimizer scan, [2] partition,
+ * [3] k-mer counting, [4] minimizer pre-count (0 when not run).
+ * Returns the number of phases written. */
+int32_t mczi_phase_times(mczi_ctx* ctx, float* ms, int32_t cap);
+/* Statistics of the last run: [0] bases, [1] superkmers, [2] counting rounds,
+ * [3] round splits, [4] distinct k-mers inserted, [5] kept records,
+ * [6] k-mer windows, [7] skipped inputs. */
+int32_t mczi_run_stats(mczi_ctx* ctx, uint64_t* out, int32_t cap);
+
+/* Tuning knobs (results never depend on them): threads per counting CTA,
+ * table slots per CTA (0 = largest that fits), CTAs per SM. */
+int32_t mczi_set_count_tuning(mczi_ctx* ctx, int32_t threads, int32_t table_slots, int32_t ctas_per_sm);
+
+/* Packer parity hook: after mczi_count/mczi_count_staged, copies the 2-bit
+ * codes (one byte per base) and fragment-start flags (one byte per base) of
+ * the packed stream; *n_bases receives the base count. */
+int32_t mczi_debug_packed(mczi_ctx* ctx, uint8_t* codes, uint8_t* starts, uint64_t cap, uint64_t* n_bases);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCZI_GPU_H */

@@ -1,0 +1,257 @@
+// host_io.cpp -- host-side output writers for libmczi_gpu.
+//
+// The reference keeps output formatting on the host (src/lib.rs:1190-1676),
+// and so does this library: the device produces (canonical k-mer, count)
+// records, the host serialises them.
+#include "host_io.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+
+namespace mczi {
+
+namespace {
+
+typedef unsigned __int128 u128;
+
+struct File {
+  FILE* f = nullptr;
+  std::vector<uint8_t> buf;
+  bool ok = true;
+  explicit File(const std::string& p) : f(std::fopen(p.c_str(), "wb")) { buf.reserve(1 << 20); }
+  ~File() { close(); }
+  void put(const void* p, size_t n) {
+    const uint8_t* b = static_cast<const uint8_t*>(p);
+    buf.insert(buf.end(), b, b + n);
+    if (buf.size() >= (1u << 20)) flush();
+  }
+  void put_u8(uint8_t v) { put(&v, 1); }
+  void put_be(uint64_t v, int bytes) {
+    uint8_t b[8];
+    for (int i = 0; i < bytes; i++) b[i] = (uint8_t)(v >> (8 * (bytes - 1 - i)));
+    put(b, (size_t)bytes);
+  }
+  void flush() {
+    if (f && !buf.empty()) {
+      if (std::fwrite(buf.data(), 1, buf.size(), f) != buf.size()) ok = false;
+    }
+    buf.clear();
+  }
+  bool close() {
+    if (f) {
+      flush();
+      if (std::fclose(f) != 0) ok = false;
+      f = nullptr;
+    }
+    return ok;
+  }
+};
+
+inline u128 key_at(const HostRecords& r, size_t i) {
+  return ((u128)(r.hi.empty() ? 0 : r.hi[i]) << 64) | r.lo[i];
+}
+
+inline uint64_t mix64(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  return x ^ (x >> 33);
+}
+inline uint64_t hash128(u128 k) { return mix64((uint64_t)k ^ mix64((uint64_t)(k >> 64) + 0x9e3779b97f4a7c15ull)); }
+
+// open-addressing set with tombstone removal (keys are never re-inserted)
+struct RemainingSet {
+  std::vector<u128> keys;
+  std::vector<uint8_t> state;  // 0 empty, 1 live, 2 removed
+  uint64_t mask = 0;
+  explicit RemainingSet(size_t n) {
+    size_t c = 64;
+    while (c < n * 2 + 64) c <<= 1;
+    keys.assign(c, 0);
+    state.assign(c, 0);
+    mask = c - 1;
+  }
+  bool insert(u128 k) {
+    uint64_t s = hash128(k) & mask;
+    while (state[s] != 0) {
+      if (keys[s] == k) return false;
+      s = (s + 1) & mask;
+    }
+    keys[s] = k;
+    state[s] = 1;
+    return true;
+  }
+  bool remove(u128 k) {
+    uint64_t s = hash128(k) & mask;
+    while (state[s] != 0) {
+      if (keys[s] == k) {
+        if (state[s] == 1) { state[s] = 2; return true; }
+        return false;
+      }
+      s = (s + 1) & mask;
+    }
+    return false;
+  }
+};
+
+inline int code_of(char b) { return b == 'A' ? 0 : b == 'C' ? 1 : b == 'G' ? 2 : 3; }
+inline char comp(char b) { return b == 'A' ? 'T' : b == 'C' ? 'G' : b == 'G' ? 'C' : 'A'; }
+
+void revcomp(std::string& s) {
+  std::reverse(s.begin(), s.end());
+  for (char& c : s) c = comp(c);
+}
+
+u128 suffix_extension(const std::string& seq, int k, char base) {
+  const u128 mask = k == 64 ? ~(u128)0 : (((u128)1 << (2 * k)) - 1);
+  const int hs = 2 * (k - 1);
+  u128 fwd = 0, rev = 0;
+  for (size_t i = seq.size() - (size_t)(k - 1); i < seq.size(); i++) {
+    const u128 b = (u128)code_of(seq[i]);
+    fwd = ((fwd << 2) | b) & mask;
+    rev = (rev >> 2) | ((b ^ 3) << hs);
+  }
+  const u128 b = (u128)code_of(base);
+  fwd = ((fwd << 2) | b) & mask;
+  rev = (rev >> 2) | ((b ^ 3) << hs);
+  return fwd < rev ? fwd : rev;
+}
+
+void extend_forward(std::string& seq, int k, RemainingSet& rem) {
+  static const char B[4] = {'A', 'C', 'G', 'T'};
+  for (;;) {
+    bool ext = false;
+    for (char b : B) {
+      if (rem.remove(suffix_extension(seq, k, b))) {
+        seq.push_back(b);
+        ext = true;
+        break;
+      }
+    }
+    if (!ext) return;
+  }
+}
+
+}  // namespace
+
+bool write_kff_file(const std::string& path, const HostRecords& r, int k, int m, uint64_t x, int count_size,
+                    std::string* err) {
+  File o(path);
+  if (!o.f) {
+    *err = "failed to create " + path;
+    return false;
+  }
+  char fb[512];
+  const int fbl = std::snprintf(fb, sizeof fb,
+                                "producer=MC\nk=%d\nm=%d\nthreshold=%llu\nfilter=count>threshold\ncanonical=1\n", k, m,
+                                (unsigned long long)x);
+  o.put("KFF", 3);
+  const uint8_t ver[5] = {1, 0, 0x1b, 1, 1};
+  o.put(ver, 5);
+  o.put_be((uint64_t)fbl, 4);
+  o.put(fb, (size_t)fbl);
+  o.put("v", 1);
+  o.put_be(6, 8);
+  const char* names[6] = {"k", "max", "data_size", "ordered", "m", "threshold"};
+  const uint64_t vals[6] = {(uint64_t)k, 1, (uint64_t)count_size, 0, (uint64_t)m, x};
+  for (int i = 0; i < 6; i++) {
+    o.put(names[i], std::strlen(names[i]) + 1);
+    o.put_be(vals[i], 8);
+  }
+  o.put("r", 1);
+  const size_t n = r.lo.size();
+  o.put_be(n, 8);
+  const int nb = (k + 3) / 4;
+  const uint64_t sat = (x + 1) < 255 ? (x + 1) : 255;
+  uint8_t rec[32];
+  for (size_t i = 0; i < n; i++) {
+    uint8_t be[16];
+    const uint64_t hi = r.hi.empty() ? 0 : r.hi[i], lo = r.lo[i];
+    for (int j = 0; j < 8; j++) {
+      be[j] = (uint8_t)(hi >> (56 - 8 * j));
+      be[8 + j] = (uint8_t)(lo >> (56 - 8 * j));
+    }
+    std::memcpy(rec, be + 16 - nb, (size_t)nb);
+    int len = nb;
+    const uint64_t c = r.count[i];
+    if (count_size == 1) {
+      rec[len++] = (uint8_t)(c < sat ? c : sat);
+    } else {
+      for (int j = 0; j < count_size; j++) rec[len++] = (uint8_t)(c >> (8 * (count_size - 1 - j)));
+    }
+    o.put(rec, (size_t)len);
+  }
+  o.put("KFF", 3);
+  if (!o.close()) {
+    *err = "failed to write " + path;
+    return false;
+  }
+  return true;
+}
+
+bool write_simplitig_file(const std::string& path, const HostRecords& r, int k, std::string* err) {
+  File o(path);
+  if (!o.f) {
+    *err = "failed to create " + path;
+    return false;
+  }
+  const size_t n = r.lo.size();
+  RemainingSet rem(n);
+  std::vector<u128> seeds;
+  seeds.reserve(n);
+  for (size_t i = 0; i < n; i++) {
+    const u128 key = key_at(r, i);
+    if (rem.insert(key)) seeds.push_back(key);
+  }
+  std::sort(seeds.begin(), seeds.end());
+  static const char B[4] = {'A', 'C', 'G', 'T'};
+  uint64_t idx = 0;
+  std::string seq;
+  char line[64];
+  for (u128 seed : seeds) {
+    if (!rem.remove(seed)) continue;
+    seq.clear();
+    for (int j = 0; j < k; j++) seq.push_back(B[(int)((seed >> (2 * (k - 1 - j))) & 3)]);
+    extend_forward(seq, k, rem);
+    revcomp(seq);
+    extend_forward(seq, k, rem);
+    revcomp(seq);
+    idx++;
+    const int l = std::snprintf(line, sizeof line, ">MC_simplitig_%llu kmers=%llu\n", (unsigned long long)idx,
+                                (unsigned long long)(seq.size() - (size_t)k + 1));
+    o.put(line, (size_t)l);
+    for (size_t p = 0; p < seq.size(); p += 80) {
+      const size_t len = std::min<size_t>(80, seq.size() - p);
+      o.put(seq.data() + p, len);
+      o.put_u8('\n');
+    }
+  }
+  if (!o.close()) {
+    *err = "failed to write " + path;
+    return false;
+  }
+  return true;
+}
+
+bool read_file(const std::string& path, std::vector<uint8_t>* out, std::string* err) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) {
+    *err = "failed to open FASTA/FASTQ input " + path;
+    return false;
+  }
+  out->clear();
+  uint8_t buf[1 << 16];
+  size_t got;
+  while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) out->insert(out->end(), buf, buf + got);
+  const bool bad = std::ferror(f) != 0;
+  std::fclose(f);
+  if (bad) {
+    *err = "failed to read " + path;
+    return false;
+  }
+  return true;
+}
+
+}  // namespace mczi

@@ -1,0 +1,386 @@
+// mc_count.cu -- K5: per-partition canonical k-mer counting in shared memory
+// with MC's strict `count > x` threshold.
+//
+// Replaces MC's phase-2/3 partition counters: the k <= 32 sort + run-length
+// path (src/lib.rs:2512-2570), the u128 AHashMap path for k > 32
+// (src/lib.rs:2400-2425, 3589-3614) and the fof per-dataset dedup + presence
+// table (src/lib.rs:2213-2247, 4450-4522).
+//
+// A persistent CTA takes p1 buckets from a work counter.  For each bucket it
+// histograms the window occupancy of the 4096 p2 bins, cuts the bins into
+// rounds whose expected number of distinct k-mers fits the shared-memory
+// table (expected = occupancy x the distinct/occurrence ratio measured so far
+// across the grid), and for every round: clears the table, regenerates the
+// canonical k-mers of the round's superkmers on chip (the k-mers never touch
+// HBM), inserts them with shared-memory CAS, and emits the slots whose count
+// passes the threshold.  A round whose table fills past 85 % is abandoned and
+// split -- by bins while it spans several, then by k-mer hash range -- so the
+// result never depends on the estimate.  Every k-mer of a bucket lands in
+// exactly one round because the p2 bin and the hash range are functions of
+// the canonical k-mer.
+//
+// Presence mode (fof): the table holds a bitmask of datasets per k-mer; the
+// dataset of a superkmer is found from its base offset.  count = popcount.
+#include "mczi_internal.h"
+#include "mczi_common.cuh"
+
+namespace mczi {
+
+namespace {
+
+constexpr int MAX_STACK = 48;
+
+template <class K>
+struct KeyOps;
+
+template <>
+struct KeyOps<K64> {
+  static __device__ __forceinline__ K64 cas(K64* p, K64 cmp, K64 val) {
+    unsigned long long r = atomicCAS(reinterpret_cast<unsigned long long*>(p), (unsigned long long)cmp.v,
+                                     (unsigned long long)val.v);
+    return K64{(uint64_t)r};
+  }
+};
+
+template <>
+struct KeyOps<K128> {
+  static __device__ __forceinline__ K128 cas(K128* p, K128 cmp, K128 val) { return atomicCAS(p, cmp, val); }
+};
+
+struct RoundRange {
+  uint32_t bl, bh;   // p2 bins [bl, bh)
+  uint32_t hlo, hhi; // k-mer hash range [hlo, hhi]
+};
+
+__device__ __forceinline__ uint32_t popc_words(const unsigned long long* m, int W) {
+  uint32_t c = 0;
+  for (int i = 0; i < W; i++) c += __popcll(m[i]);
+  return c;
+}
+
+}  // namespace
+
+size_t count_slot_bytes(int k, int mode, int n_datasets) {
+  const size_t keyb = k <= 32 ? 8 : 16;
+  const size_t valb = mode == 0 ? 4 : 8 * (size_t)((n_datasets + 63) / 64);
+  return keyb + valb;
+}
+
+size_t count_fixed_smem_bytes(int mode, int n_datasets) {
+  const size_t hist = 2 * (NP2 + 1) * sizeof(uint32_t) + (NP2 + 1) * sizeof(uint16_t);
+  const size_t dsb = mode == 0 ? 0 : ((size_t)n_datasets + 1) * sizeof(uint64_t);
+  return hist + dsb + 96;
+}
+
+size_t count_smem_bytes(int k, int mode, int n_datasets, uint32_t table_slots) {
+  const size_t S = table_slots;
+  const size_t keyb = k <= 32 ? 8 : 16;
+  size_t b = S * keyb;
+  b = (b + 15) & ~(size_t)15;
+  b += S * (count_slot_bytes(k, mode, n_datasets) - keyb);
+  b = (b + 15) & ~(size_t)15;
+  return b + count_fixed_smem_bytes(mode, n_datasets);
+}
+
+template <class K, class R, int MODE>
+__global__ void k_count(CountArgs a) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const uint32_t S = a.table_slots;
+  const int W = MODE == 0 ? 1 : (a.n_datasets + 63) / 64;
+  K* keys = reinterpret_cast<K*>(smem);
+  size_t off = ((size_t)S * sizeof(K) + 15) & ~(size_t)15;
+  uint32_t* cnt = reinterpret_cast<uint32_t*>(smem + off);                     // MODE 0
+  unsigned long long* msk = reinterpret_cast<unsigned long long*>(smem + off);  // MODE 1
+  off += MODE == 0 ? (size_t)S * 4 : (size_t)S * 8 * W;
+  off = (off + 15) & ~(size_t)15;
+  uint32_t* occ = reinterpret_cast<uint32_t*>(smem + off);   // NP2 + 1, becomes occupancy prefix
+  off += (NP2 + 1) * sizeof(uint32_t);
+  uint32_t* dst = reinterpret_cast<uint32_t*>(smem + off);   // NP2 + 1, descriptor prefix
+  off += (NP2 + 1) * sizeof(uint32_t);
+  uint16_t* rstart = reinterpret_cast<uint16_t*>(smem + off);  // round start bins
+  off += (NP2 + 1) * sizeof(uint16_t);
+  off = (off + 7) & ~(size_t)7;
+  uint64_t* dsbase = reinterpret_cast<uint64_t*>(smem + off);  // MODE 1
+
+  __shared__ uint32_t s_bucket, s_nused, s_over, s_nrounds, s_sp;
+  __shared__ RoundRange stack[MAX_STACK];
+  __shared__ uint32_t warp_tmp[32];
+  __shared__ float s_rho;
+
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int lane = tid & 31;
+  const int k = a.k;
+  const K EMPTY = key_empty<K>();
+  const uint32_t limit = (uint32_t)(0.85f * (float)S);
+
+  if (MODE == 1) {
+    for (int i = tid; i <= a.n_datasets; i += nth) dsbase[i] = a.dataset_base[i];
+  }
+
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) {
+      s_bucket = atomicAdd(a.work_counter, 1u);
+      const unsigned long long o = a.stats[0], d = a.stats[1];
+      float rho = 1.0f;
+      if (o > 200000ull) rho = fminf(1.0f, 1.3f * (float)d / (float)o + 0.02f);
+      s_rho = rho;
+    }
+    __syncthreads();
+    const uint32_t b = s_bucket;
+    if (b >= (uint32_t)NP1) break;
+    const uint64_t lo = a.bucket_off[b], hi = a.bucket_off[b + 1];
+    if (hi <= lo) continue;
+
+    // ---- per-bin occupancy and descriptor counts
+    for (int i = tid; i <= NP2; i += nth) { occ[i] = 0; dst[i] = 0; }
+    __syncthreads();
+    for (uint64_t i = lo + tid; i < hi; i += nth) {
+      const uint32_t bin = (a.key[i] >> (32 - P1_BITS - P2_BITS)) & (NP2 - 1);
+      const uint32_t len = (uint32_t)(a.desc[i] & 0xffffffu) + 1u;
+      atomicAdd(&occ[bin], len);
+      atomicAdd(&dst[bin], 1u);
+    }
+    __syncthreads();
+    // exclusive prefix of both arrays (sequential chunks + warp scan)
+    {
+      const int per = (NP2 + nth - 1) / nth;
+      const int base = tid * per;
+      uint32_t so = 0, sd = 0;
+      for (int i = 0; i < per; i++) {
+        const int j = base + i;
+        if (j < NP2) { so += occ[j]; sd += dst[j]; }
+      }
+      // block scan of (so, sd) via two passes of warp scans
+      uint32_t vo = so, vd = sd;
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t yo = __shfl_up_sync(0xffffffffu, vo, o);
+        uint32_t yd = __shfl_up_sync(0xffffffffu, vd, o);
+        if (lane >= o) { vo += yo; vd += yd; }
+      }
+      __shared__ uint32_t wo[32], wd[32];
+      if (lane == 31) { wo[tid >> 5] = vo; wd[tid >> 5] = vd; }
+      __syncthreads();
+      if (tid < 32) {
+        const int nw = nth / 32;
+        uint32_t to = tid < nw ? wo[tid] : 0u, td = tid < nw ? wd[tid] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+          uint32_t yo = __shfl_up_sync(0xffffffffu, to, o);
+          uint32_t yd = __shfl_up_sync(0xffffffffu, td, o);
+          if (tid >= o) { to += yo; td += yd; }
+        }
+        wo[tid] = to;
+        wd[tid] = td;
+      }
+      __syncthreads();
+      uint32_t ro = vo - so + ((tid >> 5) ? wo[(tid >> 5) - 1] : 0u);
+      uint32_t rd = vd - sd + ((tid >> 5) ? wd[(tid >> 5) - 1] : 0u);
+      for (int i = 0; i < per; i++) {
+        const int j = base + i;
+        if (j < NP2) {
+          const uint32_t co = occ[j], cd = dst[j];
+          occ[j] = ro;
+          dst[j] = rd;
+          ro += co;
+          rd += cd;
+        }
+      }
+      __syncthreads();
+      if (tid == nth - 1) { occ[NP2] = ro; dst[NP2] = rd; }
+      __syncthreads();
+    }
+
+    // ---- cut bins into rounds: round id of a bin = floor(occ_prefix / budget)
+    const float budget_f = a.fill * (float)S / s_rho;
+    const uint32_t budget = budget_f < 1.0f ? 1u : (uint32_t)budget_f;
+    if (tid == 0) s_nrounds = 0;
+    __syncthreads();
+    {
+      // compaction of round starts, in bin order: warp ballots, chunked
+      for (int base = 0; base < NP2; base += nth) {
+        const int j = base + tid;
+        bool st = false;
+        if (j < NP2) st = (j == 0) || (occ[j] / budget != occ[j - 1] / budget);
+        const unsigned bal = __ballot_sync(0xffffffffu, st);
+        if (lane == 0) warp_tmp[tid >> 5] = __popc(bal);
+        __syncthreads();
+        if (tid == 0) {
+          uint32_t run = s_nrounds;
+          for (int w2 = 0; w2 < nth / 32; w2++) { const uint32_t c = warp_tmp[w2]; warp_tmp[w2] = run; run += c; }
+          s_nrounds = run;
+        }
+        __syncthreads();
+        if (st) rstart[warp_tmp[tid >> 5] + __popc(bal & ((1u << lane) - 1u))] = (uint16_t)j;
+        __syncthreads();
+      }
+    }
+    const uint32_t nrounds = s_nrounds;
+
+    for (uint32_t r = 0; r < nrounds; r++) {
+      __syncthreads();
+      if (tid == 0) {
+        const uint32_t bl = rstart[r];
+        const uint32_t bh = (r + 1 < nrounds) ? rstart[r + 1] : (uint32_t)NP2;
+        stack[0] = RoundRange{bl, bh, 0u, 0xffffffffu};
+        s_sp = 1;
+      }
+      __syncthreads();
+      while (s_sp > 0) {
+        __syncthreads();
+        const RoundRange rr = stack[s_sp - 1];
+        __syncthreads();
+        if (tid == 0) { s_sp--; s_nused = 0; s_over = 0; }
+        const uint32_t dlo = dst[rr.bl], dhi = dst[rr.bh];
+        if (dhi == dlo) { __syncthreads(); continue; }
+        // clear the table
+        for (uint32_t i = tid; i < S; i += nth) {
+          keys[i] = EMPTY;
+          if (MODE == 0) cnt[i] = 0;
+          else for (int q = 0; q < W; q++) msk[(size_t)i * W + q] = 0ull;
+        }
+        __syncthreads();
+        const bool full_range = (rr.hlo == 0u && rr.hhi == 0xffffffffu);
+        // ---- insert: one thread per superkmer descriptor
+        for (uint64_t di = lo + dlo + tid; di < lo + dhi; di += nth) {
+          if (*(volatile uint32_t*)&s_over) break;
+          const uint64_t dsc = a.desc[di];
+          const uint64_t s0 = dsc >> 24;
+          const uint32_t nwin = (uint32_t)(dsc & 0xffffffu) + 1u;
+          uint32_t dset = 0;
+          if (MODE == 1) {
+            int l2 = 0, h2 = a.n_datasets;  // largest i with dsbase[i] <= s0
+            while (h2 - l2 > 1) { const int mid = (l2 + h2) >> 1; if (dsbase[mid] <= s0) l2 = mid; else h2 = mid; }
+            dset = (uint32_t)l2;
+          }
+          R roll;
+          roll.init(k);
+          if constexpr (sizeof(K) == 8) {
+            roll.set(field64(a.packed, s0, k), k);
+          } else {
+            if (k > 32) roll.set(field64(a.packed, s0, k - 32), field64(a.packed, s0 + (uint64_t)(k - 32), 32), k);
+            else roll.set(0ull, field64(a.packed, s0, k), k);
+          }
+          uint64_t p = s0 + (uint64_t)k;
+          uint32_t word = a.packed[p >> 4];
+          for (uint32_t j = 0; j < nwin; j++) {
+            if (j > 0) {
+              if ((p & 15) == 0) word = a.packed[p >> 4];
+              roll.push((word >> (30 - 2 * (uint32_t)(p & 15))) & 3u);
+              p++;
+            }
+            const K key = roll.canon();
+            const uint64_t hv = key_hash(key);
+            if (!full_range) {
+              const uint32_t hk = (uint32_t)(hv >> 32);
+              if (hk < rr.hlo || hk > rr.hhi) continue;
+            }
+            uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
+            bool done = false;
+            for (uint32_t probe = 0; probe < S; probe++) {
+              const K prev = KeyOps<K>::cas(&keys[s], EMPTY, key);
+              if (key_eq(prev, EMPTY) || key_eq(prev, key)) {
+                if (key_eq(prev, EMPTY)) {
+                  if (atomicAdd(&s_nused, 1u) + 1u > limit) s_over = 1;
+                }
+                if (MODE == 0) atomicAdd(&cnt[s], 1u);
+                else atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
+                done = true;
+                break;
+              }
+              s = (s + 1 == S) ? 0u : s + 1;
+            }
+            if (!done) { s_over = 1; break; }
+            if (*(volatile uint32_t*)&s_over) break;
+          }
+        }
+        __syncthreads();
+        if (s_over) {
+          if (tid == 0) {
+            if (rr.bh - rr.bl > 1) {
+              // split bins by occupancy midpoint
+              const uint32_t target = (occ[rr.bl] + occ[rr.bh]) / 2;
+              uint32_t mid = rr.bl + 1;
+              while (mid < rr.bh - 1 && occ[mid + 1] <= target) mid++;
+              if (s_sp + 2 <= MAX_STACK) {
+                stack[s_sp++] = RoundRange{mid, rr.bh, rr.hlo, rr.hhi};
+                stack[s_sp++] = RoundRange{rr.bl, mid, rr.hlo, rr.hhi};
+              } else set_status(a.status, ST_TABLE_STUCK);
+            } else if (rr.hhi > rr.hlo) {
+              const uint32_t hm = rr.hlo + (rr.hhi - rr.hlo) / 2;
+              if (s_sp + 2 <= MAX_STACK) {
+                stack[s_sp++] = RoundRange{rr.bl, rr.bh, hm + 1, rr.hhi};
+                stack[s_sp++] = RoundRange{rr.bl, rr.bh, rr.hlo, hm};
+              } else set_status(a.status, ST_TABLE_STUCK);
+            } else {
+              set_status(a.status, ST_TABLE_STUCK);
+            }
+            atomicAdd(&a.stats[3], 1ull);
+          }
+          __syncthreads();
+          continue;
+        }
+        // ---- emit slots with count > threshold
+        for (uint32_t base = 0; base < S; base += nth) {
+          const uint32_t s = base + tid;
+          bool emit = false;
+          uint32_t c = 0;
+          K key = EMPTY;
+          if (s < S) {
+            key = keys[s];
+            if (!key_eq(key, EMPTY)) {
+              c = MODE == 0 ? cnt[s] : popc_words(&msk[(size_t)s * W], W);
+              emit = (uint64_t)c > a.threshold;
+            }
+          }
+          const unsigned bal = __ballot_sync(0xffffffffu, emit);
+          if (bal) {
+            unsigned long long ob = 0;
+            const int leader = __ffs(bal) - 1;
+            if (lane == leader) ob = atomicAdd(a.n_out, (unsigned long long)__popc(bal));
+            ob = __shfl_sync(0xffffffffu, ob, leader);
+            if (emit) {
+              const unsigned long long idx = ob + __popc(bal & ((1u << lane) - 1u));
+              if (idx < a.out_cap) {
+                if constexpr (sizeof(K) == 8) {
+                  a.out_lo[idx] = reinterpret_cast<const K64&>(key).v;
+                } else {
+                  a.out_lo[idx] = reinterpret_cast<const K128&>(key).lo;
+                  a.out_hi[idx] = reinterpret_cast<const K128&>(key).hi;
+                }
+                a.out_count[idx] = c;
+              } else {
+                set_status(a.status, ST_OUT_OVERFLOW);
+              }
+            }
+          }
+        }
+        if (tid == 0) {
+          const double frac = ((double)rr.hhi - (double)rr.hlo + 1.0) / 4294967296.0;
+          atomicAdd(&a.stats[0], (unsigned long long)((double)(occ[rr.bh] - occ[rr.bl]) * frac));
+          atomicAdd(&a.stats[1], (unsigned long long)s_nused);
+          atomicAdd(&a.stats[2], 1ull);
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
+template <class K, class R, int MODE>
+static void launch_one(const CountArgs& a, cudaStream_t s) {
+  const size_t smem = count_smem_bytes(a.k, a.mode, a.n_datasets, a.table_slots);
+  cudaFuncSetAttribute(k_count<K, R, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_count<K, R, MODE><<<a.ctas, a.threads, smem, s>>>(a);
+}
+
+void launch_count(const CountArgs& a, cudaStream_t s) {
+  if (a.k <= 32) {
+    if (a.mode == 0) launch_one<K64, Roll64, 0>(a, s);
+    else launch_one<K64, Roll64, 1>(a, s);
+  } else {
+    if (a.mode == 0) launch_one<K128, Roll128, 0>(a, s);
+    else launch_one<K128, Roll128, 1>(a, s);
+  }
+}
+
+}  // namespace mczi

@@ -1,0 +1,311 @@
+// mc_pack.cu -- K1: FASTA/FASTQ bytes -> 2-bit packed base stream + fragment
+// start bits, on the device.
+//
+// Replaces helicase's `dna_packed().split_non_actg()` parse as MC uses it
+// (src/lib.rs:3264-3308): headers and quality lines are dropped, line breaks
+// inside a FASTA record are transparent, any byte other than A/C/G/T (either
+// case) ends the current fragment, and so does the start of a new record.
+// Fragments shorter than k are not removed here: the window scan never emits
+// a window that crosses a fragment start, so they simply contribute nothing.
+//
+// Layout: inputs are copied to HBM at offsets aligned to PACK_TILE bytes (the
+// gaps are filled with '\n').  Three passes over 8 KiB tiles:
+//   1. k_pack_lines : newline count and last newline per tile
+//   2. k_pack_count : bases and fragment-break summary per tile, given the
+//                     line state from the scan of pass 1
+//   3. k_pack_write : 2-bit codes and fragment-start bits, staged in shared
+//                     memory, interior words stored, edge words OR-ed.
+#include "mczi_internal.h"
+#include "scan.cuh"
+
+namespace mczi {
+
+namespace {
+
+enum : uint32_t { LS = 0, HDR = 1, SEQ = 2 };
+
+__device__ __forceinline__ int8_t code_of(uint32_t c) {
+  // A/a 0, C/c 1, G/g 2, T/t 3, else -1
+  switch (c | 0x20u) {
+    case 'a': return 0;
+    case 'c': return 1;
+    case 'g': return 2;
+    case 't': return 3;
+    default: return -1;
+  }
+}
+
+struct LineOp {
+  static __device__ LineSum identity() { return LineSum{-1, 0, 0, 0}; }
+  static __device__ LineSum combine(const LineSum& a, const LineSum& b) {
+    if (b.reset) return b;
+    return LineSum{a.last > b.last ? a.last : b.last, a.nl + b.nl, a.reset, 0};
+  }
+};
+
+struct BaseOp {
+  static __device__ BaseSum identity() { return BaseSum{0, 0, 0, 0}; }
+  static __device__ BaseSum combine(const BaseSum& a, const BaseSum& b) {
+    if (a.nb == 0 && b.nb == 0) return BaseSum{0, 0, a.lb | b.lb, 0};
+    if (a.nb == 0) return BaseSum{b.nb, a.lb | b.fb, b.lb, 0};
+    if (b.nb == 0) return BaseSum{a.nb, a.fb, a.lb | b.lb, 0};
+    return BaseSum{a.nb + b.nb, a.fb, b.lb, 0};
+  }
+};
+
+// per-thread newline summary, in-tile positions
+struct NlSum {
+  int32_t last;
+  uint32_t nl;
+};
+struct NlOp {
+  static __device__ NlSum identity() { return NlSum{-1, 0}; }
+  static __device__ NlSum combine(const NlSum& a, const NlSum& b) {
+    return NlSum{a.last > b.last ? a.last : b.last, a.nl + b.nl};
+  }
+};
+
+__device__ __forceinline__ void load_tile(const uint8_t* __restrict__ text, uint64_t tile, uint8_t* sb) {
+  const uint4* src = reinterpret_cast<const uint4*>(text + tile * PACK_TILE);
+  uint4* dst = reinterpret_cast<uint4*>(sb);
+#pragma unroll
+  for (int i = 0; i < PACK_TILE / 16 / PACK_THREADS; i++)
+    dst[threadIdx.x + i * PACK_THREADS] = src[threadIdx.x + i * PACK_THREADS];
+}
+
+// Line state at this thread's first byte.
+// FASTA: returns LS/HDR/SEQ.  FASTQ: returns the line index mod 4.
+__device__ __forceinline__ uint32_t thread_state(const uint8_t* sb, bool fastq, uint32_t tile_state,
+                                                 uint32_t tile_line4, int first) {
+  __shared__ NlSum sh[SCAN_THREADS + 1];
+  NlSum mine{-1, 0};
+  for (int i = 0; i < PACK_PER_THREAD; i++) {
+    if (sb[first + i] == '\n') {
+      mine.last = first + i;
+      mine.nl++;
+    }
+  }
+  NlSum tot;
+  NlSum pre = block_exclusive_scan<NlSum, NlOp>(mine, &tot, sh);
+  if (fastq) return (tile_line4 + pre.nl) & 3u;
+  if (pre.last >= 0) {
+    const int ls = pre.last + 1;
+    if (ls == first) return LS;
+    return sb[ls] == '>' ? HDR : SEQ;
+  }
+  if (tile_state == LS) {
+    if (first == 0) return LS;
+    return sb[0] == '>' ? HDR : SEQ;
+  }
+  return tile_state;
+}
+
+// Classify one byte.  Returns 0..3 for a base, 4 for a break, 5 for skip.
+__device__ __forceinline__ uint32_t step_fasta(uint32_t c, uint32_t& st) {
+  if (c == '\n') { st = LS; return 5; }
+  if (st == LS) {
+    if (c == '>') { st = HDR; return 4; }
+    st = SEQ;
+  }
+  if (st == HDR) return 4;
+  if (c == '\r') return 5;
+  int8_t code = code_of(c);
+  return code < 0 ? 4u : (uint32_t)code;
+}
+
+__device__ __forceinline__ uint32_t step_fastq(uint32_t c, uint32_t& line) {
+  if (c == '\n') {
+    uint32_t r = ((line & 3u) == 1u) ? 4u : 5u;  // end of a sequence line ends the fragment
+    line++;
+    return r;
+  }
+  if ((line & 3u) != 1u) return 4;
+  if (c == '\r') return 5;
+  int8_t code = code_of(c);
+  return code < 0 ? 4u : (uint32_t)code;
+}
+
+__device__ __forceinline__ void tile_line_state(const uint8_t* __restrict__ text, const uint32_t* __restrict__ tile_info,
+                                                const uint64_t* __restrict__ input_tile0, const LineSum* __restrict__ line_pre,
+                                                uint64_t tile, bool& fastq, uint32_t& st, uint32_t& line4) {
+  const uint32_t info = tile_info[tile];
+  fastq = (info >> 1) & 1u;
+  if (info & 1u) {  // input starts here
+    st = LS;
+    line4 = 0;
+    return;
+  }
+  const LineSum e = line_pre[tile];
+  line4 = (uint32_t)(e.nl & 3u);
+  const uint64_t p0 = tile * PACK_TILE;
+  uint64_t ls;
+  if (e.last >= 0) ls = (uint64_t)e.last + 1;
+  else ls = input_tile0[info >> 2] * PACK_TILE;
+  if (ls == p0) st = LS;
+  else st = (text[ls] == '>') ? HDR : SEQ;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(PACK_THREADS) k_pack_lines(const uint8_t* __restrict__ text,
+                                                             const uint32_t* __restrict__ tile_info,
+                                                             uint64_t n_tiles, LineSum* __restrict__ out) {
+  const uint64_t tile = blockIdx.x;
+  if (tile >= n_tiles) return;
+  const uint4* src = reinterpret_cast<const uint4*>(text + tile * PACK_TILE);
+  int32_t last = -1;
+  uint32_t nl = 0;
+#pragma unroll
+  for (int i = 0; i < PACK_TILE / 16 / PACK_THREADS; i++) {
+    const int vi = threadIdx.x + i * PACK_THREADS;
+    uint4 v = src[vi];
+    uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+#pragma unroll
+      for (int b = 0; b < 4; b++) {
+        if (((w[j] >> (8 * b)) & 0xffu) == '\n') {
+          nl++;
+          last = vi * 16 + j * 4 + b;
+        }
+      }
+    }
+  }
+  // block reduce
+  for (int o = 16; o > 0; o >>= 1) {
+    nl += __shfl_down_sync(0xffffffffu, nl, o);
+    int32_t l2 = __shfl_down_sync(0xffffffffu, last, o);
+    last = l2 > last ? l2 : last;
+  }
+  __shared__ uint32_t snl[PACK_THREADS / 32];
+  __shared__ int32_t slast[PACK_THREADS / 32];
+  if ((threadIdx.x & 31) == 0) {
+    snl[threadIdx.x >> 5] = nl;
+    slast[threadIdx.x >> 5] = last;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t n = 0;
+    int32_t l = -1;
+    for (int i = 0; i < PACK_THREADS / 32; i++) {
+      n += snl[i];
+      l = slast[i] > l ? slast[i] : l;
+    }
+    LineSum s;
+    s.last = l >= 0 ? (int64_t)(tile * PACK_TILE + (uint64_t)l) : -1;
+    s.nl = n;
+    s.reset = tile_info[tile] & 1u;
+    s.pad = 0;
+    out[tile] = s;
+  }
+}
+
+__global__ void __launch_bounds__(PACK_THREADS) k_pack_count(const uint8_t* __restrict__ text,
+                                                             const uint32_t* __restrict__ tile_info,
+                                                             const uint64_t* __restrict__ input_tile0,
+                                                             const LineSum* __restrict__ line_pre, uint64_t n_tiles,
+                                                             BaseSum* __restrict__ out) {
+  __shared__ __align__(16) uint8_t sb[PACK_TILE];
+  __shared__ BaseSum shs[SCAN_THREADS + 1];
+  const uint64_t tile = blockIdx.x;
+  if (tile >= n_tiles) return;
+  load_tile(text, tile, sb);
+  bool fastq;
+  uint32_t tst, tl4;
+  tile_line_state(text, tile_info, input_tile0, line_pre, tile, fastq, tst, tl4);
+  __syncthreads();
+  const int first = threadIdx.x * PACK_PER_THREAD;
+  uint32_t st = thread_state(sb, fastq, tst, tl4, first);
+  BaseSum s{0, 0, 0, 0};
+  for (int i = 0; i < PACK_PER_THREAD; i++) {
+    uint32_t c = sb[first + i];
+    uint32_t r = fastq ? step_fastq(c, st) : step_fasta(c, st);
+    if (r < 4) { s.nb++; s.lb = 0; }
+    else if (r == 4) { if (s.nb == 0) s.fb = 1; s.lb = 1; }
+  }
+  // for nb == 0 lb means "any break"; for nb > 0 fb is a break before the first base
+  BaseSum tot;
+  block_exclusive_scan<BaseSum, BaseOp>(s, &tot, shs);
+  if (threadIdx.x == 0) out[tile] = tot;
+}
+
+__global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __restrict__ text,
+                                                             const uint32_t* __restrict__ tile_info,
+                                                             const uint64_t* __restrict__ input_tile0,
+                                                             const LineSum* __restrict__ line_pre,
+                                                             const BaseSum* __restrict__ base_pre, uint64_t n_tiles,
+                                                             uint32_t* __restrict__ packed, uint32_t* __restrict__ fbits,
+                                                             uint64_t* __restrict__ input_base) {
+  __shared__ __align__(16) uint8_t sb[PACK_TILE];
+  __shared__ BaseSum shs[SCAN_THREADS + 1];
+  __shared__ uint32_t spk[PACK_TILE / 16 + 2];
+  __shared__ uint32_t sfb[PACK_TILE / 32 + 2];
+  const uint64_t tile = blockIdx.x;
+  if (tile >= n_tiles) return;
+  load_tile(text, tile, sb);
+  for (int i = threadIdx.x; i < PACK_TILE / 16 + 2; i += PACK_THREADS) spk[i] = 0;
+  for (int i = threadIdx.x; i < PACK_TILE / 32 + 2; i += PACK_THREADS) sfb[i] = 0;
+  bool fastq;
+  uint32_t tst, tl4;
+  tile_line_state(text, tile_info, input_tile0, line_pre, tile, fastq, tst, tl4);
+  __syncthreads();
+  const int first = threadIdx.x * PACK_PER_THREAD;
+  const uint32_t st0 = thread_state(sb, fastq, tst, tl4, first);
+  // pass A: this thread's summary
+  uint32_t st = st0;
+  BaseSum s{0, 0, 0, 0};
+  for (int i = 0; i < PACK_PER_THREAD; i++) {
+    uint32_t r = fastq ? step_fastq(sb[first + i], st) : step_fasta(sb[first + i], st);
+    if (r < 4) { s.nb++; s.lb = 0; }
+    else if (r == 4) { if (s.nb == 0) s.fb = 1; s.lb = 1; }
+  }
+  BaseSum tot;
+  const BaseSum tile_pre = base_pre[tile];
+  BaseSum excl = BaseOp::combine(tile_pre, block_exclusive_scan<BaseSum, BaseOp>(s, &tot, shs));
+  if (threadIdx.x == 0 && (tile_info[tile] & 1u)) input_base[tile_info[tile] >> 2] = tile_pre.nb;
+  // pass B: write codes and start bits into the staging buffers
+  const uint64_t tb = tile_pre.nb;        // first base of this tile
+  const uint64_t w0 = tb >> 4, f0 = tb >> 5;
+  uint64_t p = excl.nb;
+  uint32_t pending = (excl.nb == 0) ? 1u : excl.lb;
+  st = st0;
+  for (int i = 0; i < PACK_PER_THREAD; i++) {
+    uint32_t r = fastq ? step_fastq(sb[first + i], st) : step_fasta(sb[first + i], st);
+    if (r < 4) {
+      atomicOr(&spk[(p >> 4) - w0], r << (30 - 2 * (uint32_t)(p & 15)));
+      if (pending) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
+      pending = 0;
+      p++;
+    } else if (r == 4) {
+      pending = 1;
+    }
+  }
+  __syncthreads();
+  const uint64_t nb = tot.nb;
+  if (nb == 0) return;
+  const uint64_t wl = (tb + nb - 1) >> 4, fl = (tb + nb - 1) >> 5;
+  for (uint64_t w = w0 + threadIdx.x; w <= wl; w += PACK_THREADS) {
+    uint32_t v = spk[w - w0];
+    if (w == w0 || w == wl) atomicOr(&packed[w], v);
+    else packed[w] = v;
+  }
+  for (uint64_t f = f0 + threadIdx.x; f <= fl; f += PACK_THREADS) {
+    uint32_t v = sfb[f - f0];
+    if (f == f0 || f == fl) { if (v) atomicOr(&fbits[f], v); }
+    else fbits[f] = v;
+  }
+}
+
+void launch_pack(const PackArgs& a, cudaStream_t s) {
+  if (a.n_tiles == 0) return;
+  k_pack_lines<<<(unsigned)a.n_tiles, PACK_THREADS, 0, s>>>(a.text, a.tile_info, a.n_tiles, a.line_sum);
+  exclusive_scan<LineSum, LineOp>(a.line_sum, a.line_pre, a.n_tiles, a.line_tmp, s);
+  k_pack_count<<<(unsigned)a.n_tiles, PACK_THREADS, 0, s>>>(a.text, a.tile_info, a.input_tile0, a.line_pre,
+                                                             a.n_tiles, a.base_sum);
+  exclusive_scan<BaseSum, BaseOp>(a.base_sum, a.base_pre, a.n_tiles, a.base_tmp, s);
+  k_pack_write<<<(unsigned)a.n_tiles, PACK_THREADS, 0, s>>>(a.text, a.tile_info, a.input_tile0, a.line_pre,
+                                                             a.base_pre, a.n_tiles, a.packed, a.fbits,
+                                                             a.input_base);
+}
+
+}  // namespace mczi

@@ -1,0 +1,654 @@
+// mczi_api.cu -- context, device-memory management, MC pipeline orchestration
+// and the C ABI declared in include/mczi_gpu.h.
+//
+// The MC pipeline on one GPU (all intermediate data stays in HBM; the
+// reference round-trips it through temporary partition files):
+//   stage   : inputs -> HBM, each at a PACK_TILE-aligned offset
+//   K1 pack : bytes -> 2-bit packed stream + fragment-start bits
+//   K2 scan : minimizer scan -> superkmer descriptors + partition keys
+//   K3 part : two-digit radix partition of the descriptors
+//   K5 count: per-bucket shared-memory counting, threshold, records out
+// Entry points mirror MC's library functions (src/lib.rs:278-524).
+#include "../../include/mczi_gpu.h"
+#include "host_io.h"
+#include "mczi_internal.h"
+#include "mczi_common.cuh"
+#include "scan.cuh"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+using namespace mczi;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+// device scalars, in u64 slots
+enum { SC_NDESC = 0, SC_NOUT = 1, SC_STATS = 2, SC_STATUS = 10, SC_WORK = 11, SC_COUNT = 16 };
+
+constexpr int N_PHASES = 5;
+
+}  // namespace
+
+struct mczi_ctx {
+  int device = 0;
+  int sm_count = 0;
+  size_t smem_optin = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  DevBuf text, tile_info, input_tile0, line_sum, line_pre, line_tmp, base_sum, base_pre, base_tmp;
+  DevBuf packed, fbits, input_base;
+  DevBuf desc, key, desc2, key2, part_hist, part_tmp, bucket_off;
+  DevBuf out_lo, out_hi, out_cnt;
+  DevBuf scalars;
+
+  // staged inputs
+  bool staged = false;
+  uint64_t text_len = 0, n_tiles = 0;
+  int n_inputs = 0;
+  uint64_t skipped = 0;
+
+  // last result
+  bool have_result = false;
+  int mode = 0, k = 0, m = 0;
+  uint64_t x = 0;
+  uint64_t n_out = 0;
+  float phase_ms[N_PHASES] = {0, 0, 0, 0, 0};
+  uint64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  cudaEvent_t ev[N_PHASES + 1] = {};
+
+  // tuning
+  int count_threads = 512;
+  int count_slots = 0;
+  int count_ctas_per_sm = 2;
+  float count_fill = 0.6f;
+};
+
+namespace {
+
+int32_t fail(mczi_ctx* c, int32_t code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int32_t cuda_fail(mczi_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, MCZI_ERR_DEVICE, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                         \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+#define CKA(buf, bytes)                                                                 \
+  do {                                                                                  \
+    cudaError_t e_ = (buf).ensure(bytes);                                               \
+    if (e_ != cudaSuccess) {                                                            \
+      cudaGetLastError();                                                               \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? MCZI_ERR_OOM : MCZI_ERR_DEVICE, \
+                  std::string("device allocation of ") + std::to_string(bytes) +      \
+                      " bytes failed: " + cudaGetErrorString(e_));                     \
+    }                                                                                   \
+  } while (0)
+
+// reference messages: src/lib.rs:110-152
+int32_t validate(mczi_ctx* ctx, const mczi_counter_config* c, int mode) {
+  if (!c) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "missing config");
+  if (c->k == 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "k must be greater than 0");
+  if (c->k > 64) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "k must be <= 64 because MC stores k-mers in u128");
+  if (c->minimizer == 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "minimizer size must be greater than 0");
+  if (c->minimizer > c->k) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "minimizer size must be <= k");
+  if (c->minimizer > 64)
+    return fail(ctx, MCZI_ERR_INVALID_CONFIG, "minimizer size must be <= 64 because MC stores minimizers in u128");
+  if (c->partition_count == 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "partition count must be greater than 0");
+  if (mode == MCZI_MODE_ABUNDANCE) {
+    if (c->threshold >= 255)
+      return fail(ctx, MCZI_ERR_INVALID_CONFIG,
+                  "threshold must be < 255 because compact minimizer counts saturate in u8");
+  } else if (mode == MCZI_MODE_PRESENCE) {
+    if (c->k > 32) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "FOFN dataset-presence mode currently requires k <= 32");
+    if (c->threshold >= 0x7fffffffull)
+      return fail(ctx, MCZI_ERR_INVALID_CONFIG, "FOFN dataset-presence threshold must be < 2^31");
+  } else {
+    return fail(ctx, MCZI_ERR_INVALID_CONFIG, "unknown counting mode");
+  }
+  return MCZI_OK;
+}
+
+// first non-newline byte: '>' FASTA, '@' FASTQ, otherwise not a FASTX record start
+int detect_format(const uint8_t* d, uint64_t n) {
+  uint64_t i = 0;
+  while (i < n && (d[i] == '\n' || d[i] == '\r')) i++;
+  if (i >= n) return 2;  // empty: contributes nothing
+  if (d[i] == '>') return 0;
+  if (d[i] == '@') return 1;
+  return -1;
+}
+
+int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n) {
+  ctx->staged = false;
+  ctx->have_result = false;
+  if (n == 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "at least one input file is required");
+  std::vector<uint64_t> off(n), len(n);
+  std::vector<int> fmt(n);
+  uint64_t pos = 0;
+  ctx->skipped = 0;
+  for (size_t i = 0; i < n; i++) {
+    const uint8_t* d = inputs[i].data;
+    uint64_t l = d ? inputs[i].len : 0;
+    int f = detect_format(d, l);
+    if (f < 0) {
+      std::fprintf(stderr, "MC_WARN\tskipped_invalid_fastx_input\tinput\t%zu\terror\tInvalid record start\n", i);
+      ctx->skipped++;
+      l = 0;
+      f = 0;
+    }
+    if (f == 2) { l = 0; f = 0; }
+    off[i] = pos;
+    len[i] = l;
+    fmt[i] = f;
+    const uint64_t tiles = l == 0 ? 1 : (l + PACK_TILE - 1) / PACK_TILE;  // every input owns >= 1 tile
+    pos += tiles * PACK_TILE;
+  }
+  const uint64_t text_len = pos;
+  const uint64_t n_tiles = text_len / PACK_TILE;
+  std::vector<uint32_t> tinfo(n_tiles);
+  std::vector<uint64_t> tile0(n);
+  for (size_t i = 0; i < n; i++) {
+    const uint64_t t0 = off[i] / PACK_TILE;
+    const uint64_t t1 = (i + 1 < n ? off[i + 1] : text_len) / PACK_TILE;
+    tile0[i] = t0;
+    for (uint64_t t = t0; t < t1; t++) tinfo[t] = ((uint32_t)i << 2) | ((uint32_t)fmt[i] << 1) | (t == t0 ? 1u : 0u);
+  }
+  CKA(ctx->text, text_len);
+  CKA(ctx->tile_info, n_tiles * sizeof(uint32_t));
+  CKA(ctx->input_tile0, n * sizeof(uint64_t));
+  cudaStream_t s = ctx->stream;
+  for (size_t i = 0; i < n; i++) {
+    uint8_t* dst = ctx->text.as<uint8_t>() + off[i];
+    if (len[i]) CK(cudaMemcpyAsync(dst, inputs[i].data, len[i], cudaMemcpyHostToDevice, s));
+    const uint64_t end = i + 1 < n ? off[i + 1] : text_len;
+    if (off[i] + len[i] < end) CK(cudaMemsetAsync(dst + len[i], '\n', end - off[i] - len[i], s));
+  }
+  CK(cudaMemcpyAsync(ctx->tile_info.p, tinfo.data(), n_tiles * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ctx->input_tile0.p, tile0.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+  // the host vectors above are pageable: the copies complete before return
+  CK(cudaStreamSynchronize(s));
+  ctx->text_len = text_len;
+  ctx->n_tiles = n_tiles;
+  ctx->n_inputs = (int)n;
+  ctx->staged = true;
+  return MCZI_OK;
+}
+
+int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint64_t* n_records) {
+  int32_t rc = validate(ctx, cfg, mode);
+  if (rc) return rc;
+  if (!ctx->staged) return fail(ctx, MCZI_ERR_STATE, "no staged inputs");
+  ctx->have_result = false;
+  cudaStream_t s = ctx->stream;
+  const int k = (int)cfg->k, m = (int)cfg->minimizer, w = k - m + 1;
+  const uint64_t n_tiles = ctx->n_tiles, text_len = ctx->text_len;
+  const int n_in = ctx->n_inputs;
+
+  CKA(ctx->scalars, SC_COUNT * sizeof(uint64_t));
+  uint64_t* sc = ctx->scalars.as<uint64_t>();
+  CK(cudaMemsetAsync(sc, 0, SC_COUNT * sizeof(uint64_t), s));
+
+  for (int i = 0; i < N_PHASES; i++) ctx->phase_ms[i] = 0.f;
+
+  // fof: the reference returns an empty result when x >= #datasets (src/lib.rs:644-648)
+  if (mode == MCZI_MODE_PRESENCE && cfg->threshold >= (uint64_t)n_in) {
+    ctx->mode = mode; ctx->k = k; ctx->m = m; ctx->x = cfg->threshold;
+    ctx->n_out = 0;
+    std::memset(ctx->stats, 0, sizeof ctx->stats);
+    ctx->have_result = true;
+    if (n_records) *n_records = 0;
+    return MCZI_OK;
+  }
+
+  // ---- K1 pack
+  const uint64_t pwords = text_len / 16 + 8, fwords = text_len / 32 + 8;
+  const uint64_t ntmp = n_tiles / SCAN_CHUNK + 2;
+  CKA(ctx->packed, pwords * 4);
+  CKA(ctx->fbits, fwords * 4);
+  CKA(ctx->line_sum, (n_tiles + 1) * sizeof(LineSum));
+  CKA(ctx->line_pre, (n_tiles + 1) * sizeof(LineSum));
+  CKA(ctx->line_tmp, ntmp * sizeof(LineSum));
+  CKA(ctx->base_sum, (n_tiles + 1) * sizeof(BaseSum));
+  CKA(ctx->base_pre, (n_tiles + 1) * sizeof(BaseSum));
+  CKA(ctx->base_tmp, ntmp * sizeof(BaseSum));
+  CKA(ctx->input_base, ((size_t)n_in + 1) * sizeof(uint64_t));
+  CK(cudaMemsetAsync(ctx->packed.p, 0, pwords * 4, s));
+  CK(cudaMemsetAsync(ctx->fbits.p, 0, fwords * 4, s));
+
+  CK(cudaEventRecord(ctx->ev[0], s));
+  PackArgs pa;
+  pa.text = ctx->text.as<uint8_t>();
+  pa.tile_info = ctx->tile_info.as<uint32_t>();
+  pa.input_tile0 = ctx->input_tile0.as<uint64_t>();
+  pa.n_tiles = n_tiles;
+  pa.line_sum = ctx->line_sum.as<LineSum>();
+  pa.line_pre = ctx->line_pre.as<LineSum>();
+  pa.line_tmp = ctx->line_tmp.as<LineSum>();
+  pa.base_sum = ctx->base_sum.as<BaseSum>();
+  pa.base_pre = ctx->base_pre.as<BaseSum>();
+  pa.base_tmp = ctx->base_tmp.as<BaseSum>();
+  pa.packed = ctx->packed.as<uint32_t>();
+  pa.fbits = ctx->fbits.as<uint32_t>();
+  pa.input_base = ctx->input_base.as<uint64_t>();
+  launch_pack(pa, s);
+  const uint64_t* d_nbases = reinterpret_cast<const uint64_t*>(ctx->base_pre.as<BaseSum>() + n_tiles);
+  CK(cudaMemcpyAsync(ctx->input_base.as<uint64_t>() + n_in, d_nbases, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->ev[1], s));
+
+  // ---- K2 scan (+ retry on descriptor overflow)
+  uint64_t desc_cap = text_len * 3 / (uint64_t)(w + 1) + (1u << 20);
+  if (desc_cap > text_len + 1024) desc_cap = text_len + 1024;
+  for (int attempt = 0; attempt < 3; attempt++) {
+    if (desc_cap >= 0xffffffffull) return fail(ctx, MCZI_ERR_OOM, "input batch too large: more than 2^32 superkmers");
+    CKA(ctx->desc, desc_cap * 8);
+    CKA(ctx->key, desc_cap * 4);
+    CK(cudaMemsetAsync(sc + SC_NDESC, 0, 8, s));
+    CK(cudaMemsetAsync(sc + SC_STATUS, 0, 8, s));
+    ScanArgs sa;
+    sa.packed = ctx->packed.as<uint32_t>();
+    sa.fbits = ctx->fbits.as<uint32_t>();
+    sa.n_bases = d_nbases;
+    sa.max_bases = text_len;
+    sa.packed_words = pwords;
+    sa.k = k;
+    sa.m = m;
+    sa.desc = ctx->desc.as<uint64_t>();
+    sa.key = ctx->key.as<uint32_t>();
+    sa.n_desc = reinterpret_cast<unsigned long long*>(sc + SC_NDESC);
+    sa.desc_cap = desc_cap;
+    sa.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
+    launch_scan(sa, s);
+    CK(cudaGetLastError());
+    uint64_t h[2];
+    CK(cudaMemcpyAsync(h, sc + SC_NDESC, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h + 1, sc + SC_STATUS, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (!(h[1] & ST_DESC_OVERFLOW)) {
+      ctx->stats[1] = h[0];
+      break;
+    }
+    desc_cap = h[0] + 1024;
+    if (attempt == 2) return fail(ctx, MCZI_ERR_DEVICE, "descriptor buffer overflow persisted");
+  }
+  CK(cudaEventRecord(ctx->ev[2], s));
+  const uint64_t n_desc = ctx->stats[1];
+
+  // ---- K3 partition
+  CKA(ctx->desc2, desc_cap * 8);
+  CKA(ctx->key2, desc_cap * 4);
+  const uint64_t nh = (uint64_t)NP1 * PART_CTAS;
+  CKA(ctx->part_hist, (2 * nh + 2) * sizeof(uint32_t));
+  CKA(ctx->part_tmp, (nh / SCAN_CHUNK + 2) * sizeof(uint32_t));
+  CKA(ctx->bucket_off, (NP1 + 1) * sizeof(uint64_t));
+  PartArgs qa;
+  qa.desc_in = ctx->desc.as<uint64_t>();
+  qa.key_in = ctx->key.as<uint32_t>();
+  qa.desc_out = ctx->desc2.as<uint64_t>();
+  qa.key_out = ctx->key2.as<uint32_t>();
+  qa.n_desc = reinterpret_cast<const unsigned long long*>(sc + SC_NDESC);
+  qa.desc_cap = desc_cap;
+  qa.hist = ctx->part_hist.as<uint32_t>();
+  qa.hist_tmp = ctx->part_tmp.as<uint32_t>();
+  qa.bucket_off = ctx->bucket_off.as<uint64_t>();
+  qa.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
+  if (n_desc > 0) launch_partition(qa, s);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->ev[3], s));
+
+  // ---- K5 count (+ retry on result overflow)
+  const bool wide = k > 32;
+  const uint64_t est_out = text_len / (cfg->threshold + 1) + 1024;
+  uint64_t out_cap = std::min<uint64_t>(est_out, 1ull << 25);
+  uint64_t n_out = 0;
+  if (n_desc > 0) {
+    int threads = ctx->count_threads;
+    int cps = ctx->count_ctas_per_sm;
+    const size_t budget = ctx->smem_optin;  // per block, opt-in
+    const size_t fixed = count_fixed_smem_bytes(mode, n_in);
+    const size_t slotb = count_slot_bytes(k, mode, n_in);
+    // shared memory per SM is ~228 KiB; leave 1 KiB per CTA for the runtime
+    size_t per_cta = std::min(budget, (size_t)(228 * 1024) / (size_t)cps - 1024);
+    uint32_t slots = ctx->count_slots > 0 ? (uint32_t)ctx->count_slots
+                                           : (uint32_t)((per_cta - fixed - 64) / slotb);
+    if (slots < (uint32_t)threads) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "counting table smaller than the CTA");
+    if (count_smem_bytes(k, mode, n_in, slots) > budget)
+      return fail(ctx, MCZI_ERR_INVALID_CONFIG, "counting table does not fit in shared memory");
+    for (int attempt = 0; attempt < 3; attempt++) {
+      CKA(ctx->out_lo, out_cap * 8);
+      if (wide) CKA(ctx->out_hi, out_cap * 8);
+      CKA(ctx->out_cnt, out_cap * 4);
+      CK(cudaMemsetAsync(sc + SC_NOUT, 0, 8, s));
+      CK(cudaMemsetAsync(sc + SC_STATS, 0, 8 * 8, s));
+      CK(cudaMemsetAsync(sc + SC_STATUS, 0, 8, s));
+      CK(cudaMemsetAsync(sc + SC_WORK, 0, 8, s));
+      CountArgs ca;
+      ca.packed = ctx->packed.as<uint32_t>();
+      ca.desc = ctx->desc.as<uint64_t>();
+      ca.key = ctx->key.as<uint32_t>();
+      ca.bucket_off = ctx->bucket_off.as<uint64_t>();
+      ca.k = k;
+      ca.threshold = cfg->threshold;
+      ca.mode = mode;
+      ca.dataset_base = ctx->input_base.as<uint64_t>();
+      ca.n_datasets = n_in;
+      ca.out_lo = ctx->out_lo.as<uint64_t>();
+      ca.out_hi = wide ? ctx->out_hi.as<uint64_t>() : nullptr;
+      ca.out_count = ctx->out_cnt.as<uint32_t>();
+      ca.n_out = reinterpret_cast<unsigned long long*>(sc + SC_NOUT);
+      ca.out_cap = out_cap;
+      ca.stats = reinterpret_cast<unsigned long long*>(sc + SC_STATS);
+      ca.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
+      ca.table_slots = slots;
+      ca.threads = threads;
+      ca.ctas = ctx->sm_count * cps;
+      ca.work_counter = reinterpret_cast<unsigned int*>(sc + SC_WORK);
+      ca.fill = ctx->count_fill;
+      launch_count(ca, s);
+      CK(cudaGetLastError());
+      uint64_t h[SC_COUNT];
+      CK(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      const uint32_t st = (uint32_t)h[SC_STATUS];
+      if (st & ST_TABLE_STUCK) return fail(ctx, MCZI_ERR_DEVICE, "counting round could not be split further");
+      if (st & ST_OUT_OVERFLOW) {
+        out_cap = h[SC_NOUT] + 1024;
+        continue;
+      }
+      n_out = h[SC_NOUT];
+      ctx->stats[2] = h[SC_STATS + 2];
+      ctx->stats[3] = h[SC_STATS + 3];
+      ctx->stats[4] = h[SC_STATS + 1];
+      ctx->stats[6] = h[SC_STATS + 0];
+      break;
+    }
+  }
+  CK(cudaEventRecord(ctx->ev[4], s));
+  CK(cudaEventRecord(ctx->ev[5], s));
+  CK(cudaStreamSynchronize(s));
+  for (int i = 0; i < 4; i++) CK(cudaEventElapsedTime(&ctx->phase_ms[i], ctx->ev[i], ctx->ev[i + 1]));
+  uint64_t nb = 0;
+  CK(cudaMemcpy(&nb, d_nbases, 8, cudaMemcpyDeviceToHost));
+  ctx->stats[0] = nb;
+  ctx->stats[5] = n_out;
+  ctx->stats[7] = ctx->skipped;
+  ctx->mode = mode;
+  ctx->k = k;
+  ctx->m = m;
+  ctx->x = cfg->threshold;
+  ctx->n_out = n_out;
+  ctx->have_result = true;
+  if (n_records) *n_records = n_out;
+  return MCZI_OK;
+}
+
+int32_t fetch_records(mczi_ctx* ctx, HostRecords* r) {
+  const uint64_t n = ctx->n_out;
+  r->lo.resize(n);
+  r->count.resize(n);
+  if (ctx->k > 32) r->hi.resize(n);
+  else r->hi.clear();
+  if (n == 0) return MCZI_OK;
+  std::vector<uint32_t> c32(n);
+  CK(cudaMemcpyAsync(r->lo.data(), ctx->out_lo.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  if (ctx->k > 32) CK(cudaMemcpyAsync(r->hi.data(), ctx->out_hi.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(c32.data(), ctx->out_cnt.p, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (uint64_t i = 0; i < n; i++) r->count[i] = c32[i];
+  return MCZI_OK;
+}
+
+int32_t count_paths(mczi_ctx* ctx, const char* const* paths, size_t n, const mczi_counter_config* cfg, int mode,
+                    const char* out, bool kff) {
+  if (!ctx) return MCZI_ERR_STATE;
+  int32_t rc = validate(ctx, cfg, mode);
+  if (rc) return rc;
+  if (n == 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, mode ? "at least one dataset file is required"
+                                                              : "at least one input file is required");
+  std::vector<std::vector<uint8_t>> data(n);
+  std::vector<mczi_input> in(n);
+  for (size_t i = 0; i < n; i++) {
+    std::string e;
+    if (!read_file(paths[i], &data[i], &e)) return fail(ctx, MCZI_ERR_IO, e);
+    in[i].data = data[i].data();
+    in[i].len = data[i].size();
+  }
+  rc = mczi_count(ctx, cfg, mode, in.data(), n, nullptr);
+  if (rc) return rc;
+  return kff ? mczi_result_write_kff(ctx, out) : mczi_result_write_fasta(ctx, out);
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t mczi_open(int32_t device, mczi_ctx** out) {
+  if (!out) return MCZI_ERR_STATE;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return MCZI_ERR_DEVICE;
+  }
+  if (device < 0 || device >= n) return MCZI_ERR_DEVICE;
+  if (cudaSetDevice(device) != cudaSuccess) return MCZI_ERR_DEVICE;
+  mczi_ctx* ctx = new mczi_ctx();
+  ctx->device = device;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+    delete ctx;
+    return MCZI_ERR_DEVICE;
+  }
+  ctx->sm_count = prop.multiProcessorCount;
+  ctx->smem_optin = prop.sharedMemPerBlockOptin;
+  if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return MCZI_ERR_DEVICE;
+  }
+  ctx->stream = ctx->own_stream;
+  for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+  *out = ctx;
+  return MCZI_OK;
+}
+
+int32_t mczi_close(mczi_ctx* ctx) {
+  if (!ctx) return MCZI_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  DevBuf* bufs[] = {&ctx->text, &ctx->tile_info, &ctx->input_tile0, &ctx->line_sum, &ctx->line_pre, &ctx->line_tmp,
+                    &ctx->base_sum, &ctx->base_pre, &ctx->base_tmp, &ctx->packed, &ctx->fbits, &ctx->input_base,
+                    &ctx->desc, &ctx->key, &ctx->desc2, &ctx->key2, &ctx->part_hist, &ctx->part_tmp,
+                    &ctx->bucket_off, &ctx->out_lo, &ctx->out_hi, &ctx->out_cnt, &ctx->scalars};
+  for (DevBuf* b : bufs) b->release();
+  for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return MCZI_OK;
+}
+
+const char* mczi_last_error(const mczi_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int32_t mczi_set_stream(mczi_ctx* ctx, void* stream) {
+  if (!ctx) return MCZI_ERR_STATE;
+  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  return MCZI_OK;
+}
+
+int32_t mczi_validate_config(mczi_ctx* ctx, const mczi_counter_config* cfg, int32_t mode) {
+  return validate(ctx, cfg, mode);
+}
+
+int32_t mczi_stage(mczi_ctx* ctx, const mczi_input* inputs, size_t n_inputs) {
+  if (!ctx) return MCZI_ERR_STATE;
+  cudaSetDevice(ctx->device);
+  return stage_inputs(ctx, inputs, n_inputs);
+}
+
+int32_t mczi_count_staged(mczi_ctx* ctx, const mczi_counter_config* cfg, int32_t mode, uint64_t* n_records) {
+  if (!ctx) return MCZI_ERR_STATE;
+  cudaSetDevice(ctx->device);
+  return run_count(ctx, cfg, mode, n_records);
+}
+
+int32_t mczi_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int32_t mode, const mczi_input* inputs,
+                   size_t n_inputs, uint64_t* n_records) {
+  if (!ctx) return MCZI_ERR_STATE;
+  cudaSetDevice(ctx->device);
+  int32_t rc = validate(ctx, cfg, mode);
+  if (rc) return rc;
+  rc = stage_inputs(ctx, inputs, n_inputs);
+  if (rc) return rc;
+  return run_count(ctx, cfg, mode, n_records);
+}
+
+int32_t mczi_result_copy(mczi_ctx* ctx, uint64_t* key_lo, uint64_t* key_hi, uint64_t* counts, uint64_t cap,
+                         int32_t sorted) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (!ctx->have_result) return fail(ctx, MCZI_ERR_STATE, "no result");
+  if (cap < ctx->n_out) return fail(ctx, MCZI_ERR_STATE, "result buffer too small");
+  cudaSetDevice(ctx->device);
+  HostRecords r;
+  int32_t rc = fetch_records(ctx, &r);
+  if (rc) return rc;
+  const uint64_t n = ctx->n_out;
+  std::vector<uint64_t> idx(n);
+  std::iota(idx.begin(), idx.end(), 0ull);
+  if (sorted) {
+    if (r.hi.empty()) std::sort(idx.begin(), idx.end(), [&](uint64_t a, uint64_t b) { return r.lo[a] < r.lo[b]; });
+    else
+      std::sort(idx.begin(), idx.end(), [&](uint64_t a, uint64_t b) {
+        return r.hi[a] < r.hi[b] || (r.hi[a] == r.hi[b] && r.lo[a] < r.lo[b]);
+      });
+  }
+  for (uint64_t i = 0; i < n; i++) {
+    const uint64_t j = idx[i];
+    if (key_lo) key_lo[i] = r.lo[j];
+    if (key_hi) key_hi[i] = r.hi.empty() ? 0 : r.hi[j];
+    if (counts) counts[i] = r.count[j];
+  }
+  return MCZI_OK;
+}
+
+int32_t mczi_result_write_kff(mczi_ctx* ctx, const char* path) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (!ctx->have_result) return fail(ctx, MCZI_ERR_STATE, "no result");
+  cudaSetDevice(ctx->device);
+  HostRecords r;
+  int32_t rc = fetch_records(ctx, &r);
+  if (rc) return rc;
+  const int count_size = ctx->mode == MCZI_MODE_PRESENCE ? 4 : (ctx->k <= 32 ? 1 : 8);
+  std::string e;
+  if (!write_kff_file(path, r, ctx->k, ctx->m, ctx->x, count_size, &e)) return fail(ctx, MCZI_ERR_IO, e);
+  return MCZI_OK;
+}
+
+int32_t mczi_result_write_fasta(mczi_ctx* ctx, const char* path) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (!ctx->have_result) return fail(ctx, MCZI_ERR_STATE, "no result");
+  cudaSetDevice(ctx->device);
+  HostRecords r;
+  int32_t rc = fetch_records(ctx, &r);
+  if (rc) return rc;
+  std::string e;
+  if (!write_simplitig_file(path, r, ctx->k, &e)) return fail(ctx, MCZI_ERR_IO, e);
+  return MCZI_OK;
+}
+
+int32_t mczi_count_inputs_to_kff_path(mczi_ctx* ctx, const char* const* inputs, size_t n,
+                                      const mczi_counter_config* cfg, const char* out) {
+  return count_paths(ctx, inputs, n, cfg, MCZI_MODE_ABUNDANCE, out, true);
+}
+int32_t mczi_count_inputs_to_fasta_path(mczi_ctx* ctx, const char* const* inputs, size_t n,
+                                        const mczi_counter_config* cfg, const char* out) {
+  return count_paths(ctx, inputs, n, cfg, MCZI_MODE_ABUNDANCE, out, false);
+}
+int32_t mczi_count_datasets_to_kff_path(mczi_ctx* ctx, const char* const* inputs, size_t n,
+                                        const mczi_counter_config* cfg, const char* out) {
+  return count_paths(ctx, inputs, n, cfg, MCZI_MODE_PRESENCE, out, true);
+}
+int32_t mczi_count_datasets_to_fasta_path(mczi_ctx* ctx, const char* const* inputs, size_t n,
+                                          const mczi_counter_config* cfg, const char* out) {
+  return count_paths(ctx, inputs, n, cfg, MCZI_MODE_PRESENCE, out, false);
+}
+
+int32_t mczi_phase_times(mczi_ctx* ctx, float* ms, int32_t cap) {
+  if (!ctx) return MCZI_ERR_STATE;
+  int32_t n = std::min<int32_t>(cap, N_PHASES);
+  for (int32_t i = 0; i < n; i++) ms[i] = ctx->phase_ms[i];
+  return n;
+}
+
+int32_t mczi_run_stats(mczi_ctx* ctx, uint64_t* out, int32_t cap) {
+  if (!ctx) return MCZI_ERR_STATE;
+  int32_t n = std::min<int32_t>(cap, 8);
+  for (int32_t i = 0; i < n; i++) out[i] = ctx->stats[i];
+  return n;
+}
+
+int32_t mczi_set_count_tuning(mczi_ctx* ctx, int32_t threads, int32_t slots, int32_t ctas_per_sm) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (threads <= 0 || threads > 1024 || (threads & 31)) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "bad thread count");
+  if (ctas_per_sm <= 0 || ctas_per_sm > 4) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "bad CTAs per SM");
+  if (slots < 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "bad slot count");
+  ctx->count_threads = threads;
+  ctx->count_slots = slots;
+  ctx->count_ctas_per_sm = ctas_per_sm;
+  return MCZI_OK;
+}
+
+int32_t mczi_debug_packed(mczi_ctx* ctx, uint8_t* codes, uint8_t* starts, uint64_t cap, uint64_t* n_bases) {
+  if (!ctx || !ctx->have_result) return fail(ctx, MCZI_ERR_STATE, "no result");
+  cudaSetDevice(ctx->device);
+  const uint64_t nb = ctx->stats[0];
+  if (n_bases) *n_bases = nb;
+  if (!codes && !starts) return MCZI_OK;
+  if (cap < nb) return fail(ctx, MCZI_ERR_STATE, "buffer too small");
+  std::vector<uint32_t> pk(nb / 16 + 1), fb(nb / 32 + 1);
+  CK(cudaMemcpy(pk.data(), ctx->packed.p, pk.size() * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(fb.data(), ctx->fbits.p, fb.size() * 4, cudaMemcpyDeviceToHost));
+  for (uint64_t i = 0; i < nb; i++) {
+    if (codes) codes[i] = (uint8_t)((pk[i >> 4] >> (30 - 2 * (i & 15))) & 3u);
+    if (starts) starts[i] = (uint8_t)((fb[i >> 5] >> (i & 31)) & 1u);
+  }
+  return MCZI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,113 @@
+// mczi_internal.h -- kernel launch interfaces shared between the .cu files
+// of libmczi_gpu (not part of the public C ABI).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mczi {
+
+// ---------------------------------------------------------------- K1 packer
+constexpr int PACK_TILE = 8192;     // text bytes per CTA
+constexpr int PACK_THREADS = 256;
+constexpr int PACK_PER_THREAD = PACK_TILE / PACK_THREADS;
+
+struct LineSum {
+  int64_t last;   // absolute position of the last '\n' (or -1)
+  uint32_t nl;    // newline count
+  uint32_t reset; // an input starts at this tile
+  uint32_t pad;
+};
+
+struct BaseSum {
+  uint64_t nb;    // bases
+  uint32_t fb;    // a break precedes the first base (nb > 0)
+  uint32_t lb;    // a break follows the last base (nb > 0) / any break (nb == 0)
+  uint32_t pad;
+};
+
+struct PackArgs {
+  const uint8_t* text;       // tile-aligned input bytes
+  const uint32_t* tile_info; // input << 2 | fastq << 1 | input starts here
+  const uint64_t* input_tile0;  // first tile of each input
+  uint64_t n_tiles;
+  LineSum* line_sum;  LineSum* line_pre;  LineSum* line_tmp;
+  BaseSum* base_sum;  BaseSum* base_pre;  BaseSum* base_tmp;  // base_pre[n_tiles].nb = total bases
+  uint32_t* packed;   // zeroed, >= n_bases/16 + 8 words
+  uint32_t* fbits;    // zeroed, >= n_bases/32 + 8 words
+  uint64_t* input_base;  // first base of each input
+};
+void launch_pack(const PackArgs& a, cudaStream_t s);
+
+// ---------------------------------------------------------------- K2 scan
+constexpr int SCAN_TILE = 4096;     // windows per CTA
+constexpr int SCANK_THREADS = 256;
+
+struct ScanArgs {
+  const uint32_t* packed;
+  const uint32_t* fbits;
+  const uint64_t* n_bases;   // device scalar
+  uint64_t max_bases;        // grid bound (host upper bound on n_bases)
+  uint64_t packed_words;     // allocated words (reads beyond are zero)
+  int k, m;
+  uint64_t* desc;            // start << 24 | (windows - 1)
+  uint32_t* key;             // partition key = mix32(minimizer hash)
+  unsigned long long* n_desc;  // device counter
+  uint64_t desc_cap;
+  uint32_t* status;
+};
+void launch_scan(const ScanArgs& a, cudaStream_t s);
+
+// ---------------------------------------------------------------- K3 partition
+constexpr int P1_BITS = 12;
+constexpr int P2_BITS = 11;
+constexpr int NP1 = 1 << P1_BITS;
+constexpr int NP2 = 1 << P2_BITS;
+constexpr int PART_CTAS = 304;   // 2 per SM on a 152-SM GB300
+constexpr int PART_THREADS = 512;
+
+struct PartArgs {
+  const uint64_t* desc_in;
+  const uint32_t* key_in;
+  uint64_t* desc_out;
+  uint32_t* key_out;
+  const unsigned long long* n_desc;  // device scalar
+  uint64_t desc_cap;
+  uint32_t* hist;       // [NP1][PART_CTAS] then scanned in place
+  uint32_t* hist_tmp;   // scan temporaries
+  uint64_t* bucket_off; // NP1 + 1 bucket offsets (p1 buckets)
+  uint32_t* status;
+};
+void launch_partition(const PartArgs& a, cudaStream_t s);
+
+// ---------------------------------------------------------------- K5 count
+struct CountArgs {
+  const uint32_t* packed;
+  const uint64_t* desc;       // sorted by (p1, p2)
+  const uint32_t* key;
+  const uint64_t* bucket_off; // NP1 + 1
+  int k;
+  uint64_t threshold;         // emit iff count > threshold
+  int mode;                   // 0 abundance, 1 presence (fof)
+  const uint64_t* dataset_base;  // n_datasets + 1 base offsets (presence mode)
+  int n_datasets;
+  // outputs
+  uint64_t* out_lo;
+  uint64_t* out_hi;           // only for k > 32
+  uint32_t* out_count;
+  unsigned long long* n_out;
+  uint64_t out_cap;
+  unsigned long long* stats;  // [0] occurrences inserted, [1] distinct keys, [2] rounds, [3] splits
+  uint32_t* status;
+  uint32_t table_slots;       // hash-table slots per CTA
+  int threads;
+  int ctas;
+  unsigned int* work_counter;
+  float fill;                 // target fill of a round's table
+};
+void launch_count(const CountArgs& a, cudaStream_t s);
+size_t count_smem_bytes(int k, int mode, int n_datasets, uint32_t table_slots);
+size_t count_fixed_smem_bytes(int mode, int n_datasets);
+size_t count_slot_bytes(int k, int mode, int n_datasets);
+size_t scan_smem_bytes();
+
+}  // namespace mczi

@@ -1,0 +1,232 @@
+"""GPU parity: libmczi_gpu (through its C ABI) against the CPU oracle.
+
+Bit-exact set equality of (canonical k-mer, count) records is required for
+every case; the oracle itself is pinned by test_oracle_golden.py.
+"""
+import numpy as np
+import pytest
+
+from oracle_ref import encode, parse_kff, to_int
+
+pytestmark = pytest.mark.gpu
+
+
+def fa(seq):
+    return f">s\n{seq}\n".encode()
+
+
+def gpu_dict(ctx, inputs, k, m, x, mode=0, sorted_=False):
+    from mczi_gb300.mc import CounterConfig
+    n = ctx.count(inputs, CounterConfig(k, m, x), mode)
+    r = ctx.records(n, sorted=sorted_)
+    hi = r.hi if r.hi is not None else np.zeros_like(r.lo)
+    d = dict(zip(to_int(r.lo, hi), (int(c) for c in r.count)))
+    assert len(d) == n, "duplicate k-mer in GPU output"
+    return d
+
+
+def oracle_dict(oracle, inputs, k, x, mode=0):
+    lo, hi, cnt = oracle.count(inputs, k, x, mode)
+    return dict(zip(to_int(lo, hi), (int(c) for c in cnt)))
+
+
+def random_fasta(rng, n_reads, lo, hi, n_rate=0.0, lower=0.0):
+    out = []
+    for i in range(n_reads):
+        L = int(rng.integers(lo, hi + 1))
+        s = rng.choice(np.frombuffer(b"ACGT", dtype=np.uint8), size=L)
+        if n_rate:
+            s[rng.random(L) < n_rate] = ord("N")
+        if lower:
+            mask = rng.random(L) < lower
+            s[mask] = s[mask] + 32
+        out.append(b">r%d\n" % i + s.tobytes() + b"\n")
+    return b"".join(out)
+
+
+def test_golden_count_inputs(gpu_ctx, golden):
+    for case in golden["count_inputs"]["cases"]:
+        got = gpu_dict(gpu_ctx, [case["fasta"].encode()], case["k"], case["m"], case["x"])
+        if "exact" in case:
+            assert got == {encode(km): c for km, c in case["exact"]}
+        for km, c in case.get("contains", []):
+            assert got[encode(km)] == c
+
+
+def test_golden_ascii_counts(gpu_ctx, golden):
+    for seq, k, expected in golden["ascii_counts"]["cases"]:
+        got = gpu_dict(gpu_ctx, [fa(seq)], k, min(2, k), 0)
+        assert got == {encode(km): c for km, c in expected}, (seq, k)
+
+
+def test_golden_count_datasets(gpu_ctx, golden):
+    for case in golden["count_datasets"]["cases"]:
+        got = gpu_dict(gpu_ctx, [d.encode() for d in case["datasets"]], case["k"], case["m"], case["x"], mode=1)
+        if "exact" in case:
+            assert got == {encode(km): c for km, c in case["exact"]}
+        for km, c in case.get("contains", []):
+            assert got[encode(km)] == c
+        for km in case.get("absent", []):
+            assert encode(km) not in got
+
+
+def test_validation_matches_reference(gpu_ctx, golden):
+    from mczi_gb300 import MCZIError
+    from mczi_gb300.mc import CounterConfig
+    for k, m, x, ds, ok in golden["validation"]["cases"]:
+        try:
+            gpu_ctx.validate(CounterConfig(k, m, x), 1 if ds else 0)
+            passed = True
+        except MCZIError:
+            passed = False
+        assert passed == ok, (k, m, x, ds)
+
+
+@pytest.mark.parametrize("k,m", [(1, 1), (2, 1), (3, 2), (5, 3), (11, 5), (16, 9), (21, 11), (31, 21), (32, 19),
+                                 (33, 21), (45, 31), (63, 21), (64, 64), (31, 31), (25, 40 // 2)])
+def test_random_parity(gpu_ctx, oracle, k, m):
+    rng = np.random.default_rng(1000 + k * 100 + m)
+    data = random_fasta(rng, 300, 1, 400, n_rate=0.01, lower=0.05)
+    for x in (0, 1, 3):
+        assert gpu_dict(gpu_ctx, [data], k, m, x) == oracle_dict(oracle, [data], k, x), (k, m, x)
+
+
+def test_low_complexity_parity(gpu_ctx, oracle):
+    # homopolymers and short tandem repeats give long superkmers and heavy keys
+    parts = [b">h\n" + b"A" * 20000 + b"\n", b">t\n" + b"ACGTTG" * 3000 + b"\n", b">c\n" + b"C" * 33 + b"\n",
+             b">d\n" + b"AT" * 9000 + b"\n"]
+    data = b"".join(parts)
+    for k, m in ((31, 21), (63, 21), (15, 7)):
+        for x in (0, 2):
+            assert gpu_dict(gpu_ctx, [data], k, m, x) == oracle_dict(oracle, [data], k, x)
+
+
+def test_formats_and_edges(gpu_ctx, oracle):
+    rng = np.random.default_rng(7)
+    seq = rng.choice(np.frombuffer(b"ACGT", dtype=np.uint8), size=50000).tobytes()
+    wrapped = b">long\n" + b"\n".join(seq[i:i + 61] for i in range(0, len(seq), 61)) + b"\n"
+    crlf = b">c\r\n" + seq[:3000] + b"\r\n" + seq[3000:5000] + b"\r\n"
+    fastq = b"".join(b"@q%d\n%s\n+\n%s\n" % (i, seq[i * 150:(i + 1) * 150], b"I" * 150) for i in range(40))
+    longline = b">ll\n" + seq + b"\n"  # one line much longer than a tile
+    inputs = [wrapped, crlf, fastq, b"", b"not a fasta file\n", b">empty\n", b">allN\n" + b"N" * 9000 + b"\n",
+              longline, b">short\nACGTA\n"]
+    for k, m, x in ((31, 21, 0), (17, 9, 1), (63, 21, 0)):
+        assert gpu_dict(gpu_ctx, inputs, k, m, x) == oracle_dict(oracle, inputs, k, x)
+    # the skipped input is reported like MC_WARN
+    assert gpu_ctx.run_stats()[7] == 1
+
+
+def test_packer_parity(gpu_ctx, oracle):
+    rng = np.random.default_rng(11)
+    a = random_fasta(rng, 2000, 1, 700, n_rate=0.02, lower=0.1)
+    b = b"@x\nACGTNNAC\n+\nIIIIIIII\n@y\nGGTT\n+\nIIII\n"
+    c = b">z\nAC\nGT\n\n>w\nTTTT\r\n"
+    from mczi_gb300.mc import CounterConfig
+    gpu_ctx.count([a, b, c], CounterConfig(1, 1, 0))
+    codes, starts = gpu_ctx.debug_packed()
+    exp_codes, exp_starts = [], []
+    for buf in (a, b, c):
+        cc, offs, _ = oracle.fragments(buf, 1)
+        exp_codes.append(cc)
+        st = np.zeros(cc.size, dtype=np.uint8)
+        st[offs[:-1].astype(np.int64)] = 1
+        exp_starts.append(st)
+    assert np.array_equal(codes, np.concatenate(exp_codes))
+    assert np.array_equal(starts, np.concatenate(exp_starts))
+
+
+def test_tuning_invariance(gpu_ctx, oracle):
+    from mczi_gb300 import gen
+    data = gen.c1_reads(scale=0.004)
+    ref = oracle_dict(oracle, [data], 31, 1)
+    try:
+        for threads, slots, cps in ((512, 0, 2), (1024, 0, 1), (256, 0, 4), (128, 1024, 2), (256, 300 * 1 + 212, 2)):
+            gpu_ctx.set_count_tuning(threads, slots, cps)
+            assert gpu_dict(gpu_ctx, [data], 31, 21, 1) == ref, (threads, slots, cps)
+    finally:
+        gpu_ctx.set_count_tuning(512, 0, 2)
+
+
+def test_c1_shape_parity(gpu_ctx, oracle):
+    from mczi_gb300 import gen
+    data = gen.c1_reads(scale=0.02)
+    for x in (5, 0):
+        assert gpu_dict(gpu_ctx, [data], 31, 21, x) == oracle_dict(oracle, [data], 31, x)
+
+
+def test_c2_shape_parity(gpu_ctx, oracle):
+    from mczi_gb300 import gen
+    data = gen.c2_reads(scale=0.002)
+    for x in (3, 0):
+        assert gpu_dict(gpu_ctx, [data], 63, 21, x) == oracle_dict(oracle, [data], 63, x)
+
+
+def test_fof_parity(gpu_ctx, oracle):
+    from mczi_gb300 import gen
+    ds = gen.c3_datasets(n_datasets=6, genome_len=200_000, coverage=(2.0, 6.0))
+    ds.insert(2, np.frombuffer(b"", dtype=np.uint8))  # an empty dataset still counts as a dataset
+    for x in (0, 2, 5, 7):
+        assert gpu_dict(gpu_ctx, ds, 31, 21, x, mode=1) == oracle_dict(oracle, ds, 31, x, mode=1), x
+
+
+def test_fof_many_datasets(gpu_ctx, oracle):
+    rng = np.random.default_rng(5)
+    base = rng.choice(np.frombuffer(b"ACGT", dtype=np.uint8), size=3000).tobytes()
+    ds = []
+    for d in range(130):  # more than 64 datasets: multi-word presence masks
+        a, b = sorted(rng.integers(0, 3000, size=2))
+        ds.append(b">d\n" + base[a:b + 40] + b"\n")
+    for x in (0, 10, 64, 100):
+        assert gpu_dict(gpu_ctx, ds, 21, 11, x, mode=1) == oracle_dict(oracle, ds, 21, x, mode=1), x
+
+
+def test_kff_output(gpu_ctx, oracle, tmp_path):
+    from mczi_gb300 import gen
+    from mczi_gb300.mc import CounterConfig
+    data = gen.c1_reads(scale=0.004)
+    cases = [(31, 21, 2, 0, 1), (45, 21, 1, 0, 8)]
+    for k, m, x, mode, cs in cases:
+        gpu_ctx.count([data], CounterConfig(k, m, x), mode)
+        p = tmp_path / f"g{k}.kff"
+        gpu_ctx.write_kff(p)
+        head, recs, ok = parse_kff(p.read_bytes())
+        assert ok
+        lo, hi, cnt = oracle.count([data], k, x, mode)
+        exp = dict(zip(to_int(lo, hi), (int(c) for c in cnt)))
+        if cs == 1:
+            exp = {e: min(c, x + 1, 255) for e, c in exp.items()}
+        assert recs == exp
+        q = tmp_path / f"o{k}.kff"
+        oracle.write_kff(q, lo, hi, cnt, k, m, x, cs)
+        ohead, _, _ = parse_kff(q.read_bytes())
+        assert head["head"][: len(head["head"]) - 1] == ohead["head"][: len(ohead["head"]) - 1]
+        assert p.stat().st_size == q.stat().st_size
+
+
+def test_fasta_output_byte_identical(gpu_ctx, oracle, tmp_path):
+    from mczi_gb300 import gen
+    from mczi_gb300.mc import CounterConfig
+    data = gen.c1_reads(scale=0.002)
+    gpu_ctx.count([data], CounterConfig(31, 21, 1))
+    p = tmp_path / "g.fa"
+    gpu_ctx.write_fasta(p)
+    lo, hi, cnt = oracle.count([data], 31, 1)
+    q = tmp_path / "o.fa"
+    oracle.write_simplitigs(q, lo, hi, 31)
+    assert p.read_bytes() == q.read_bytes()
+
+
+def test_path_entry_points(gpu_ctx, oracle, tmp_path):
+    from mczi_gb300 import mc
+    a = tmp_path / "a.fa"
+    a.write_bytes(b">r\nACGTACGTTTGCA\n>s\nAAAANAAAA\n")
+    fofn = tmp_path / "in.fofn"
+    fofn.write_text("# comment\n\na.fa\n")
+    inputs = mc.expand_fofns([fofn])
+    assert inputs == [a]
+    cfg = mc.CounterConfig(3, 2, 1)
+    got = mc.count_inputs(inputs, cfg, ctx=gpu_ctx)
+    assert got == [mc.CountedKmer(e, c) for e, c in sorted(oracle_dict(oracle, [a.read_bytes()], 3, 1).items())]
+    out = tmp_path / "o.kff"
+    mc.count_inputs_to_kff_path(inputs, cfg, out, ctx=gpu_ctx)
+    assert out.read_bytes()[:3] == b"KFF"
