@@ -1,0 +1,321 @@
+#!/usr/bin/env python3
+"""MC Gbases/s on one GB300 -- the long-read abundance workload.
+
+Workload (the configuration the headline metric is quoted on): a seeded
+100 Mbp random genome with twenty 5 kbp segments present 20x each; log-normal
+long reads (median 8 kbp, sigma 0.8, clipped to 500 bp..100 kbp) to 40x
+(4 Gbp), 5 % errors split 60/20/20 substitution/insertion/deletion; k=63
+(128-bit k-mers), m=21, x=3.  Synthetic, seeded; generated on the host.
+
+One step = one full MC count of the whole workload: pack, minimizer scan,
+superkmer partition, per-bucket counting and the `> x` threshold.
+* value : Gbases/s with the FASTA bytes already resident in HBM (device time,
+          CUDA events on the stream the kernels run on).
+* e2e   : the same through the public C ABI with host buffers: host->device
+          copy of the FASTA from pinned memory, the count, and the
+          device->host read of every kept record, inside the timed region.
+The inputs (4 GB) are larger than L2 (126 MB), so no L2 flush is needed.
+
+`--impl reference` times the CPU implementation of the same path on the host
+cores: the reference is Rust and cannot be built here (no cargo/rustc), so
+its C restatement (oracle/) is run on a bounded sample of the workload.
+N > 1 (torchrun): independent replicas, one per GPU (the path has no
+collective); value = bases of all ranks / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = {"workload": "mc_abundance_long_reads_4gbp_k63", "k": 63, "m": 21, "x": 3,
+            "genome_bp": 100_000_000, "read_bases": 4_000_000_000, "reads": "lognormal median 8 kbp sigma 0.8",
+            "errors": "5% (3% sub, 1% ins, 1% del)", "input": "one-line FASTA",
+            "l2": "inputs (4 GB) larger than L2; no flush"}
+METRIC = "MC Gbases/s"
+UNIT = "Gbases/s"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(scale: float, pinned: bool):
+    """FASTA bytes of the workload in (pinned) host memory: (tensor, nbytes)."""
+    import numpy as np
+    import torch
+    from mczi_gb300 import gen
+    n = gen.c2_reads_size(scale)
+    buf = torch.empty(n, dtype=torch.uint8, pin_memory=pinned)
+    gen.c2_reads(scale, out=(buf.data_ptr(), n))
+    return buf, n
+
+
+def algorithmic_bytes(stats, k: int, text_bytes: int):
+    """Bytes each kernel must move (its inputs read once, outputs written once).
+
+    pack     : FASTA bytes + 2-bit stream (N_b/4) + fragment bits (N_b/8)
+    scan     : 2-bit stream + fragment bits + descriptors (12 B each)
+    partition: two passes of read + write of the 12 B descriptors
+    count    : descriptors (12 B) + each superkmer's packed bases
+               ((windows + k - 1) / 4 B) + kept records (24 B for k > 32);
+               the k-mers themselves are generated on chip and never
+               written, so no k-mer bytes are credited.
+    """
+    nb, ns, win, nout = stats[0], stats[1], stats[6], stats[5]
+    rec = 24 if k > 32 else 12
+    return {
+        "pack": text_bytes + nb / 4 + nb / 8,
+        "scan": nb / 4 + nb / 8 + 12 * ns,
+        "partition": 2 * 24 * ns,
+        "count": 12 * ns + (win + ns * (k - 1)) / 4 + rec * nout,
+    }
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from mczi_gb300 import build
+    build.build_all()
+    from mczi_gb300.mc import Context, CounterConfig
+
+    k, m, x = WORKLOAD["k"], WORKLOAD["m"], WORKLOAD["x"]
+    cfg = CounterConfig(k, m, x)
+    buf, nbytes = make_workload(args.scale, pinned=True)
+    stream = torch.cuda.current_stream()
+    ctx = Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    inputs = [(buf.data_ptr(), nbytes)]
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(v: float) -> float:
+        if ws == 1:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident value
+    ctx.stage(inputs)
+    for _ in range(args.warmup):
+        ctx.count_staged(cfg)
+    stats = ctx.run_stats()
+    phase_sum = [0.0] * 5
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.count_staged(cfg)
+        for i, t in enumerate(ctx.phase_times()):
+            phase_sum[i] += t
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    dev_ms = e0.elapsed_time(e1) / args.steps
+    dev_ms = max_over_ranks(dev_ms)
+    stats = ctx.run_stats()
+    nb = stats[0]
+    value = nb * ws / (dev_ms * 1e-3) / 1e9
+
+    # ---- end to end through the C ABI: H2D from pinned + count + D2H of every record
+    n_records = stats[5]
+    for _ in range(max(1, args.warmup // 2)):
+        ctx.count(inputs, cfg)
+        ctx.records(n_records, sorted=False)
+    barrier()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        n = ctx.count(inputs, cfg)
+        rec = ctx.records(n, sorted=False)
+    e1.record(stream)
+    barrier()
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
+    e2e_value = nb * ws / (e2e_ms * 1e-3) / 1e9
+    d2h = n_records * (8 + 8 + 4)
+
+    # ---- roofline of the dominant kernel
+    names = ["pack", "scan", "partition", "count"]
+    avg = {nm: phase_sum[i] / args.steps for i, nm in enumerate(names)}
+    dom = max(avg, key=avg.get)
+    alg = algorithmic_bytes(stats, k, nbytes)
+    peak, peak_kind = load_peaks()
+    achieved = alg[dom] / (avg[dom] * 1e-3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "ncu_traffic.json"
+    if tf.exists():
+        t = json.loads(tf.read_text()).get(WORKLOAD["workload"], {}).get(dom)
+        if t and t.get("bytes_per_base"):
+            traffic = t["bytes_per_base"] * nb
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dev_ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8/u64 (2-bit bases, 128-bit k-mers)",
+        "data": "synthetic (seeded generator, no dataset)",
+        "config": dict(WORKLOAD, parallelism=f"replicas{ws}" if ws > 1 else "single-gpu", bases=nb,
+                       superkmers=stats[1], kept_records=stats[5], scale=args.scale),
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(nbytes),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3)},
+        "gpu_launches": int(stats[8]) * args.steps,
+        "phases_ms": {nm: round(v, 3) for nm, v in avg.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes": int(alg[dom]), "traffic": int(traffic) if traffic else None},
+        "pipeline_roofline": {"algorithmic_bytes": int(sum(alg.values())),
+                              "achieved_gbs": round(sum(alg.values()) / (dev_ms * 1e-3) / 1e9, 1),
+                              "frac": round(sum(alg.values()) / (dev_ms * 1e-3) / 1e9 / peak, 4)},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args)
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(args, sample_scale: float | None = None):
+    """The C restatement (oracle/, OpenMP over all host cores) on a bounded
+    sample of the same workload: the same generator at a smaller scale."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_ref
+    from mczi_gb300 import gen
+    from mczi_gb300._native import default_threads
+    scale = sample_scale if sample_scale is not None else args.cpu_sample_scale
+    data = gen.c2_reads(scale)
+    threads = default_threads()
+    t0 = time.perf_counter()
+    lo, hi, cnt = oracle_ref.count([data], WORKLOAD["k"], WORKLOAD["x"], 0, threads)
+    dt = time.perf_counter() - t0
+    bases = int(WORKLOAD["read_bases"] * scale)
+    return {"value": round(bases / dt / 1e9, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"same generator at scale {scale} ({bases / 1e6:.0f} Mbp of the 4 Gbp workload), "
+                      f"{dt:.1f} s wall, {lo.size} kept k-mers"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    steps = []
+    for _ in range(args.warmup):
+        pass  # the CPU port has no warm-up state worth priming beyond page-in
+    cb = None
+    for _ in range(args.steps):
+        cb = cpu_baseline(args, args.ref_sample_scale)
+        steps.append(cb["value"])
+    value = statistics.median(steps)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "impl": "reference", "dtype": "u8/u128", "data": "synthetic (seeded generator, no dataset)",
+            "config": dict(WORKLOAD, parallelism="cpu"),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cb["cores"], "kind": "port",
+                             "sample": cb["sample"] + "; the Rust reference cannot be built here (no cargo/rustc)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0, help="workload scale (1.0 = 4 Gbp)")
+    ap.add_argument("--cpu-sample-scale", type=float, default=0.005)
+    ap.add_argument("--ref-sample-scale", type=float, default=0.004)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

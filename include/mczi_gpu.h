@@ -120,12 +120,17 @@ int32_t mczi_count_datasets_to_fasta_path(mczi_ctx* ctx, const char* const* inpu
 int32_t mczi_phase_times(mczi_ctx* ctx, float* ms, int32_t cap);
 /* Statistics of the last run: [0] bases, [1] superkmers, [2] counting rounds,
  * [3] round splits, [4] distinct k-mers inserted, [5] kept records,
- * [6] k-mer windows, [7] skipped inputs. */
+ * [6] k-mer windows, [7] skipped inputs, [8] kernel launches of the last
+ * count, [9] host-to-device input bytes of the last staging. */
 int32_t mczi_run_stats(mczi_ctx* ctx, uint64_t* out, int32_t cap);
 
 /* Tuning knobs (results never depend on them): threads per counting CTA,
- * table slots per CTA (0 = largest that fits), CTAs per SM. */
+ * table slots per CTA (0 = largest that fits), CTAs per SM; 0 selects the
+ * built-in default for the key width. */
 int32_t mczi_set_count_tuning(mczi_ctx* ctx, int32_t threads, int32_t table_slots, int32_t ctas_per_sm);
+/* Windows per work item of the counting insert phase (0 = derived from
+ * k - m) and the target fill of a counting round's table (0 = default 0.6). */
+int32_t mczi_set_count_options(mczi_ctx* ctx, int32_t chunk, float fill);
 
 /* Packer parity hook: after mczi_count/mczi_count_staged, copies the 2-bit
  * codes (one byte per base) and fragment-start flags (one byte per base) of

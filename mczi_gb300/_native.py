@@ -73,6 +73,7 @@ SIGNATURES = [
     ("mczi_phase_times", C.c_int32, [C.c_void_p, C.POINTER(C.c_float), C.c_int32]),
     ("mczi_run_stats", C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int32]),
     ("mczi_set_count_tuning", C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
+    ("mczi_set_count_options", C.c_int32, [C.c_void_p, C.c_int32, C.c_float]),
     ("mczi_debug_packed", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
 ]
 

@@ -29,12 +29,42 @@ namespace mczi {
 namespace {
 
 constexpr int MAX_STACK = 48;
+constexpr uint32_t PROBE_LIMIT = 256;
+constexpr int MAX_THREADS = 1024;
+
+// exclusive scan of one u32 per thread over the block (<= 1024 threads);
+// `ws` is 32 words of shared scratch.  Ends with a barrier.
+__device__ __forceinline__ uint32_t block_excl_scan_u32(uint32_t v, uint32_t* total, uint32_t* ws) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t t = lane < nw ? ws[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    ws[lane] = t;
+  }
+  __syncthreads();
+  const uint32_t r = x - v + (wid ? ws[wid - 1] : 0u);
+  *total = ws[nw - 1];
+  __syncthreads();
+  return r;
+}
 
 template <class K>
 struct KeyOps;
 
 template <>
 struct KeyOps<K64> {
+  // 64-bit shared loads are single-copy atomic: only EMPTY needs the CAS
+  static __device__ __forceinline__ bool maybe_partial(K64 c) { return c.v == ~0ull; }
   static __device__ __forceinline__ K64 cas(K64* p, K64 cmp, K64 val) {
     unsigned long long r = atomicCAS(reinterpret_cast<unsigned long long*>(p), (unsigned long long)cmp.v,
                                      (unsigned long long)val.v);
@@ -44,6 +74,9 @@ struct KeyOps<K64> {
 
 template <>
 struct KeyOps<K128> {
+  // a 16-byte load may observe half of a concurrent EMPTY -> key store; such
+  // a value has an all-ones half, as EMPTY has
+  static __device__ __forceinline__ bool maybe_partial(K128 c) { return c.lo == ~0ull || c.hi == ~0ull; }
   static __device__ __forceinline__ K128 cas(K128* p, K128 cmp, K128 val) { return atomicCAS(p, cmp, val); }
 };
 
@@ -106,12 +139,15 @@ __global__ void k_count(CountArgs a) {
   __shared__ RoundRange stack[MAX_STACK];
   __shared__ uint32_t warp_tmp[32];
   __shared__ float s_rho;
+  __shared__ uint32_t sh_cpre[MAX_THREADS + 1];
+  __shared__ uint64_t sh_desc[MAX_THREADS];
+  __shared__ uint16_t sh_dset[MODE == 1 ? MAX_THREADS : 1];
+  const uint32_t chunk = a.chunk;
 
   const int tid = threadIdx.x, nth = blockDim.x;
   const int lane = tid & 31;
   const int k = a.k;
   const K EMPTY = key_empty<K>();
-  const uint32_t limit = (uint32_t)(0.85f * (float)S);
 
   if (MODE == 1) {
     for (int i = tid; i <= a.n_datasets; i += nth) dsbase[i] = a.dataset_base[i];
@@ -240,59 +276,103 @@ __global__ void k_count(CountArgs a) {
         }
         __syncthreads();
         const bool full_range = (rr.hlo == 0u && rr.hhi == 0xffffffffu);
-        // ---- insert: one thread per superkmer descriptor
-        for (uint64_t di = lo + dlo + tid; di < lo + dhi; di += nth) {
-          if (*(volatile uint32_t*)&s_over) break;
-          const uint64_t dsc = a.desc[di];
-          const uint64_t s0 = dsc >> 24;
-          const uint32_t nwin = (uint32_t)(dsc & 0xffffffu) + 1u;
-          uint32_t dset = 0;
-          if (MODE == 1) {
-            int l2 = 0, h2 = a.n_datasets;  // largest i with dsbase[i] <= s0
-            while (h2 - l2 > 1) { const int mid = (l2 + h2) >> 1; if (dsbase[mid] <= s0) l2 = mid; else h2 = mid; }
-            dset = (uint32_t)l2;
+        uint32_t claimed = 0;  // slots this thread claimed in this round
+        // ---- insert.  The round's superkmers are taken in batches of up to
+        // blockDim descriptors; each is cut into chunks of `chunk` windows and
+        // the chunks are spread over all threads, so long and short superkmers
+        // keep every lane busy.  A chunk extracts its first k-mer from the
+        // packed stream and rolls through the rest.
+        for (uint64_t bb = dlo; bb < dhi; bb += (uint64_t)nth) {
+          const bool has = bb + (uint64_t)tid < dhi;
+          uint64_t dsc = 0;
+          uint32_t nch = 0;
+          if (has) {
+            dsc = a.desc[lo + bb + (uint64_t)tid];
+            const uint32_t len = (uint32_t)(dsc & 0xffffffu) + 1u;
+            nch = (len + chunk - 1) / chunk;
+            if (MODE == 1) {
+              const uint64_t s0 = dsc >> 24;
+              int l2 = 0, h2 = a.n_datasets;  // largest i with dsbase[i] <= s0
+              while (h2 - l2 > 1) { const int mid = (l2 + h2) >> 1; if (dsbase[mid] <= s0) l2 = mid; else h2 = mid; }
+              sh_dset[tid] = (uint16_t)l2;
+            }
           }
-          R roll;
-          roll.init(k);
-          if constexpr (sizeof(K) == 8) {
-            roll.set(field64(a.packed, s0, k), k);
-          } else {
-            if (k > 32) roll.set(field64(a.packed, s0, k - 32), field64(a.packed, s0 + (uint64_t)(k - 32), 32), k);
-            else roll.set(0ull, field64(a.packed, s0, k), k);
-          }
-          uint64_t p = s0 + (uint64_t)k;
-          uint32_t word = a.packed[p >> 4];
-          for (uint32_t j = 0; j < nwin; j++) {
-            if (j > 0) {
-              if ((p & 15) == 0) word = a.packed[p >> 4];
-              roll.push((word >> (30 - 2 * (uint32_t)(p & 15))) & 3u);
-              p++;
-            }
-            const K key = roll.canon();
-            const uint64_t hv = key_hash(key);
-            if (!full_range) {
-              const uint32_t hk = (uint32_t)(hv >> 32);
-              if (hk < rr.hlo || hk > rr.hhi) continue;
-            }
-            uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
-            bool done = false;
-            for (uint32_t probe = 0; probe < S; probe++) {
-              const K prev = KeyOps<K>::cas(&keys[s], EMPTY, key);
-              if (key_eq(prev, EMPTY) || key_eq(prev, key)) {
-                if (key_eq(prev, EMPTY)) {
-                  if (atomicAdd(&s_nused, 1u) + 1u > limit) s_over = 1;
-                }
-                if (MODE == 0) atomicAdd(&cnt[s], 1u);
-                else atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
-                done = true;
-                break;
-              }
-              s = (s + 1 == S) ? 0u : s + 1;
-            }
-            if (!done) { s_over = 1; break; }
+          sh_desc[tid] = dsc;
+          uint32_t total;
+          sh_cpre[tid] = block_excl_scan_u32(nch, &total, warp_tmp);
+          if (tid == 0) sh_cpre[nth] = total;
+          __syncthreads();
+          const int nd = (int)min((uint64_t)nth, dhi - bb);
+          for (uint32_t c = tid; c < total; c += nth) {
             if (*(volatile uint32_t*)&s_over) break;
+            int lo2 = 0, hi2 = nd;  // descriptor j: sh_cpre[j] <= c < sh_cpre[j + 1]
+            while (hi2 - lo2 > 1) { const int mid = (lo2 + hi2) >> 1; if (sh_cpre[mid] <= c) lo2 = mid; else hi2 = mid; }
+            const uint64_t d2 = sh_desc[lo2];
+            const uint32_t len = (uint32_t)(d2 & 0xffffffu) + 1u;
+            const uint32_t w0 = (c - sh_cpre[lo2]) * chunk;
+            const uint32_t w1 = min(w0 + chunk, len);
+            const uint32_t dset = MODE == 1 ? (uint32_t)sh_dset[lo2] : 0u;
+            const uint64_t s0 = (d2 >> 24) + w0;
+            R roll;
+            roll.init(k);
+            if constexpr (sizeof(K) == 8) {
+              roll.set(field64(a.packed, s0, k), k);
+            } else {
+              if (k > 32) roll.set(field64(a.packed, s0, k - 32), field64(a.packed, s0 + (uint64_t)(k - 32), 32), k);
+              else roll.set(0ull, field64(a.packed, s0, k), k);
+            }
+            uint64_t p = s0 + (uint64_t)k;
+            uint32_t word = a.packed[p >> 4];
+            for (uint32_t j = w0; j < w1; j++) {
+              if (j > w0) {
+                if ((p & 15) == 0) word = a.packed[p >> 4];
+                roll.push((word >> (30 - 2 * (uint32_t)(p & 15))) & 3u);
+                p++;
+              }
+              const K key = roll.canon();
+              const uint64_t hv = key_hash(key);
+              if (!full_range) {
+                const uint32_t hk = (uint32_t)(hv >> 32);
+                if (hk < rr.hlo || hk > rr.hhi) continue;
+              }
+              uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
+              bool done = false;
+              // Probe with plain loads; CAS only on a slot that looks empty.
+              // A slot goes from EMPTY to a key exactly once, so a load that
+              // shows a complete key (no all-ones half) is final; anything
+              // else is resolved by the CAS's atomic snapshot.  The claiming
+              // thread's own occurrence is implicit: a slot's stored count is
+              // (occurrences - 1).  A probe run longer than PROBE_LIMIT means
+              // the table is far past its target fill: the round is split.
+              for (uint32_t probe = 0; probe < PROBE_LIMIT; probe++) {
+                K cur = keys[s];
+                if (KeyOps<K>::maybe_partial(cur)) {
+                  const K prev = KeyOps<K>::cas(&keys[s], EMPTY, key);
+                  if (key_eq(prev, EMPTY)) {
+                    claimed++;
+                    if (MODE == 1) atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
+                    done = true;
+                    break;
+                  }
+                  cur = prev;
+                }
+                if (key_eq(cur, key)) {
+                  if (MODE == 0) atomicAdd(&cnt[s], 1u);
+                  else atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
+                  done = true;
+                  break;
+                }
+                s = (s + 1 == S) ? 0u : s + 1;
+              }
+              if (!done) { s_over = 1; break; }
+            }
           }
+          __syncthreads();
+          if (s_over) break;
         }
+        // distinct keys of the round (for the distinct/occurrence estimate)
+        for (int o = 16; o > 0; o >>= 1) claimed += __shfl_down_sync(0xffffffffu, claimed, o);
+        if (lane == 0 && claimed) atomicAdd(&s_nused, claimed);
         __syncthreads();
         if (s_over) {
           if (tid == 0) {
@@ -328,7 +408,7 @@ __global__ void k_count(CountArgs a) {
           if (s < S) {
             key = keys[s];
             if (!key_eq(key, EMPTY)) {
-              c = MODE == 0 ? cnt[s] : popc_words(&msk[(size_t)s * W], W);
+              c = MODE == 0 ? cnt[s] + 1u : popc_words(&msk[(size_t)s * W], W);
               emit = (uint64_t)c > a.threshold;
             }
           }
@@ -371,6 +451,14 @@ static void launch_one(const CountArgs& a, cudaStream_t s) {
   const size_t smem = count_smem_bytes(a.k, a.mode, a.n_datasets, a.table_slots);
   cudaFuncSetAttribute(k_count<K, R, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k_count<K, R, MODE><<<a.ctas, a.threads, smem, s>>>(a);
+}
+
+size_t count_static_smem(int k, int mode) {
+  cudaFuncAttributes fa{};
+  cudaError_t e;
+  if (k <= 32) e = mode == 0 ? cudaFuncGetAttributes(&fa, k_count<K64, Roll64, 0>) : cudaFuncGetAttributes(&fa, k_count<K64, Roll64, 1>);
+  else e = mode == 0 ? cudaFuncGetAttributes(&fa, k_count<K128, Roll128, 0>) : cudaFuncGetAttributes(&fa, k_count<K128, Roll128, 1>);
+  return e == cudaSuccess ? fa.sharedSizeBytes : 4096;
 }
 
 void launch_count(const CountArgs& a, cudaStream_t s) {

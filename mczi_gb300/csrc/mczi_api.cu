@@ -83,14 +83,18 @@ struct mczi_ctx {
   uint64_t x = 0;
   uint64_t n_out = 0;
   float phase_ms[N_PHASES] = {0, 0, 0, 0, 0};
-  uint64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  uint64_t stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  uint64_t h2d_bytes = 0;
   cudaEvent_t ev[N_PHASES + 1] = {};
 
   // tuning
-  int count_threads = 512;
+  // 0 = per-key-width defaults measured on GB300: 128-bit keys 1024 threads x
+  // 1 CTA/SM, fill 0.4; 64-bit keys 512 x 2, fill 0.6; 2 windows per item
+  int count_threads = 0;
   int count_slots = 0;
-  int count_ctas_per_sm = 2;
-  float count_fill = 0.6f;
+  int count_ctas_per_sm = 0;
+  float count_fill = 0.f;
+  int count_chunk = 0;
 };
 
 namespace {
@@ -163,6 +167,7 @@ int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n) {
   std::vector<int> fmt(n);
   uint64_t pos = 0;
   ctx->skipped = 0;
+  ctx->h2d_bytes = 0;
   for (size_t i = 0; i < n; i++) {
     const uint8_t* d = inputs[i].data;
     uint64_t l = d ? inputs[i].len : 0;
@@ -197,6 +202,7 @@ int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n) {
   for (size_t i = 0; i < n; i++) {
     uint8_t* dst = ctx->text.as<uint8_t>() + off[i];
     if (len[i]) CK(cudaMemcpyAsync(dst, inputs[i].data, len[i], cudaMemcpyHostToDevice, s));
+    ctx->h2d_bytes += len[i];
     const uint64_t end = i + 1 < n ? off[i + 1] : text_len;
     if (off[i] + len[i] < end) CK(cudaMemsetAsync(dst + len[i], '\n', end - off[i] - len[i], s));
   }
@@ -232,6 +238,7 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
     ctx->mode = mode; ctx->k = k; ctx->m = m; ctx->x = cfg->threshold;
     ctx->n_out = 0;
     std::memset(ctx->stats, 0, sizeof ctx->stats);
+    ctx->stats[9] = ctx->h2d_bytes;
     ctx->have_result = true;
     if (n_records) *n_records = 0;
     return MCZI_OK;
@@ -268,6 +275,7 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
   pa.fbits = ctx->fbits.as<uint32_t>();
   pa.input_base = ctx->input_base.as<uint64_t>();
   launch_pack(pa, s);
+  uint64_t launches = 9;
   const uint64_t* d_nbases = reinterpret_cast<const uint64_t*>(ctx->base_pre.as<BaseSum>() + n_tiles);
   CK(cudaMemcpyAsync(ctx->input_base.as<uint64_t>() + n_in, d_nbases, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
   CK(cudaGetLastError());
@@ -296,6 +304,7 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
     sa.desc_cap = desc_cap;
     sa.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
     launch_scan(sa, s);
+    launches += 1;
     CK(cudaGetLastError());
     uint64_t h[2];
     CK(cudaMemcpyAsync(h, sc + SC_NDESC, 8, cudaMemcpyDeviceToHost, s));
@@ -329,7 +338,10 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
   qa.hist_tmp = ctx->part_tmp.as<uint32_t>();
   qa.bucket_off = ctx->bucket_off.as<uint64_t>();
   qa.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
-  if (n_desc > 0) launch_partition(qa, s);
+  if (n_desc > 0) {
+    launch_partition(qa, s);
+    launches += 7;
+  }
   CK(cudaGetLastError());
   CK(cudaEventRecord(ctx->ev[3], s));
 
@@ -339,13 +351,15 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
   uint64_t out_cap = std::min<uint64_t>(est_out, 1ull << 25);
   uint64_t n_out = 0;
   if (n_desc > 0) {
-    int threads = ctx->count_threads;
-    int cps = ctx->count_ctas_per_sm;
+    int threads = ctx->count_threads > 0 ? ctx->count_threads : (wide ? 1024 : 512);
+    int cps = ctx->count_ctas_per_sm > 0 ? ctx->count_ctas_per_sm : (wide ? 1 : 2);
     const size_t budget = ctx->smem_optin;  // per block, opt-in
     const size_t fixed = count_fixed_smem_bytes(mode, n_in);
     const size_t slotb = count_slot_bytes(k, mode, n_in);
-    // shared memory per SM is ~228 KiB; leave 1 KiB per CTA for the runtime
-    size_t per_cta = std::min(budget, (size_t)(228 * 1024) / (size_t)cps - 1024);
+    // shared memory per SM is 228 KiB with 1 KiB per CTA reserved; the
+    // kernel's static shared memory counts against the same budget
+    const size_t stat = count_static_smem(k, mode);
+    size_t per_cta = std::min(budget, (size_t)(228 * 1024) / (size_t)cps - 1024) - stat - 64;
     uint32_t slots = ctx->count_slots > 0 ? (uint32_t)ctx->count_slots
                                            : (uint32_t)((per_cta - fixed - 64) / slotb);
     if (slots < (uint32_t)threads) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "counting table smaller than the CTA");
@@ -380,8 +394,10 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
       ca.threads = threads;
       ca.ctas = ctx->sm_count * cps;
       ca.work_counter = reinterpret_cast<unsigned int*>(sc + SC_WORK);
-      ca.fill = ctx->count_fill;
+      ca.fill = ctx->count_fill > 0.f ? ctx->count_fill : (wide ? 0.4f : 0.6f);
+      ca.chunk = ctx->count_chunk > 0 ? (uint32_t)ctx->count_chunk : 2u;
       launch_count(ca, s);
+      launches += 1;
       CK(cudaGetLastError());
       uint64_t h[SC_COUNT];
       CK(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, s));
@@ -409,6 +425,8 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
   ctx->stats[0] = nb;
   ctx->stats[5] = n_out;
   ctx->stats[7] = ctx->skipped;
+  ctx->stats[8] = launches;
+  ctx->stats[9] = ctx->h2d_bytes;
   ctx->mode = mode;
   ctx->k = k;
   ctx->m = m;
@@ -618,19 +636,28 @@ int32_t mczi_phase_times(mczi_ctx* ctx, float* ms, int32_t cap) {
 
 int32_t mczi_run_stats(mczi_ctx* ctx, uint64_t* out, int32_t cap) {
   if (!ctx) return MCZI_ERR_STATE;
-  int32_t n = std::min<int32_t>(cap, 8);
+  int32_t n = std::min<int32_t>(cap, 10);
   for (int32_t i = 0; i < n; i++) out[i] = ctx->stats[i];
   return n;
 }
 
 int32_t mczi_set_count_tuning(mczi_ctx* ctx, int32_t threads, int32_t slots, int32_t ctas_per_sm) {
   if (!ctx) return MCZI_ERR_STATE;
-  if (threads <= 0 || threads > 1024 || (threads & 31)) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "bad thread count");
-  if (ctas_per_sm <= 0 || ctas_per_sm > 4) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "bad CTAs per SM");
+  if (threads < 0 || threads > 1024 || (threads & 31)) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "bad thread count");
+  if (ctas_per_sm < 0 || ctas_per_sm > 4) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "bad CTAs per SM");
   if (slots < 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "bad slot count");
   ctx->count_threads = threads;
   ctx->count_slots = slots;
   ctx->count_ctas_per_sm = ctas_per_sm;
+  return MCZI_OK;
+}
+
+int32_t mczi_set_count_options(mczi_ctx* ctx, int32_t chunk, float fill) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (chunk < 0 || chunk > 4096) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "bad chunk");
+  if (fill < 0.f || fill > 0.85f) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "fill must be in (0, 0.85]");
+  ctx->count_chunk = chunk;
+  ctx->count_fill = fill;
   return MCZI_OK;
 }
 

@@ -64,7 +64,7 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
 
 __device__ __forceinline__ uint64_t key_hash(K64 k) { return mix64(k.v); }
 __device__ __forceinline__ uint64_t key_hash(K128 k) {
-  return mix64(k.lo ^ mix64(k.hi + 0x9e3779b97f4a7c15ull));
+  return mix64(k.lo ^ (k.hi * 0x9e3779b97f4a7c15ull));
 }
 
 // reverse the order of 2-bit groups and complement (x ^ 3 per base)

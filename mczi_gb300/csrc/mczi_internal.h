@@ -103,11 +103,13 @@ struct CountArgs {
   int ctas;
   unsigned int* work_counter;
   float fill;                 // target fill of a round's table
+  uint32_t chunk;             // windows per work item in the insert phase
 };
 void launch_count(const CountArgs& a, cudaStream_t s);
 size_t count_smem_bytes(int k, int mode, int n_datasets, uint32_t table_slots);
 size_t count_fixed_smem_bytes(int mode, int n_datasets);
 size_t count_slot_bytes(int k, int mode, int n_datasets);
 size_t scan_smem_bytes();
+size_t count_static_smem(int k, int mode);
 
 }  // namespace mczi

@@ -190,12 +190,15 @@ class Context:
         return [float(buf[i]) for i in range(n)]
 
     def run_stats(self) -> list[int]:
-        buf = (C.c_uint64 * 8)()
-        n = self._ck(self._lib.mczi_run_stats(self._h, buf, 8))
+        buf = (C.c_uint64 * 10)()
+        n = self._ck(self._lib.mczi_run_stats(self._h, buf, 10))
         return [int(buf[i]) for i in range(n)]
 
     def set_count_tuning(self, threads: int, table_slots: int = 0, ctas_per_sm: int = 2) -> None:
         self._ck(self._lib.mczi_set_count_tuning(self._h, threads, table_slots, ctas_per_sm))
+
+    def set_count_options(self, chunk: int = 0, fill: float = 0.0) -> None:
+        self._ck(self._lib.mczi_set_count_options(self._h, chunk, fill))
 
     def debug_packed(self) -> tuple[np.ndarray, np.ndarray]:
         nb = C.c_uint64()

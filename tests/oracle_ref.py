@@ -156,6 +156,7 @@ def parse_kff(data: bytes):
     p += 1
     n = int.from_bytes(data[p:p + 8], "big")
     p += 8
+    hdr_end = p
     k = vals["k"]
     nb = (k + 3) // 4
     cs = vals["data_size"]
@@ -167,4 +168,4 @@ def parse_kff(data: bytes):
         p += cs
         recs[key] = c
     trailer = data[p:] == b"KFF"
-    return {"free_block": free_block, "values": vals, "n": n, "head": data[:p - 0]}, recs, trailer
+    return {"free_block": free_block, "values": vals, "n": n, "head": data[:hdr_end]}, recs, trailer
