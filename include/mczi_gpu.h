@@ -34,6 +34,7 @@ extern "C" {
 #define MCZI_ERR_DEVICE (-4)         /* CUDA error or kernels unavailable */
 #define MCZI_ERR_TIMEOUT (-5)        /* a bounded device-side wait gave up */
 #define MCZI_ERR_STATE (-6)          /* call out of order (e.g. no result yet) */
+#define MCZI_ERR_TOO_LARGE (-7)      /* input beyond a fixed maximum (mczi_pack_fastx_noalloc) */
 
 #define MCZI_MODE_ABUNDANCE 0 /* count every occurrence */
 #define MCZI_MODE_PRESENCE 1  /* fof: count each dataset (input) at most once */
@@ -136,6 +137,35 @@ int32_t mczi_set_count_options(mczi_ctx* ctx, int32_t chunk, float fill);
  * codes (one byte per base) and fragment-start flags (one byte per base) of
  * the packed stream; *n_bases receives the base count. */
 int32_t mczi_debug_packed(mczi_ctx* ctx, uint8_t* codes, uint8_t* starts, uint64_t cap, uint64_t* n_bases);
+
+/* ------------------------------------------------ packing without allocation */
+
+/* The 2-bit packer of mczi_count's first phase, for callers that cannot
+ * allocate device memory where they call it: code running while a stream is
+ * being captured into a CUDA graph, services that give out device memory only
+ * from their own pre-sized arena, or latency-critical paths where a
+ * cudaMalloc (and the synchronisation it may cause) is not allowed.  This
+ * entry point has no counterpart in the reference; it allocates nothing and
+ * calls no allocating routine.
+ *
+ * Inputs and outputs are the caller's device buffers: `d_text` holds one
+ * FASTA (fastq = 0) or four-line FASTQ (fastq = 1) input of `text_len` bytes,
+ * padded with '\n' to a multiple of 8192 bytes; at most 512 MiB
+ * (65,536 tiles of 8192 bytes) -- larger inputs return MCZI_ERR_TOO_LARGE.
+ * `d_packed` (>= text_len/16 + 8 words) receives the bases, 16 per word,
+ * MSB-first, A0 C1 G2 T3; `d_fbits` (>= text_len/32 + 8 words) one bit per
+ * base, set where a fragment (a maximal A/C/G/T run of one record) starts.
+ * Both are cleared by the call.  *n_bases (host) receives the base count; the
+ * call synchronises `stream` before returning.
+ *
+ * Scratch: an 8 MiB array in device memory, reserved once per process on every
+ * GPU that loads this library and held until exit.  The first call on a device
+ * looks its address up (cudaGetSymbolAddress) with that device current; make
+ * that first call before any stream capture.  Every call shares the array, so
+ * calls that overlap on the GPU race: issue them one at a time. */
+int32_t mczi_pack_fastx_noalloc(const uint8_t* d_text, uint64_t text_len, int32_t fastq, uint32_t* d_packed,
+                                uint64_t packed_words, uint32_t* d_fbits, uint64_t fbits_words, uint64_t* n_bases,
+                                void* stream);
 
 #ifdef __cplusplus
 }

@@ -19,6 +19,7 @@ MCZI_ERR_OOM = -3
 MCZI_ERR_DEVICE = -4
 MCZI_ERR_TIMEOUT = -5
 MCZI_ERR_STATE = -6
+MCZI_ERR_TOO_LARGE = -7
 
 MODE_ABUNDANCE = 0
 MODE_PRESENCE = 1
@@ -30,6 +31,7 @@ _CODE_NAMES = {
     MCZI_ERR_DEVICE: "device error",
     MCZI_ERR_TIMEOUT: "device wait timed out",
     MCZI_ERR_STATE: "call out of order",
+    MCZI_ERR_TOO_LARGE: "input larger than the fixed maximum",
 }
 
 
@@ -75,6 +77,8 @@ SIGNATURES = [
     ("mczi_set_count_tuning", C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]),
     ("mczi_set_count_options", C.c_int32, [C.c_void_p, C.c_int32, C.c_float]),
     ("mczi_debug_packed", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    ("mczi_pack_fastx_noalloc", C.c_int32, [C.c_void_p, C.c_uint64, C.c_int32, C.c_void_p, C.c_uint64, C.c_void_p,
+                                            C.c_uint64, C.POINTER(C.c_uint64), C.c_void_p]),
 ]
 
 _lib = None
