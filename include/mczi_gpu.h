@@ -133,6 +133,13 @@ int32_t mczi_set_count_tuning(mczi_ctx* ctx, int32_t threads, int32_t table_slot
  * k - m) and the target fill of a counting round's table (0 = default 0.6). */
 int32_t mczi_set_count_options(mczi_ctx* ctx, int32_t chunk, float fill);
 
+/* Pass-1 minimizer pre-count (MC's CompactMinimizerTable / DatasetMinimizerTable,
+ * src/lib.rs:4171-4370, filter :4625-4629): when enabled, superkmers whose
+ * minimizer count (windows, or datasets in fof mode) is <= threshold are dropped
+ * before counting.  The filter is conservative, so results are identical with
+ * it on or off; it only changes the work done.  Default off. */
+int32_t mczi_set_minimizer_precount(mczi_ctx* ctx, int32_t enable);
+
 /* Packer parity hook: after mczi_count/mczi_count_staged, copies the 2-bit
  * codes (one byte per base) and fragment-start flags (one byte per base) of
  * the packed stream; *n_bases receives the base count. */

@@ -51,7 +51,7 @@ struct DevBuf {
 };
 
 // device scalars, in u64 slots
-enum { SC_NDESC = 0, SC_NOUT = 1, SC_STATS = 2, SC_STATUS = 10, SC_WORK = 11, SC_COUNT = 16 };
+enum { SC_NDESC = 0, SC_NOUT = 1, SC_STATS = 2, SC_STATUS = 10, SC_WORK = 11, SC_NKEPT = 12, SC_COUNT = 16 };
 
 constexpr int N_PHASES = 5;
 
@@ -70,6 +70,7 @@ struct mczi_ctx {
   DevBuf desc, key, desc2, key2, part_hist, part_tmp, bucket_off;
   DevBuf out_lo, out_hi, out_cnt;
   DevBuf scalars;
+  DevBuf mintab, pairtab;
 
   // staged inputs
   bool staged = false;
@@ -86,6 +87,8 @@ struct mczi_ctx {
   uint64_t stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   uint64_t h2d_bytes = 0;
   cudaEvent_t ev[N_PHASES + 1] = {};
+  cudaEvent_t ev_pre[2] = {};
+  int precount = 0;  // pass-1 minimizer table + filter (results identical either way)
 
   // tuning
   // 0 = per-key-width defaults measured on GB300: 128-bit keys 1024 threads x
@@ -317,8 +320,55 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
     desc_cap = h[0] + 1024;
     if (attempt == 2) return fail(ctx, MCZI_ERR_DEVICE, "descriptor buffer overflow persisted");
   }
+  uint64_t n_desc = ctx->stats[1];
+  float pre_ms = 0.f;
+  if (ctx->precount && n_desc > 0) {
+    // ---- K4 pass-1 minimizer table, then keep superkmers whose minimizer count > x
+    uint64_t slots = 1024;
+    while (slots < 2 * n_desc) slots <<= 1;
+    CKA(ctx->mintab, slots * 8);
+    CKA(ctx->desc2, desc_cap * 8);
+    CKA(ctx->key2, desc_cap * 4);
+    CK(cudaMemsetAsync(ctx->mintab.p, 0, slots * 8, s));
+    if (mode == MCZI_MODE_PRESENCE) {
+      CKA(ctx->pairtab, slots * 8);
+      CK(cudaMemsetAsync(ctx->pairtab.p, 0, slots * 8, s));
+    }
+    CK(cudaMemsetAsync(sc + SC_NKEPT, 0, 8, s));
+    CK(cudaEventRecord(ctx->ev_pre[0], s));
+    PrecountArgs pc;
+    pc.desc = ctx->desc.as<uint64_t>();
+    pc.key = ctx->key.as<uint32_t>();
+    pc.n_desc = reinterpret_cast<const unsigned long long*>(sc + SC_NDESC);
+    pc.table = ctx->mintab.as<unsigned long long>();
+    pc.mask = slots - 1;
+    pc.pairs = mode == MCZI_MODE_PRESENCE ? ctx->pairtab.as<unsigned long long>() : nullptr;
+    pc.pair_mask = slots - 1;
+    pc.mode = mode;
+    pc.dataset_base = ctx->input_base.as<uint64_t>();
+    pc.n_datasets = n_in;
+    pc.threshold = cfg->threshold;
+    pc.desc_out = ctx->desc2.as<uint64_t>();
+    pc.key_out = ctx->key2.as<uint32_t>();
+    pc.n_kept = reinterpret_cast<unsigned long long*>(sc + SC_NKEPT);
+    pc.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
+    launch_precount(pc, ctx->sm_count, s);
+    launches += 2;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev_pre[1], s));
+    uint64_t h[2];
+    CK(cudaMemcpyAsync(h, sc + SC_NKEPT, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h + 1, sc + SC_STATUS, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h[1] & ST_MINTAB_FULL) return fail(ctx, MCZI_ERR_DEVICE, "minimizer table full");
+    std::swap(ctx->desc, ctx->desc2);
+    std::swap(ctx->key, ctx->key2);
+    n_desc = h[0];
+    CK(cudaMemcpyAsync(sc + SC_NDESC, &n_desc, 8, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    CK(cudaEventElapsedTime(&pre_ms, ctx->ev_pre[0], ctx->ev_pre[1]));
+  }
   CK(cudaEventRecord(ctx->ev[2], s));
-  const uint64_t n_desc = ctx->stats[1];
 
   // ---- K3 partition
   CKA(ctx->desc2, desc_cap * 8);
@@ -420,10 +470,13 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
   CK(cudaEventRecord(ctx->ev[5], s));
   CK(cudaStreamSynchronize(s));
   for (int i = 0; i < 4; i++) CK(cudaEventElapsedTime(&ctx->phase_ms[i], ctx->ev[i], ctx->ev[i + 1]));
+  ctx->phase_ms[1] -= pre_ms;  // the scan phase window also spans the pre-count
+  ctx->phase_ms[4] = pre_ms;
   uint64_t nb = 0;
   CK(cudaMemcpy(&nb, d_nbases, 8, cudaMemcpyDeviceToHost));
   ctx->stats[0] = nb;
   ctx->stats[5] = n_out;
+  ctx->stats[1] = n_desc;  // superkmers counted (after the pre-count filter, when on)
   ctx->stats[7] = ctx->skipped;
   ctx->stats[8] = launches;
   ctx->stats[9] = ctx->h2d_bytes;
@@ -503,6 +556,7 @@ int32_t mczi_open(int32_t device, mczi_ctx** out) {
   }
   ctx->stream = ctx->own_stream;
   for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+  for (auto& ev : ctx->ev_pre) cudaEventCreate(&ev);
   *out = ctx;
   return MCZI_OK;
 }
@@ -514,9 +568,11 @@ int32_t mczi_close(mczi_ctx* ctx) {
   DevBuf* bufs[] = {&ctx->text, &ctx->tile_info, &ctx->input_tile0, &ctx->line_sum, &ctx->line_pre, &ctx->line_tmp,
                     &ctx->base_sum, &ctx->base_pre, &ctx->base_tmp, &ctx->packed, &ctx->fbits, &ctx->input_base,
                     &ctx->desc, &ctx->key, &ctx->desc2, &ctx->key2, &ctx->part_hist, &ctx->part_tmp,
-                    &ctx->bucket_off, &ctx->out_lo, &ctx->out_hi, &ctx->out_cnt, &ctx->scalars};
+                    &ctx->bucket_off, &ctx->out_lo, &ctx->out_hi, &ctx->out_cnt, &ctx->scalars,
+                    &ctx->mintab, &ctx->pairtab};
   for (DevBuf* b : bufs) b->release();
   for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
+  for (auto& ev : ctx->ev_pre) if (ev) cudaEventDestroy(ev);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return MCZI_OK;
@@ -658,6 +714,12 @@ int32_t mczi_set_count_options(mczi_ctx* ctx, int32_t chunk, float fill) {
   if (fill < 0.f || fill > 0.85f) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "fill must be in (0, 0.85]");
   ctx->count_chunk = chunk;
   ctx->count_fill = fill;
+  return MCZI_OK;
+}
+
+int32_t mczi_set_minimizer_precount(mczi_ctx* ctx, int32_t enable) {
+  if (!ctx) return MCZI_ERR_STATE;
+  ctx->precount = enable ? 1 : 0;
   return MCZI_OK;
 }
 

@@ -79,6 +79,26 @@ struct PartArgs {
 };
 void launch_partition(const PartArgs& a, cudaStream_t s);
 
+// ---------------------------------------------------------------- K4 pre-count
+struct PrecountArgs {
+  const uint64_t* desc;
+  const uint32_t* key;
+  const unsigned long long* n_desc;   // device scalar
+  unsigned long long* table;          // key << 32 | count, 0 = empty
+  uint64_t mask;                      // slots - 1 (power of two)
+  unsigned long long* pairs;          // fof: key << 32 | (dataset + 1)
+  uint64_t pair_mask;
+  int mode;
+  const uint64_t* dataset_base;
+  int n_datasets;
+  uint64_t threshold;
+  uint64_t* desc_out;
+  uint32_t* key_out;
+  unsigned long long* n_kept;
+  uint32_t* status;
+};
+void launch_precount(const PrecountArgs& a, int sm_count, cudaStream_t s);
+
 // ---------------------------------------------------------------- K5 count
 struct CountArgs {
   const uint32_t* packed;

@@ -200,6 +200,9 @@ class Context:
     def set_count_options(self, chunk: int = 0, fill: float = 0.0) -> None:
         self._ck(self._lib.mczi_set_count_options(self._h, chunk, fill))
 
+    def set_minimizer_precount(self, enable: bool) -> None:
+        self._ck(self._lib.mczi_set_minimizer_precount(self._h, 1 if enable else 0))
+
     def debug_packed(self) -> tuple[np.ndarray, np.ndarray]:
         nb = C.c_uint64()
         self._ck(self._lib.mczi_debug_packed(self._h, None, None, 0, C.byref(nb)))

@@ -233,3 +233,27 @@ def test_path_entry_points(gpu_ctx, oracle, tmp_path):
     out = tmp_path / "o.kff"
     mc.count_inputs_to_kff_path(inputs, cfg, out, ctx=gpu_ctx)
     assert out.read_bytes()[:3] == b"KFF"
+
+
+def test_minimizer_precount_is_conservative(gpu_ctx, oracle):
+    """With the pass-1 minimizer table on, results are unchanged and the
+    filter removes work (superkmers) only."""
+    from mczi_gb300 import gen
+    data = gen.c2_reads(scale=0.001)
+    ds = gen.c3_datasets(n_datasets=5, genome_len=100_000, coverage=(2.0, 5.0))
+    try:
+        for k, m, x in ((63, 21, 3), (31, 21, 2), (25, 11, 0)):
+            gpu_ctx.set_minimizer_precount(False)
+            off = gpu_dict(gpu_ctx, [data], k, m, x)
+            n_off = gpu_ctx.run_stats()[1]
+            gpu_ctx.set_minimizer_precount(True)
+            on = gpu_dict(gpu_ctx, [data], k, m, x)
+            n_on = gpu_ctx.run_stats()[1]
+            assert on == off == oracle_dict(oracle, [data], k, x)
+            assert n_on <= n_off
+        for x in (0, 1, 3):
+            gpu_ctx.set_minimizer_precount(True)
+            on = gpu_dict(gpu_ctx, ds, 31, 21, x, mode=1)
+            assert on == oracle_dict(oracle, ds, 31, x, mode=1)
+    finally:
+        gpu_ctx.set_minimizer_precount(False)
