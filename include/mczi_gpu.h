@@ -145,6 +145,35 @@ int32_t mczi_set_minimizer_precount(mczi_ctx* ctx, int32_t enable);
  * the packed stream; *n_bases receives the base count. */
 int32_t mczi_debug_packed(mczi_ctx* ctx, uint8_t* codes, uint8_t* starts, uint64_t cap, uint64_t* n_bases);
 
+/* ---------------------------------------------------------------- ZI */
+
+/* build_dictionary (src/zi.rs:114-141): indexes the canonical k-mers of the
+ * index FASTA (fragments of length >= k) in a device-resident dictionary --
+ * the 2-bit index stream, its superkmers bucketed by minimizer, a BBHash-style
+ * minimal perfect hash of the minimizers and the bucket offsets -- which
+ * stays on the device until the next build or mczi_close.  k odd in [3, 63],
+ * 0 < m < k (validate_k, src/zi.rs:103-107). */
+int32_t mczi_zi_build(mczi_ctx* ctx, const uint8_t* index_fasta, uint64_t len, uint32_t k, uint32_t m);
+
+/* collect_query_kmers_absent_from_index (src/zi.rs:152-175): the distinct
+ * canonical k-mers of the queries (fragments of length >= k) absent from the
+ * index.  They become the context's result: mczi_result_copy gives them
+ * (counts are the number of absent occurrences), mczi_result_write_fasta
+ * writes them as simplitigs like write_novel_simplitigs (src/zi.rs:177-189). */
+int32_t mczi_zi_query(mczi_ctx* ctx, const mczi_input* queries, size_t n, uint64_t* n_absent);
+
+/* The same for a batch of independent requests (one input each) in one set
+ * of launches: each absent k-mer carries the set of inputs it is absent
+ * from; mczi_zi_input_result extracts one input's sorted absent set, which is
+ * identical to what that input gives when queried alone. */
+int32_t mczi_zi_query_per_input(mczi_ctx* ctx, const mczi_input* queries, size_t n, uint64_t* n_records);
+int32_t mczi_zi_input_result(mczi_ctx* ctx, int32_t input, uint64_t* key_lo, uint64_t* key_hi, uint64_t cap,
+                             uint64_t* n);
+
+/* Index description: [0] built, [1] k, [2] m, [3] index bases, [4] superkmers,
+ * [5] distinct minimizers (MPHF keys), [6] MPHF levels, [7] build time (us). */
+int32_t mczi_zi_info(mczi_ctx* ctx, uint64_t* out, int32_t cap);
+
 /* ------------------------------------------------ packing without allocation */
 
 /* The 2-bit packer of mczi_count's first phase, for callers that cannot

@@ -1,0 +1,148 @@
+// api_internal.h -- the context object and the pipeline stages shared by the
+// MC and ZI host code of libmczi_gpu (not part of the public C ABI).
+#pragma once
+#include "../../include/mczi_gpu.h"
+#include "mczi_internal.h"
+
+#include <string>
+
+namespace mczi {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+// device scalars, in u64 slots
+enum { SC_NDESC = 0, SC_NOUT = 1, SC_STATS = 2, SC_STATUS = 10, SC_WORK = 11, SC_NKEPT = 12, SC_NRUNS = 13,
+       SC_COUNT = 16 };
+
+constexpr int N_PHASES = 5;
+constexpr int MPHF_MAX_LEVELS = 40;
+
+// device-resident SSHash-style dictionary of the ZI index
+struct ZiIndex {
+  bool built = false;
+  int k = 0, m = 0;
+  DevBuf packed;         // the index's 2-bit stream (its own copy)
+  uint64_t pwords = 0;
+  uint64_t n_bases = 0;
+  DevBuf sk;             // superkmer descriptors grouped by bucket
+  DevBuf bucket_off;     // n_keys + 1 offsets into sk (u32)
+  DevBuf bits, rank;     // MPHF bit vector (u64 words) and per-word rank (u32)
+  uint64_t n_keys = 0, n_sk = 0, n_words = 0;
+  int levels = 0;
+  uint64_t lvl_off[MPHF_MAX_LEVELS + 1] = {};
+  uint64_t lvl_size[MPHF_MAX_LEVELS] = {};
+  float build_ms = 0.f;
+};
+
+}  // namespace mczi
+
+struct mczi_ctx {
+  int device = 0;
+  int sm_count = 0;
+  size_t smem_optin = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  mczi::DevBuf text, tile_info, input_tile0, line_sum, line_pre, line_tmp, base_sum, base_pre, base_tmp;
+  mczi::DevBuf packed, fbits, input_base;
+  mczi::DevBuf desc, key, desc2, key2, part_hist, part_tmp, bucket_off;
+  mczi::DevBuf out_lo, out_hi, out_cnt, out_mask;
+  mczi::DevBuf scalars;
+  mczi::DevBuf mintab, pairtab;
+  mczi::DevBuf zi_tmp0, zi_tmp1, zi_tmp2;
+
+  // staged inputs
+  bool staged = false;
+  uint64_t text_len = 0, n_tiles = 0;
+  int n_inputs = 0;
+  uint64_t skipped = 0;
+  uint64_t h2d_bytes = 0;
+
+  // last result
+  bool have_result = false;
+  int mode = 0, k = 0, m = 0;
+  uint64_t x = 0;
+  uint64_t n_out = 0;
+  int mask_words = 0;  // > 0 when the last result carries per-input masks
+  float phase_ms[mczi::N_PHASES] = {0, 0, 0, 0, 0};
+  uint64_t stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  cudaEvent_t ev[mczi::N_PHASES + 1] = {};
+  cudaEvent_t ev_pre[2] = {};
+  int precount = 0;  // pass-1 minimizer table + filter (results identical either way)
+
+  // tuning (0 = per-key-width defaults)
+  int count_threads = 0;
+  int count_slots = 0;
+  int count_ctas_per_sm = 0;
+  float count_fill = 0.f;
+  int count_chunk = 0;
+
+  mczi::ZiIndex zi;
+};
+
+namespace mczi {
+
+int32_t fail(mczi_ctx* c, int32_t code, const std::string& msg);
+int32_t cuda_fail(mczi_ctx* c, cudaError_t e, const char* what);
+
+#define CK(call)                                             \
+  do {                                                       \
+    cudaError_t e_ = (call);                                 \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+#define CKA(buf, bytes)                                                                 \
+  do {                                                                                  \
+    cudaError_t e_ = (buf).ensure(bytes);                                               \
+    if (e_ != cudaSuccess) {                                                            \
+      cudaGetLastError();                                                               \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? MCZI_ERR_OOM : MCZI_ERR_DEVICE, \
+                  std::string("device allocation of ") + std::to_string(bytes) +      \
+                      " bytes failed: " + cudaGetErrorString(e_));                     \
+    }                                                                                   \
+  } while (0)
+
+// state of one pass through the pipeline
+struct Pipe {
+  uint64_t launches = 0;
+  uint64_t desc_cap = 0;
+  uint64_t n_desc = 0;
+  uint64_t pwords = 0;
+  const uint64_t* d_nbases = nullptr;
+  float pre_ms = 0.f;
+};
+
+int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n);
+int32_t pipe_pack(mczi_ctx* ctx, Pipe& p);
+int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m);
+int32_t pipe_precount(mczi_ctx* ctx, Pipe& p, int mode, uint64_t x);
+int32_t pipe_partition(mczi_ctx* ctx, Pipe& p);
+// emit_masks: presence mode only; result records then carry one mask word per
+// 64 inputs (which inputs contain the k-mer)
+int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emit_masks, uint64_t* n_out);
+int32_t pipe_finish(mczi_ctx* ctx, Pipe& p, int mode, int k, int m, uint64_t x, uint64_t n_out);
+
+}  // namespace mczi

@@ -428,6 +428,8 @@ __global__ void k_count(CountArgs a) {
                   a.out_hi[idx] = reinterpret_cast<const K128&>(key).hi;
                 }
                 a.out_count[idx] = c;
+                if (MODE == 1 && a.out_mask)
+                  for (int q = 0; q < W; q++) a.out_mask[idx * W + q] = msk[(size_t)s * W + q];
               } else {
                 set_status(a.status, ST_OUT_OVERFLOW);
               }

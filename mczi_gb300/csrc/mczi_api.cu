@@ -1,17 +1,17 @@
-// mczi_api.cu -- context, device-memory management, MC pipeline orchestration
-// and the C ABI declared in include/mczi_gpu.h.
+// mczi_api.cu -- device-memory management, the MC pipeline stages and the
+// MC half of the C ABI declared in include/mczi_gpu.h.
 //
 // The MC pipeline on one GPU (all intermediate data stays in HBM; the
 // reference round-trips it through temporary partition files):
 //   stage   : inputs -> HBM, each at a PACK_TILE-aligned offset
 //   K1 pack : bytes -> 2-bit packed stream + fragment-start bits
 //   K2 scan : minimizer scan -> superkmer descriptors + partition keys
+//   K4 pre  : (optional) pass-1 minimizer table and superkmer filter
 //   K3 part : two-digit radix partition of the descriptors
 //   K5 count: per-bucket shared-memory counting, threshold, records out
 // Entry points mirror MC's library functions (src/lib.rs:278-524).
-#include "../../include/mczi_gpu.h"
+#include "api_internal.h"
 #include "host_io.h"
-#include "mczi_internal.h"
 #include "mczi_common.cuh"
 #include "scan.cuh"
 
@@ -24,83 +24,7 @@
 
 using namespace mczi;
 
-namespace {
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-  cudaError_t ensure(size_t bytes) {
-    if (bytes == 0) bytes = 16;
-    if (bytes <= cap) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    cudaError_t e = cudaMalloc(&p, bytes);
-    if (e == cudaSuccess) cap = bytes;
-    return e;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-  template <class T>
-  T* as() const {
-    return static_cast<T*>(p);
-  }
-};
-
-// device scalars, in u64 slots
-enum { SC_NDESC = 0, SC_NOUT = 1, SC_STATS = 2, SC_STATUS = 10, SC_WORK = 11, SC_NKEPT = 12, SC_COUNT = 16 };
-
-constexpr int N_PHASES = 5;
-
-}  // namespace
-
-struct mczi_ctx {
-  int device = 0;
-  int sm_count = 0;
-  size_t smem_optin = 0;
-  cudaStream_t own_stream = nullptr;
-  cudaStream_t stream = nullptr;
-  std::string err;
-
-  DevBuf text, tile_info, input_tile0, line_sum, line_pre, line_tmp, base_sum, base_pre, base_tmp;
-  DevBuf packed, fbits, input_base;
-  DevBuf desc, key, desc2, key2, part_hist, part_tmp, bucket_off;
-  DevBuf out_lo, out_hi, out_cnt;
-  DevBuf scalars;
-  DevBuf mintab, pairtab;
-
-  // staged inputs
-  bool staged = false;
-  uint64_t text_len = 0, n_tiles = 0;
-  int n_inputs = 0;
-  uint64_t skipped = 0;
-
-  // last result
-  bool have_result = false;
-  int mode = 0, k = 0, m = 0;
-  uint64_t x = 0;
-  uint64_t n_out = 0;
-  float phase_ms[N_PHASES] = {0, 0, 0, 0, 0};
-  uint64_t stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-  uint64_t h2d_bytes = 0;
-  cudaEvent_t ev[N_PHASES + 1] = {};
-  cudaEvent_t ev_pre[2] = {};
-  int precount = 0;  // pass-1 minimizer table + filter (results identical either way)
-
-  // tuning
-  // 0 = per-key-width defaults measured on GB300: 128-bit keys 1024 threads x
-  // 1 CTA/SM, fill 0.4; 64-bit keys 512 x 2, fill 0.6; 2 windows per item
-  int count_threads = 0;
-  int count_slots = 0;
-  int count_ctas_per_sm = 0;
-  float count_fill = 0.f;
-  int count_chunk = 0;
-};
-
-namespace {
+namespace mczi {
 
 int32_t fail(mczi_ctx* c, int32_t code, const std::string& msg) {
   if (c) c->err = msg;
@@ -111,22 +35,7 @@ int32_t cuda_fail(mczi_ctx* c, cudaError_t e, const char* what) {
   return fail(c, MCZI_ERR_DEVICE, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define CK(call)                                         \
-  do {                                                   \
-    cudaError_t e_ = (call);                             \
-    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
-  } while (0)
-
-#define CKA(buf, bytes)                                                                 \
-  do {                                                                                  \
-    cudaError_t e_ = (buf).ensure(bytes);                                               \
-    if (e_ != cudaSuccess) {                                                            \
-      cudaGetLastError();                                                               \
-      return fail(ctx, e_ == cudaErrorMemoryAllocation ? MCZI_ERR_OOM : MCZI_ERR_DEVICE, \
-                  std::string("device allocation of ") + std::to_string(bytes) +      \
-                      " bytes failed: " + cudaGetErrorString(e_));                     \
-    }                                                                                   \
-  } while (0)
+namespace {
 
 // reference messages: src/lib.rs:110-152
 int32_t validate(mczi_ctx* ctx, const mczi_counter_config* c, int mode) {
@@ -161,6 +70,8 @@ int detect_format(const uint8_t* d, uint64_t n) {
   if (d[i] == '@') return 1;
   return -1;
 }
+
+}  // namespace
 
 int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n) {
   ctx->staged = false;
@@ -220,34 +131,13 @@ int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n) {
   return MCZI_OK;
 }
 
-int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint64_t* n_records) {
-  int32_t rc = validate(ctx, cfg, mode);
-  if (rc) return rc;
-  if (!ctx->staged) return fail(ctx, MCZI_ERR_STATE, "no staged inputs");
-  ctx->have_result = false;
+
+int32_t pipe_pack(mczi_ctx* ctx, Pipe& p) {
   cudaStream_t s = ctx->stream;
-  const int k = (int)cfg->k, m = (int)cfg->minimizer, w = k - m + 1;
   const uint64_t n_tiles = ctx->n_tiles, text_len = ctx->text_len;
   const int n_in = ctx->n_inputs;
-
   CKA(ctx->scalars, SC_COUNT * sizeof(uint64_t));
-  uint64_t* sc = ctx->scalars.as<uint64_t>();
-  CK(cudaMemsetAsync(sc, 0, SC_COUNT * sizeof(uint64_t), s));
-
-  for (int i = 0; i < N_PHASES; i++) ctx->phase_ms[i] = 0.f;
-
-  // fof: the reference returns an empty result when x >= #datasets (src/lib.rs:644-648)
-  if (mode == MCZI_MODE_PRESENCE && cfg->threshold >= (uint64_t)n_in) {
-    ctx->mode = mode; ctx->k = k; ctx->m = m; ctx->x = cfg->threshold;
-    ctx->n_out = 0;
-    std::memset(ctx->stats, 0, sizeof ctx->stats);
-    ctx->stats[9] = ctx->h2d_bytes;
-    ctx->have_result = true;
-    if (n_records) *n_records = 0;
-    return MCZI_OK;
-  }
-
-  // ---- K1 pack
+  CK(cudaMemsetAsync(ctx->scalars.p, 0, SC_COUNT * sizeof(uint64_t), s));
   const uint64_t pwords = text_len / 16 + 8, fwords = text_len / 32 + 8;
   const uint64_t ntmp = n_tiles / SCAN_CHUNK + 2;
   CKA(ctx->packed, pwords * 4);
@@ -261,7 +151,6 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
   CKA(ctx->input_base, ((size_t)n_in + 1) * sizeof(uint64_t));
   CK(cudaMemsetAsync(ctx->packed.p, 0, pwords * 4, s));
   CK(cudaMemsetAsync(ctx->fbits.p, 0, fwords * 4, s));
-
   CK(cudaEventRecord(ctx->ev[0], s));
   PackArgs pa;
   pa.text = ctx->text.as<uint8_t>();
@@ -278,13 +167,20 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
   pa.fbits = ctx->fbits.as<uint32_t>();
   pa.input_base = ctx->input_base.as<uint64_t>();
   launch_pack(pa, s);
-  uint64_t launches = 9;
-  const uint64_t* d_nbases = reinterpret_cast<const uint64_t*>(ctx->base_pre.as<BaseSum>() + n_tiles);
-  CK(cudaMemcpyAsync(ctx->input_base.as<uint64_t>() + n_in, d_nbases, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+  p.launches += 9;
+  p.pwords = pwords;
+  p.d_nbases = reinterpret_cast<const uint64_t*>(ctx->base_pre.as<BaseSum>() + n_tiles);
+  CK(cudaMemcpyAsync(ctx->input_base.as<uint64_t>() + n_in, p.d_nbases, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
   CK(cudaGetLastError());
   CK(cudaEventRecord(ctx->ev[1], s));
+  return MCZI_OK;
+}
 
-  // ---- K2 scan (+ retry on descriptor overflow)
+int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m) {
+  cudaStream_t s = ctx->stream;
+  uint64_t* sc = ctx->scalars.as<uint64_t>();
+  const uint64_t text_len = ctx->text_len;
+  const int w = k - m + 1;
   uint64_t desc_cap = text_len * 3 / (uint64_t)(w + 1) + (1u << 20);
   if (desc_cap > text_len + 1024) desc_cap = text_len + 1024;
   for (int attempt = 0; attempt < 3; attempt++) {
@@ -296,9 +192,9 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
     ScanArgs sa;
     sa.packed = ctx->packed.as<uint32_t>();
     sa.fbits = ctx->fbits.as<uint32_t>();
-    sa.n_bases = d_nbases;
+    sa.n_bases = p.d_nbases;
     sa.max_bases = text_len;
-    sa.packed_words = pwords;
+    sa.packed_words = p.pwords;
     sa.k = k;
     sa.m = m;
     sa.desc = ctx->desc.as<uint64_t>();
@@ -307,72 +203,78 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
     sa.desc_cap = desc_cap;
     sa.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
     launch_scan(sa, s);
-    launches += 1;
+    p.launches += 1;
     CK(cudaGetLastError());
     uint64_t h[2];
     CK(cudaMemcpyAsync(h, sc + SC_NDESC, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(h + 1, sc + SC_STATUS, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (!(h[1] & ST_DESC_OVERFLOW)) {
-      ctx->stats[1] = h[0];
-      break;
+      p.n_desc = h[0];
+      p.desc_cap = desc_cap;
+      return MCZI_OK;
     }
     desc_cap = h[0] + 1024;
-    if (attempt == 2) return fail(ctx, MCZI_ERR_DEVICE, "descriptor buffer overflow persisted");
   }
-  uint64_t n_desc = ctx->stats[1];
-  float pre_ms = 0.f;
-  if (ctx->precount && n_desc > 0) {
-    // ---- K4 pass-1 minimizer table, then keep superkmers whose minimizer count > x
-    uint64_t slots = 1024;
-    while (slots < 2 * n_desc) slots <<= 1;
-    CKA(ctx->mintab, slots * 8);
-    CKA(ctx->desc2, desc_cap * 8);
-    CKA(ctx->key2, desc_cap * 4);
-    CK(cudaMemsetAsync(ctx->mintab.p, 0, slots * 8, s));
-    if (mode == MCZI_MODE_PRESENCE) {
-      CKA(ctx->pairtab, slots * 8);
-      CK(cudaMemsetAsync(ctx->pairtab.p, 0, slots * 8, s));
-    }
-    CK(cudaMemsetAsync(sc + SC_NKEPT, 0, 8, s));
-    CK(cudaEventRecord(ctx->ev_pre[0], s));
-    PrecountArgs pc;
-    pc.desc = ctx->desc.as<uint64_t>();
-    pc.key = ctx->key.as<uint32_t>();
-    pc.n_desc = reinterpret_cast<const unsigned long long*>(sc + SC_NDESC);
-    pc.table = ctx->mintab.as<unsigned long long>();
-    pc.mask = slots - 1;
-    pc.pairs = mode == MCZI_MODE_PRESENCE ? ctx->pairtab.as<unsigned long long>() : nullptr;
-    pc.pair_mask = slots - 1;
-    pc.mode = mode;
-    pc.dataset_base = ctx->input_base.as<uint64_t>();
-    pc.n_datasets = n_in;
-    pc.threshold = cfg->threshold;
-    pc.desc_out = ctx->desc2.as<uint64_t>();
-    pc.key_out = ctx->key2.as<uint32_t>();
-    pc.n_kept = reinterpret_cast<unsigned long long*>(sc + SC_NKEPT);
-    pc.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
-    launch_precount(pc, ctx->sm_count, s);
-    launches += 2;
-    CK(cudaGetLastError());
-    CK(cudaEventRecord(ctx->ev_pre[1], s));
-    uint64_t h[2];
-    CK(cudaMemcpyAsync(h, sc + SC_NKEPT, 8, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(h + 1, sc + SC_STATUS, 8, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (h[1] & ST_MINTAB_FULL) return fail(ctx, MCZI_ERR_DEVICE, "minimizer table full");
-    std::swap(ctx->desc, ctx->desc2);
-    std::swap(ctx->key, ctx->key2);
-    n_desc = h[0];
-    CK(cudaMemcpyAsync(sc + SC_NDESC, &n_desc, 8, cudaMemcpyHostToDevice, s));
-    CK(cudaStreamSynchronize(s));
-    CK(cudaEventElapsedTime(&pre_ms, ctx->ev_pre[0], ctx->ev_pre[1]));
-  }
-  CK(cudaEventRecord(ctx->ev[2], s));
+  return fail(ctx, MCZI_ERR_DEVICE, "descriptor buffer overflow persisted");
+}
 
-  // ---- K3 partition
-  CKA(ctx->desc2, desc_cap * 8);
-  CKA(ctx->key2, desc_cap * 4);
+int32_t pipe_precount(mczi_ctx* ctx, Pipe& p, int mode, uint64_t x) {
+  if (p.n_desc == 0) return MCZI_OK;
+  cudaStream_t s = ctx->stream;
+  uint64_t* sc = ctx->scalars.as<uint64_t>();
+  uint64_t slots = 1024;
+  while (slots < 2 * p.n_desc) slots <<= 1;
+  CKA(ctx->mintab, slots * 8);
+  CKA(ctx->desc2, p.desc_cap * 8);
+  CKA(ctx->key2, p.desc_cap * 4);
+  CK(cudaMemsetAsync(ctx->mintab.p, 0, slots * 8, s));
+  if (mode == MCZI_MODE_PRESENCE) {
+    CKA(ctx->pairtab, slots * 8);
+    CK(cudaMemsetAsync(ctx->pairtab.p, 0, slots * 8, s));
+  }
+  CK(cudaMemsetAsync(sc + SC_NKEPT, 0, 8, s));
+  CK(cudaEventRecord(ctx->ev_pre[0], s));
+  PrecountArgs pc;
+  pc.desc = ctx->desc.as<uint64_t>();
+  pc.key = ctx->key.as<uint32_t>();
+  pc.n_desc = reinterpret_cast<const unsigned long long*>(sc + SC_NDESC);
+  pc.table = ctx->mintab.as<unsigned long long>();
+  pc.mask = slots - 1;
+  pc.pairs = mode == MCZI_MODE_PRESENCE ? ctx->pairtab.as<unsigned long long>() : nullptr;
+  pc.pair_mask = slots - 1;
+  pc.mode = mode;
+  pc.dataset_base = ctx->input_base.as<uint64_t>();
+  pc.n_datasets = ctx->n_inputs;
+  pc.threshold = x;
+  pc.desc_out = ctx->desc2.as<uint64_t>();
+  pc.key_out = ctx->key2.as<uint32_t>();
+  pc.n_kept = reinterpret_cast<unsigned long long*>(sc + SC_NKEPT);
+  pc.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
+  launch_precount(pc, ctx->sm_count, s);
+  p.launches += 2;
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->ev_pre[1], s));
+  uint64_t h[2];
+  CK(cudaMemcpyAsync(h, sc + SC_NKEPT, 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(h + 1, sc + SC_STATUS, 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (h[1] & ST_MINTAB_FULL) return fail(ctx, MCZI_ERR_DEVICE, "minimizer table full");
+  std::swap(ctx->desc, ctx->desc2);
+  std::swap(ctx->key, ctx->key2);
+  p.n_desc = h[0];
+  CK(cudaMemcpyAsync(sc + SC_NDESC, &p.n_desc, 8, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaEventElapsedTime(&p.pre_ms, ctx->ev_pre[0], ctx->ev_pre[1]));
+  return MCZI_OK;
+}
+
+int32_t pipe_partition(mczi_ctx* ctx, Pipe& p) {
+  cudaStream_t s = ctx->stream;
+  uint64_t* sc = ctx->scalars.as<uint64_t>();
+  CK(cudaEventRecord(ctx->ev[2], s));
+  CKA(ctx->desc2, p.desc_cap * 8);
+  CKA(ctx->key2, p.desc_cap * 4);
   const uint64_t nh = (uint64_t)NP1 * PART_CTAS;
   CKA(ctx->part_hist, (2 * nh + 2) * sizeof(uint32_t));
   CKA(ctx->part_tmp, (nh / SCAN_CHUNK + 2) * sizeof(uint32_t));
@@ -383,24 +285,30 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
   qa.desc_out = ctx->desc2.as<uint64_t>();
   qa.key_out = ctx->key2.as<uint32_t>();
   qa.n_desc = reinterpret_cast<const unsigned long long*>(sc + SC_NDESC);
-  qa.desc_cap = desc_cap;
+  qa.desc_cap = p.desc_cap;
   qa.hist = ctx->part_hist.as<uint32_t>();
   qa.hist_tmp = ctx->part_tmp.as<uint32_t>();
   qa.bucket_off = ctx->bucket_off.as<uint64_t>();
   qa.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
-  if (n_desc > 0) {
+  if (p.n_desc > 0) {
     launch_partition(qa, s);
-    launches += 7;
+    p.launches += 7;
   }
   CK(cudaGetLastError());
   CK(cudaEventRecord(ctx->ev[3], s));
+  return MCZI_OK;
+}
 
-  // ---- K5 count (+ retry on result overflow)
+int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emit_masks, uint64_t* n_out_ret) {
+  cudaStream_t s = ctx->stream;
+  uint64_t* sc = ctx->scalars.as<uint64_t>();
   const bool wide = k > 32;
-  const uint64_t est_out = text_len / (cfg->threshold + 1) + 1024;
+  const int n_in = ctx->n_inputs;
+  const int W = (n_in + 63) / 64;
+  const uint64_t est_out = ctx->text_len / (x + 1) + 1024;
   uint64_t out_cap = std::min<uint64_t>(est_out, 1ull << 25);
   uint64_t n_out = 0;
-  if (n_desc > 0) {
+  if (p.n_desc > 0) {
     int threads = ctx->count_threads > 0 ? ctx->count_threads : (wide ? 1024 : 512);
     int cps = ctx->count_ctas_per_sm > 0 ? ctx->count_ctas_per_sm : (wide ? 1 : 2);
     const size_t budget = ctx->smem_optin;  // per block, opt-in
@@ -419,6 +327,7 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
       CKA(ctx->out_lo, out_cap * 8);
       if (wide) CKA(ctx->out_hi, out_cap * 8);
       CKA(ctx->out_cnt, out_cap * 4);
+      if (emit_masks) CKA(ctx->out_mask, out_cap * 8 * (uint64_t)W);
       CK(cudaMemsetAsync(sc + SC_NOUT, 0, 8, s));
       CK(cudaMemsetAsync(sc + SC_STATS, 0, 8 * 8, s));
       CK(cudaMemsetAsync(sc + SC_STATUS, 0, 8, s));
@@ -429,13 +338,14 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
       ca.key = ctx->key.as<uint32_t>();
       ca.bucket_off = ctx->bucket_off.as<uint64_t>();
       ca.k = k;
-      ca.threshold = cfg->threshold;
+      ca.threshold = x;
       ca.mode = mode;
       ca.dataset_base = ctx->input_base.as<uint64_t>();
       ca.n_datasets = n_in;
       ca.out_lo = ctx->out_lo.as<uint64_t>();
       ca.out_hi = wide ? ctx->out_hi.as<uint64_t>() : nullptr;
       ca.out_count = ctx->out_cnt.as<uint32_t>();
+      ca.out_mask = emit_masks ? ctx->out_mask.as<unsigned long long>() : nullptr;
       ca.n_out = reinterpret_cast<unsigned long long*>(sc + SC_NOUT);
       ca.out_cap = out_cap;
       ca.stats = reinterpret_cast<unsigned long long*>(sc + SC_STATS);
@@ -447,7 +357,7 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
       ca.fill = ctx->count_fill > 0.f ? ctx->count_fill : (wide ? 0.4f : 0.6f);
       ca.chunk = ctx->count_chunk > 0 ? (uint32_t)ctx->count_chunk : 2u;
       launch_count(ca, s);
-      launches += 1;
+      p.launches += 1;
       CK(cudaGetLastError());
       uint64_t h[SC_COUNT];
       CK(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, s));
@@ -467,25 +377,63 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
     }
   }
   CK(cudaEventRecord(ctx->ev[4], s));
+  ctx->mask_words = emit_masks ? W : 0;
+  *n_out_ret = n_out;
+  return MCZI_OK;
+}
+
+int32_t pipe_finish(mczi_ctx* ctx, Pipe& p, int mode, int k, int m, uint64_t x, uint64_t n_out) {
+  cudaStream_t s = ctx->stream;
   CK(cudaEventRecord(ctx->ev[5], s));
   CK(cudaStreamSynchronize(s));
   for (int i = 0; i < 4; i++) CK(cudaEventElapsedTime(&ctx->phase_ms[i], ctx->ev[i], ctx->ev[i + 1]));
-  ctx->phase_ms[1] -= pre_ms;  // the scan phase window also spans the pre-count
-  ctx->phase_ms[4] = pre_ms;
+  ctx->phase_ms[1] -= p.pre_ms;  // the scan phase window also spans the pre-count
+  ctx->phase_ms[4] = p.pre_ms;
   uint64_t nb = 0;
-  CK(cudaMemcpy(&nb, d_nbases, 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(&nb, p.d_nbases, 8, cudaMemcpyDeviceToHost));
   ctx->stats[0] = nb;
+  ctx->stats[1] = p.n_desc;  // superkmers counted (after the pre-count filter, when on)
   ctx->stats[5] = n_out;
-  ctx->stats[1] = n_desc;  // superkmers counted (after the pre-count filter, when on)
   ctx->stats[7] = ctx->skipped;
-  ctx->stats[8] = launches;
+  ctx->stats[8] = p.launches;
   ctx->stats[9] = ctx->h2d_bytes;
   ctx->mode = mode;
   ctx->k = k;
   ctx->m = m;
-  ctx->x = cfg->threshold;
+  ctx->x = x;
   ctx->n_out = n_out;
   ctx->have_result = true;
+  return MCZI_OK;
+}
+
+namespace {
+
+int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint64_t* n_records) {
+  int32_t rc = validate(ctx, cfg, mode);
+  if (rc) return rc;
+  if (!ctx->staged) return fail(ctx, MCZI_ERR_STATE, "no staged inputs");
+  ctx->have_result = false;
+  ctx->mask_words = 0;
+  const int k = (int)cfg->k, m = (int)cfg->minimizer;
+  for (int i = 0; i < N_PHASES; i++) ctx->phase_ms[i] = 0.f;
+  // fof: the reference returns an empty result when x >= #datasets (src/lib.rs:644-648)
+  if (mode == MCZI_MODE_PRESENCE && cfg->threshold >= (uint64_t)ctx->n_inputs) {
+    ctx->mode = mode; ctx->k = k; ctx->m = m; ctx->x = cfg->threshold;
+    ctx->n_out = 0;
+    std::memset(ctx->stats, 0, sizeof ctx->stats);
+    ctx->stats[9] = ctx->h2d_bytes;
+    ctx->have_result = true;
+    if (n_records) *n_records = 0;
+    return MCZI_OK;
+  }
+  Pipe p;
+  if ((rc = pipe_pack(ctx, p))) return rc;
+  if ((rc = pipe_scan(ctx, p, k, m))) return rc;
+  if (ctx->precount && (rc = pipe_precount(ctx, p, mode, cfg->threshold))) return rc;
+  if ((rc = pipe_partition(ctx, p))) return rc;
+  uint64_t n_out = 0;
+  if ((rc = pipe_count(ctx, p, k, cfg->threshold, mode, false, &n_out))) return rc;
+  if ((rc = pipe_finish(ctx, p, mode, k, m, cfg->threshold, n_out))) return rc;
   if (n_records) *n_records = n_out;
   return MCZI_OK;
 }
@@ -525,6 +473,8 @@ int32_t count_paths(mczi_ctx* ctx, const char* const* paths, size_t n, const mcz
   if (rc) return rc;
   return kff ? mczi_result_write_kff(ctx, out) : mczi_result_write_fasta(ctx, out);
 }
+
+}  // namespace
 
 }  // namespace
 
@@ -569,7 +519,9 @@ int32_t mczi_close(mczi_ctx* ctx) {
                     &ctx->base_sum, &ctx->base_pre, &ctx->base_tmp, &ctx->packed, &ctx->fbits, &ctx->input_base,
                     &ctx->desc, &ctx->key, &ctx->desc2, &ctx->key2, &ctx->part_hist, &ctx->part_tmp,
                     &ctx->bucket_off, &ctx->out_lo, &ctx->out_hi, &ctx->out_cnt, &ctx->scalars,
-                    &ctx->mintab, &ctx->pairtab};
+                    &ctx->mintab, &ctx->pairtab, &ctx->out_mask, &ctx->zi_tmp0, &ctx->zi_tmp1,
+                    &ctx->zi_tmp2, &ctx->zi.packed, &ctx->zi.sk, &ctx->zi.bucket_off, &ctx->zi.bits,
+                    &ctx->zi.rank};
   for (DevBuf* b : bufs) b->release();
   for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
   for (auto& ev : ctx->ev_pre) if (ev) cudaEventDestroy(ev);

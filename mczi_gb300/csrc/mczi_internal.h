@@ -114,6 +114,7 @@ struct CountArgs {
   uint64_t* out_lo;
   uint64_t* out_hi;           // only for k > 32
   uint32_t* out_count;
+  unsigned long long* out_mask;  // presence mode: W words per record when non-null
   unsigned long long* n_out;
   uint64_t out_cap;
   unsigned long long* stats;  // [0] occurrences inserted, [1] distinct keys, [2] rounds, [3] splits

@@ -1,0 +1,105 @@
+"""ZI on the GPU: subtract a device-resident k-mer index from query k-mers.
+
+Mirrors ZI (``src/zi.rs``): ``validate_k`` (:103-107), ``default_minimizer_size``
+(:109-112), ``build_dictionary`` (:114-141), ``collect_query_kmers_absent_from_index``
+(:152-175) and ``write_novel_simplitigs`` (:177-189).  The dictionary lives in
+HBM inside a :class:`mczi_gb300.mc.Context` and is reused by every query until
+the next build.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Sequence
+
+import numpy as np
+
+from . import _native as N
+from .mc import Context, Records, _inputs_c, _write_through, default_context, read_input
+
+
+def validate_k(k: int) -> None:
+    if not 3 <= k <= 63:
+        raise N.MCZIError(N.MCZI_ERR_INVALID_CONFIG, "k must be in [3, 63] for sshash-rs")
+    if k % 2 == 0:
+        raise N.MCZIError(N.MCZI_ERR_INVALID_CONFIG, "k must be odd for sshash-rs")
+
+
+def default_minimizer_size(k: int) -> int:
+    m = min(19, k - 2)
+    return m if m % 2 == 1 else m - 1
+
+
+def _bytes(x):
+    if isinstance(x, (bytes, bytearray, memoryview, np.ndarray, tuple)):
+        return x
+    return read_input(x)
+
+
+def build_dictionary(index, k: int, m: int | None = None, ctx: Context | None = None) -> Context:
+    """Builds the device dictionary of the canonical k-mers of `index`
+    (a FASTA path or bytes)."""
+    validate_k(k)
+    m = default_minimizer_size(k) if m is None else m
+    if not 0 < m < k:
+        raise N.MCZIError(N.MCZI_ERR_INVALID_CONFIG, "minimizer size must be > 0 and < k")
+    ctx = ctx or default_context()
+    data = _bytes(index)
+    arr, keep = _inputs_c([data])
+    ctx._ck(ctx._lib.mczi_zi_build(ctx.handle, arr[0].data, arr[0].len, k, m))
+    del keep
+    ctx.k = k
+    return ctx
+
+
+def collect_query_kmers_absent_from_index(ctx: Context, queries: Sequence) -> Records:
+    """Distinct canonical query k-mers absent from the index, sorted."""
+    data = [_bytes(q) for q in queries]
+    arr, keep = _inputs_c(data)
+    n = C.c_uint64()
+    ctx._ck(ctx._lib.mczi_zi_query(ctx.handle, arr, len(data), C.byref(n)))
+    del keep
+    return ctx.records(n.value, sorted=True)
+
+
+def query_per_input(ctx: Context, queries: Sequence) -> int:
+    """One batch of independent requests; returns the number of records."""
+    data = [_bytes(q) for q in queries]
+    arr, keep = _inputs_c(data)
+    n = C.c_uint64()
+    ctx._ck(ctx._lib.mczi_zi_query_per_input(ctx.handle, arr, len(data), C.byref(n)))
+    del keep
+    return n.value
+
+
+def input_result(ctx: Context, i: int) -> list[int]:
+    """Sorted absent canonical k-mers of input `i` of the last per-input batch."""
+    n = C.c_uint64()
+    ctx._ck(ctx._lib.mczi_zi_input_result(ctx.handle, i, None, None, 0, C.byref(n)))
+    lo = np.empty(n.value, dtype=np.uint64)
+    hi = np.empty(n.value, dtype=np.uint64)
+    if n.value:
+        ctx._ck(ctx._lib.mczi_zi_input_result(ctx.handle, i, lo.ctypes.data, hi.ctypes.data, n.value, C.byref(n)))
+    return [(int(h) << 64) | int(l) for l, h in zip(lo, hi)]
+
+
+def write_novel_simplitigs(ctx: Context, output_path) -> None:
+    """Simplitig FASTA of the last query's absent set (src/zi.rs:177-189)."""
+    _write_through(output_path, ctx.write_fasta)
+
+
+def info(ctx: Context) -> dict:
+    buf = (C.c_uint64 * 8)()
+    ctx._ck(ctx._lib.mczi_zi_info(ctx.handle, buf, 8))
+    keys = ["built", "k", "m", "index_bases", "superkmers", "minimizers", "mphf_levels", "build_us"]
+    return {k: int(buf[i]) for i, k in enumerate(keys)}
+
+
+def subtract(index, queries: Sequence, k: int, m: int | None = None, output=None,
+             ctx: Context | None = None) -> Records:
+    """ZI's main flow: build, query, write the absent k-mers as simplitigs."""
+    ctx = build_dictionary(index, k, m, ctx)
+    rec = collect_query_kmers_absent_from_index(ctx, queries)
+    if output is not None:
+        write_novel_simplitigs(ctx, output)
+    return rec

@@ -1,0 +1,102 @@
+"""ZI on the GPU against the oracle: absent canonical k-mer sets must be equal."""
+import numpy as np
+import pytest
+
+from oracle_ref import encode, to_int
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_absent(oracle, index, queries, k):
+    lo, hi = oracle.zi_absent(index, queries, k)
+    return to_int(lo, hi)
+
+
+def gpu_absent(ctx, index, queries, k, m):
+    from mczi_gb300 import zi
+    zi.build_dictionary(index, k, m, ctx=ctx)
+    return zi.collect_query_kmers_absent_from_index(ctx, queries).encoded()
+
+
+def rand_seq(rng, n):
+    return rng.choice(np.frombuffer(b"ACGT", dtype=np.uint8), size=n).tobytes()
+
+
+def mutate(rng, s, rate):
+    a = np.frombuffer(s, dtype=np.uint8).copy()
+    pos = rng.random(a.size) < rate
+    a[pos] = rng.choice(np.frombuffer(b"ACGTN", dtype=np.uint8), size=int(pos.sum()))
+    return a.tobytes()
+
+
+def reads(rng, genome, n, L, rate):
+    out = []
+    for i in range(n):
+        p = int(rng.integers(0, max(1, len(genome) - L)))
+        out.append(b">q%d\n" % i + mutate(rng, genome[p:p + L], rate) + b"\n")
+    return b"".join(out)
+
+
+def test_golden_zi(gpu_ctx, golden):
+    z = golden["zi"]
+    got = gpu_absent(gpu_ctx, z["subtract"]["index"].encode(), [z["subtract"]["query"].encode()], 3, 1)
+    assert sorted(got) == sorted(encode(s) for s in z["subtract"]["absent"])
+    got = gpu_absent(gpu_ctx, z["dedup"]["index"].encode(), [z["dedup"]["query"].encode()], 3, 1)
+    assert got == [encode("CCC")]
+
+
+def test_zi_validation(gpu_ctx, golden):
+    from mczi_gb300 import MCZIError, zi
+    for k in golden["zi"]["validate_k"]["ok"]:
+        zi.validate_k(k)
+    for k in golden["zi"]["validate_k"]["err"]:
+        with pytest.raises(MCZIError):
+            zi.validate_k(k)
+    for k, m in golden["zi"]["default_minimizer_size"]:
+        assert zi.default_minimizer_size(k) == m
+    with pytest.raises(MCZIError):
+        zi.build_dictionary(b">i\nACGTACGT\n", 4, 2, ctx=gpu_ctx)
+
+
+@pytest.mark.parametrize("k,m", [(3, 1), (5, 3), (11, 5), (21, 11), (31, 19), (33, 19), (45, 21), (63, 31)])
+def test_zi_random_parity(gpu_ctx, oracle, k, m):
+    rng = np.random.default_rng(k * 31 + m)
+    g = rand_seq(rng, 20000)
+    index = b">g\n" + g[:12000] + b"\n>h\n" + mutate(rng, g[12000:], 0.002) + b"\n"
+    q1 = reads(rng, g, 300, 150, 0.01)
+    q2 = reads(rng, rand_seq(rng, 5000), 100, 120, 0.0)
+    q3 = b">n\nNNNNACGTNN\n>s\nAC\n"
+    assert gpu_absent(gpu_ctx, index, [q1, q2, q3], k, m) == oracle_absent(oracle, index, [q1, q2, q3], k)
+
+
+def test_zi_c4_shape(gpu_ctx, oracle):
+    from mczi_gb300 import gen
+    index, query = gen.c4_index_and_query(genome_len=400_000, query_bases=6_000_000, k=31)
+    assert gpu_absent(gpu_ctx, index, [query], 31, 19) == oracle_absent(oracle, index, [query], 31)
+
+
+def test_zi_per_input_equals_alone(gpu_ctx, oracle):
+    """A request's result is the same alone and in a batch."""
+    from mczi_gb300 import zi
+    rng = np.random.default_rng(3)
+    g = rand_seq(rng, 30000)
+    zi.build_dictionary(b">g\n" + g + b"\n", 31, 19, ctx=gpu_ctx)
+    reqs = [reads(rng, g if i % 2 else rand_seq(rng, 3000), int(rng.integers(1, 80)), 150, 0.01) for i in range(70)]
+    alone = [zi.collect_query_kmers_absent_from_index(gpu_ctx, [r]).encoded() for r in reqs]
+    zi.query_per_input(gpu_ctx, reqs)
+    for i, r in enumerate(reqs):
+        assert zi.input_result(gpu_ctx, i) == alone[i], i
+        assert alone[i] == oracle_absent(oracle, b">g\n" + g + b"\n", [r], 31)
+
+
+def test_zi_fasta_output(gpu_ctx, oracle, tmp_path):
+    from mczi_gb300 import zi
+    rng = np.random.default_rng(9)
+    g = rand_seq(rng, 8000)
+    q = reads(rng, g, 200, 150, 0.02)
+    zi.subtract(b">g\n" + g + b"\n", [q], 31, output=tmp_path / "z.fa", ctx=gpu_ctx)
+    lo, hi = oracle.zi_absent(b">g\n" + g + b"\n", [q], 31)
+    oracle.write_simplitigs(tmp_path / "o.fa", lo, hi, 31)
+    assert (tmp_path / "z.fa").read_bytes() == (tmp_path / "o.fa").read_bytes()
+    info = zi.info(gpu_ctx)
+    assert info["built"] == 1 and info["mphf_levels"] >= 1
