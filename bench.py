@@ -298,6 +298,152 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _record_starts(buf) -> "np.ndarray":
+    import numpy as np
+    return np.flatnonzero(buf == ord(">"))
+
+
+def run_zi(args):
+    """ZI subtraction, batched vs plain: the index is the k-mer set of a 60 Mbp
+    random genome (as overlapping chunks, the same set as MC's k=31 x=1 FASTA of
+    that genome fed twice); the query is 2 Gbp of 150 bp reads, half from that
+    genome and half from an independent one, 1 % errors, split into files.
+    Batched = all files in one set of launches; plain = one pipeline per file
+    (its own launches and syncs), absent sets merged on the host."""
+    import numpy as np
+    import torch
+    from mczi_gb300 import build, gen, zi
+    from mczi_gb300.mc import Context
+    build.build_all()
+    k, m = 31, 19
+    glen = int(60_000_000 * args.scale)
+    qbases = int(2_000_000_000 * args.scale)
+    index, query = gen.c4_index_and_query(genome_len=glen, query_bases=qbases, k=k)
+    starts = _record_starts(query)
+    nfiles = args.zi_files
+    cuts = [int(starts[int(i * len(starts) / nfiles)]) for i in range(nfiles)] + [query.size]
+    files = [query[cuts[i]:cuts[i + 1]] for i in range(nfiles)]
+    windows = int(qbases / 150) * (150 - k + 1)
+    ctx = Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    zi.build_dictionary(index, k, m, ctx=ctx)
+    info = zi.info(ctx)
+    # batched: all files in one set of launches, a result per file (input masks)
+    for _ in range(args.warmup):
+        zi.query_per_input(ctx, files)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        n_rec = zi.query_per_input(ctx, files)
+    torch.cuda.synchronize()
+    batched_s = (time.perf_counter() - t0) / args.steps
+    phases = ctx.phase_times()
+    # plain: one pipeline per file, a result per file
+    lat = []
+    sizes = []
+    t0 = time.perf_counter()
+    for f in files:
+        t1 = time.perf_counter()
+        sizes.append(zi.query(ctx, [f]))
+        lat.append(time.perf_counter() - t1)
+    plain_s = time.perf_counter() - t0
+    # the reference's union semantics (one absent set over all files)
+    t0 = time.perf_counter()
+    n_absent = zi.query(ctx, files)
+    union_s = time.perf_counter() - t0
+    # spot-check: per-file results of the batch equal the per-file runs
+    zi.query_per_input(ctx, files[:4])
+    chk = zi.batch_results(ctx, 4)
+    for i in range(4):
+        assert len(chk[i]) == sizes[i], (i, len(chk[i]), sizes[i])
+    from mczi_gb300.serve import percentile
+    line = {"metric": "ZI queries/s", "value": round(windows / batched_s, 1), "unit": "k-mer lookups/s",
+            "impl": "ours", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "config": {"workload": "zi_subtract_2gbp_k31", "k": k, "m": m, "index_genome_bp": glen,
+                       "index_kmers": info["index_bases"], "query_bases": qbases, "query_files": nfiles,
+                       "mphf_levels": info["mphf_levels"], "minimizers": info["minimizers"],
+                       "index_build_ms": info["build_us"] / 1000.0, "records_batched": n_rec},
+            "batched": {"s": round(batched_s, 4), "lookups_per_s": round(windows / batched_s, 1),
+                        "phases_ms": dict(zip(["pack", "scan", "partition", "dedup_count", "probe"],
+                                              [round(x, 3) for x in phases]))},
+            "plain": {"s": round(plain_s, 4), "lookups_per_s": round(windows / plain_s, 1),
+                      "file_p50_ms": round(percentile(lat, 50) * 1e3, 3),
+                      "file_p99_ms": round(percentile(lat, 99) * 1e3, 3)},
+            "batched_over_plain": round(plain_s / batched_s, 2),
+            "union": {"s": round(union_s, 4), "lookups_per_s": round(windows / union_s, 1), "absent_kmers": n_absent},
+            "data": "synthetic (seeded generator, no dataset)"}
+    ctx.close()
+    print(json.dumps(line), flush=True)
+
+
+def run_zi_serve(args):
+    """ZI serving: the index stays resident; requests of log-uniform size
+    (10 kbp .. max) arrive as a Poisson process at offered loads 0.2 .. 1.0 of
+    the measured batched peak; p50/p99 latency and aggregate lookups/s."""
+    import numpy as np
+    from mczi_gb300 import build, gen, zi
+    from mczi_gb300.mc import Context
+    from mczi_gb300.serve import ZIServer, percentile
+    build.build_all()
+    k, m = 31, 19
+    glen = int(60_000_000 * args.scale)
+    index, pool = gen.c4_index_and_query(genome_len=glen, query_bases=int(args.serve_pool_bases), k=k)
+    starts = _record_starts(pool)
+    rng = np.random.default_rng(5)
+    lo_b, hi_b = 10_000, int(args.serve_max_bytes)
+
+    def make_request():
+        size = int(np.exp(rng.uniform(np.log(lo_b), np.log(hi_b))))
+        i0 = int(rng.integers(0, max(1, len(starts) - 2)))
+        a = int(starts[i0])
+        j = int(np.searchsorted(starts, a + size))
+        b = int(starts[j]) if j < len(starts) else pool.size
+        return pool[a:b].tobytes()
+
+    # measured peak: one large batched request stream
+    ctx = Context(0)
+    zi.build_dictionary(index, k, m, ctx=ctx)
+    probe = [make_request() for _ in range(64)]
+    zi.query_per_input(ctx, probe)
+    t0 = time.perf_counter()
+    zi.query_per_input(ctx, probe)
+    peak_bps = sum(len(p) for p in probe) / (time.perf_counter() - t0)
+    ctx.close()
+    points = []
+    with ZIServer(index, k, m, workers=args.serve_workers, max_batch=64) as srv:
+        for load in (0.2, 0.4, 0.6, 0.8, 1.0):
+            reqs = [make_request() for _ in range(args.serve_requests)]
+            mean = sum(len(r) for r in reqs) / len(reqs)
+            rate = load * peak_bps / mean
+            arr = np.cumsum(rng.exponential(1.0 / rate, size=len(reqs)))
+            futs = []
+            t_start = time.perf_counter()
+            for r, at in zip(reqs, arr):
+                d = t_start + at - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                futs.append(srv.submit(r))
+            for f in futs:
+                f.result()
+            t_end = time.perf_counter()
+            lat = [(f.request.finished - f.request.arrival) * 1e3 for f in futs]
+            win = sum(max(0, len(r) - 2 * (len(r) // 157)) for r in reqs)  # ~bases; lookups ~ bases
+            points.append({"offered_load": load, "requests": len(reqs), "p50_ms": round(percentile(lat, 50), 3),
+                           "p99_ms": round(percentile(lat, 99), 3),
+                           "throughput_bases_per_s": round(sum(len(r) for r in reqs) / (t_end - t_start), 1),
+                           "mean_batch": round(float(np.mean(srv.batch_sizes[-50:])), 2),
+                           "batches": srv.batches, "query_s_total": round(srv.t_query, 3),
+                           "results_s_total": round(srv.t_results, 3)})
+    line = {"metric": "ZI-serve p99 ms", "value": points[-1]["p99_ms"], "unit": "ms", "impl": "ours",
+            "higher_is_better": False, "n_gpus": 1,
+            "config": {"workload": "zi_serve_k31", "index_genome_bp": glen, "workers": args.serve_workers,
+                       "request_bytes": [lo_b, hi_b], "requests_per_load": args.serve_requests,
+                       "peak_bytes_per_s": round(peak_bps, 1)},
+            "sweep": points, "data": "synthetic (seeded generator, no dataset)"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -308,7 +454,17 @@ def main():
     ap.add_argument("--cpu-sample-scale", type=float, default=0.005)
     ap.add_argument("--ref-sample-scale", type=float, default=0.004)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="mc", choices=["mc", "zi", "zi-serve"])
+    ap.add_argument("--zi-files", type=int, default=200)
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-workers", type=int, default=2)
+    ap.add_argument("--serve-max-bytes", type=float, default=20e6)
+    ap.add_argument("--serve-pool-bases", type=float, default=400e6)
     args = ap.parse_args()
+    if args.workload == "zi" and args.impl == "ours":
+        return run_zi(args)
+    if args.workload == "zi-serve" and args.impl == "ours":
+        return run_zi_serve(args)
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":

@@ -170,6 +170,18 @@ int32_t mczi_zi_query_per_input(mczi_ctx* ctx, const mczi_input* queries, size_t
 int32_t mczi_zi_input_result(mczi_ctx* ctx, int32_t input, uint64_t* key_lo, uint64_t* key_hi, uint64_t cap,
                              uint64_t* n);
 
+/* The per-input masks of the last mczi_zi_query_per_input, in the record order
+ * of mczi_result_copy(..., sorted = 0): *words_per_record words per record,
+ * bit i set when the k-mer is absent for input i. */
+int32_t mczi_zi_result_masks(mczi_ctx* ctx, uint64_t* masks, uint64_t cap_words, int32_t* words_per_record);
+
+/* All inputs' absent sets of the last mczi_zi_query_per_input in one pass:
+ * input i's k-mers are key_lo/key_hi[offsets[i] .. offsets[i + 1]) (a set,
+ * in no particular order, like ZI's AHashSet).  offsets holds n_inputs + 1
+ * entries; call with key_lo == NULL to get *total first. */
+int32_t mczi_zi_batch_split(mczi_ctx* ctx, uint64_t* key_lo, uint64_t* key_hi, uint64_t* offsets, uint64_t cap,
+                            uint64_t* total);
+
 /* Index description: [0] built, [1] k, [2] m, [3] index bases, [4] superkmers,
  * [5] distinct minimizers (MPHF keys), [6] MPHF levels, [7] build time (us). */
 int32_t mczi_zi_info(mczi_ctx* ctx, uint64_t* out, int32_t cap);

@@ -83,6 +83,9 @@ SIGNATURES = [
     ("mczi_zi_query_per_input", C.c_int32, [C.c_void_p, C.POINTER(InputC), C.c_size_t, C.POINTER(C.c_uint64)]),
     ("mczi_zi_input_result", C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64,
                                          C.POINTER(C.c_uint64)]),
+    ("mczi_zi_result_masks", C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_int32)]),
+    ("mczi_zi_batch_split", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64,
+                                        C.POINTER(C.c_uint64)]),
     ("mczi_zi_info", C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int32]),
     ("mczi_pack_fastx_noalloc", C.c_int32, [C.c_void_p, C.c_uint64, C.c_int32, C.c_void_p, C.c_uint64, C.c_void_p,
                                             C.c_uint64, C.POINTER(C.c_uint64), C.c_void_p]),

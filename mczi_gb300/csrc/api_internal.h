@@ -11,14 +11,23 @@ namespace mczi {
 struct DevBuf {
   void* p = nullptr;
   size_t cap = 0;
+  // grows by at least half the current size, so a stream of slightly larger
+  // requests does not reallocate (cudaFree synchronises the whole device)
   cudaError_t ensure(size_t bytes) {
     if (bytes == 0) bytes = 16;
     if (bytes <= cap) return cudaSuccess;
+    const size_t want = cap && bytes < cap + cap / 2 ? cap + cap / 2 : bytes;
     if (p) cudaFree(p);
     p = nullptr;
     cap = 0;
-    cudaError_t e = cudaMalloc(&p, bytes);
-    if (e == cudaSuccess) cap = bytes;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess && want > bytes) {
+      cudaGetLastError();
+      e = cudaMalloc(&p, bytes);
+      if (e == cudaSuccess) cap = bytes;
+      return e;
+    }
+    if (e == cudaSuccess) cap = want;
     return e;
   }
   void release() {

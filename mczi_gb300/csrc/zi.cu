@@ -543,6 +543,57 @@ int32_t mczi_zi_input_result(mczi_ctx* ctx, int32_t input, uint64_t* key_lo, uin
   return MCZI_OK;
 }
 
+int32_t mczi_zi_result_masks(mczi_ctx* ctx, uint64_t* masks, uint64_t cap_words, int32_t* words_per_record) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (!ctx->have_result || ctx->mask_words == 0) return fail(ctx, MCZI_ERR_STATE, "no per-input ZI result");
+  if (words_per_record) *words_per_record = ctx->mask_words;
+  if (!masks) return MCZI_OK;
+  const uint64_t need = ctx->n_out * (uint64_t)ctx->mask_words;
+  if (cap_words < need) return fail(ctx, MCZI_ERR_STATE, "mask buffer too small");
+  cudaSetDevice(ctx->device);
+  if (need) {
+    CK(cudaMemcpyAsync(masks, ctx->out_mask.p, need * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return MCZI_OK;
+}
+
+int32_t mczi_zi_batch_split(mczi_ctx* ctx, uint64_t* key_lo, uint64_t* key_hi, uint64_t* offsets, uint64_t cap,
+                            uint64_t* total) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (!ctx->have_result || ctx->mask_words == 0) return fail(ctx, MCZI_ERR_STATE, "no per-input ZI result");
+  cudaSetDevice(ctx->device);
+  const uint64_t nr = ctx->n_out;
+  const int W = ctx->mask_words;
+  const int ni = ctx->n_inputs;
+  std::vector<uint64_t> lo(nr), hi(ctx->k > 32 ? nr : 0), msk(nr * (uint64_t)W);
+  if (nr) {
+    CK(cudaMemcpyAsync(lo.data(), ctx->out_lo.p, nr * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (ctx->k > 32) CK(cudaMemcpyAsync(hi.data(), ctx->out_hi.p, nr * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(msk.data(), ctx->out_mask.p, nr * 8 * W, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  // counting pass: per-input sizes and offsets
+  std::vector<uint64_t> off((size_t)ni + 1, 0);
+  for (uint64_t i = 0; i < nr; i++)
+    for (int q = 0; q < W; q++)
+      for (uint64_t m = msk[i * W + q]; m; m &= m - 1) off[(size_t)q * 64 + __builtin_ctzll(m) + 1]++;
+  for (int i = 0; i < ni; i++) off[i + 1] += off[i];
+  if (total) *total = off[ni];
+  if (offsets) std::copy(off.begin(), off.end(), offsets);
+  if (!key_lo) return MCZI_OK;
+  if (cap < off[ni]) return fail(ctx, MCZI_ERR_STATE, "result buffer too small");
+  std::vector<uint64_t> cur(off.begin(), off.end() - 1);
+  for (uint64_t i = 0; i < nr; i++)
+    for (int q = 0; q < W; q++)
+      for (uint64_t m = msk[i * W + q]; m; m &= m - 1) {
+        const uint64_t o = cur[(size_t)q * 64 + __builtin_ctzll(m)]++;
+        key_lo[o] = lo[i];
+        if (key_hi) key_hi[o] = ctx->k > 32 ? hi[i] : 0;
+      }
+  return MCZI_OK;
+}
+
 int32_t mczi_zi_info(mczi_ctx* ctx, uint64_t* out, int32_t cap) {
   if (!ctx) return MCZI_ERR_STATE;
   const ZiIndex& z = ctx->zi;

@@ -52,14 +52,21 @@ def build_dictionary(index, k: int, m: int | None = None, ctx: Context | None = 
     return ctx
 
 
-def collect_query_kmers_absent_from_index(ctx: Context, queries: Sequence) -> Records:
-    """Distinct canonical query k-mers absent from the index, sorted."""
+def query(ctx: Context, queries: Sequence) -> int:
+    """Runs the subtraction; the absent set stays on the device as the
+    context's result.  Returns its size."""
     data = [_bytes(q) for q in queries]
     arr, keep = _inputs_c(data)
     n = C.c_uint64()
     ctx._ck(ctx._lib.mczi_zi_query(ctx.handle, arr, len(data), C.byref(n)))
     del keep
-    return ctx.records(n.value, sorted=True)
+    return n.value
+
+
+def collect_query_kmers_absent_from_index(ctx: Context, queries: Sequence) -> Records:
+    """Distinct canonical query k-mers absent from the index, sorted."""
+    n = query(ctx, queries)
+    return ctx.records(n, sorted=True)
 
 
 def query_per_input(ctx: Context, queries: Sequence) -> int:
@@ -81,6 +88,24 @@ def input_result(ctx: Context, i: int) -> list[int]:
     if n.value:
         ctx._ck(ctx._lib.mczi_zi_input_result(ctx.handle, i, lo.ctypes.data, hi.ctypes.data, n.value, C.byref(n)))
     return [(int(h) << 64) | int(l) for l, h in zip(lo, hi)]
+
+
+def batch_results(ctx: Context, n_inputs: int) -> list[np.ndarray]:
+    """Every input's absent set from the last per-input batch (unordered, as
+    ZI's set), split in one pass by the library.  k <= 32: 1-D uint64 arrays;
+    k > 32: (n, 2) arrays of (lo, hi)."""
+    total = C.c_uint64()
+    offs = np.empty(n_inputs + 1, dtype=np.uint64)
+    ctx._ck(ctx._lib.mczi_zi_batch_split(ctx.handle, None, None, offs.ctypes.data, 0, C.byref(total)))
+    lo = np.empty(total.value, dtype=np.uint64)
+    hi = np.empty(total.value, dtype=np.uint64)
+    if total.value:
+        ctx._ck(ctx._lib.mczi_zi_batch_split(ctx.handle, lo.ctypes.data, hi.ctypes.data, offs.ctypes.data,
+                                             total.value, C.byref(total)))
+    o = offs.astype(np.int64)
+    if ctx.k <= 32:
+        return [lo[o[i]:o[i + 1]] for i in range(n_inputs)]
+    return [np.stack([lo[o[i]:o[i + 1]], hi[o[i]:o[i + 1]]], axis=1) for i in range(n_inputs)]
 
 
 def write_novel_simplitigs(ctx: Context, output_path) -> None:

@@ -84,8 +84,10 @@ def test_zi_per_input_equals_alone(gpu_ctx, oracle):
     reqs = [reads(rng, g if i % 2 else rand_seq(rng, 3000), int(rng.integers(1, 80)), 150, 0.01) for i in range(70)]
     alone = [zi.collect_query_kmers_absent_from_index(gpu_ctx, [r]).encoded() for r in reqs]
     zi.query_per_input(gpu_ctx, reqs)
+    batch = zi.batch_results(gpu_ctx, len(reqs))
     for i, r in enumerate(reqs):
         assert zi.input_result(gpu_ctx, i) == alone[i], i
+        assert sorted(int(v) for v in batch[i]) == alone[i], i
         assert alone[i] == oracle_absent(oracle, b">g\n" + g + b"\n", [r], 31)
 
 
@@ -100,3 +102,22 @@ def test_zi_fasta_output(gpu_ctx, oracle, tmp_path):
     assert (tmp_path / "z.fa").read_bytes() == (tmp_path / "o.fa").read_bytes()
     info = zi.info(gpu_ctx)
     assert info["built"] == 1 and info["mphf_levels"] >= 1
+
+
+def test_serving_results_match_alone(gpu_ctx, oracle):
+    """Continuous batching: requests submitted while others run are batched,
+    and every request's result equals its result alone."""
+    from mczi_gb300 import zi
+    from mczi_gb300.serve import ZIServer
+    rng = np.random.default_rng(21)
+    g = rand_seq(rng, 40000)
+    index = b">g\n" + g + b"\n"
+    reqs = [reads(rng, g if i % 3 else rand_seq(rng, 4000), int(rng.integers(1, 200)), 150, 0.01) for i in range(60)]
+    zi.build_dictionary(index, 31, 19, ctx=gpu_ctx)
+    alone = [zi.collect_query_kmers_absent_from_index(gpu_ctx, [r]).encoded() for r in reqs]
+    with ZIServer(index, 31, 19, workers=2, max_batch=16, hbm_budget=1 << 30) as srv:
+        futs = [srv.submit(r) for r in reqs]
+        got = [f.result(timeout=120) for f in futs]
+        assert srv.batches < len(reqs)  # requests were batched
+    for i in range(len(reqs)):
+        assert sorted(int(v) for v in got[i]) == alone[i], i
