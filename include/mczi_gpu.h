@@ -133,6 +133,11 @@ int32_t mczi_set_count_tuning(mczi_ctx* ctx, int32_t threads, int32_t table_slot
  * k - m) and the target fill of a counting round's table (0 = default 0.6). */
 int32_t mczi_set_count_options(mczi_ctx* ctx, int32_t chunk, float fill);
 
+/* Counting rounds for threshold >= 1: 1 uses two passes over a shared-memory
+ * bitmap so that k-mers seen once are never stored; 0 uses one claim-or-count
+ * pass; -1 (default) picks two passes for k > 32.  Results are identical. */
+int32_t mczi_set_count_filter(mczi_ctx* ctx, int32_t mode);
+
 /* Pass-1 minimizer pre-count (MC's CompactMinimizerTable / DatasetMinimizerTable,
  * src/lib.rs:4171-4370, filter :4625-4629): when enabled, superkmers whose
  * minimizer count (windows, or datasets in fof mode) is <= threshold are dropped

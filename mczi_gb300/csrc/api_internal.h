@@ -108,6 +108,7 @@ struct mczi_ctx {
   int count_ctas_per_sm = 0;
   float count_fill = 0.f;
   int count_chunk = 0;
+  int count_filter = -1;  // two-pass bitmap-filtered rounds: -1 auto (when x >= 1), 0 off, 1 on
 
   mczi::ZiIndex zi;
 };

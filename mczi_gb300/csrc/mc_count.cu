@@ -105,12 +105,14 @@ size_t count_fixed_smem_bytes(int mode, int n_datasets) {
   return hist + dsb + 96;
 }
 
-size_t count_smem_bytes(int k, int mode, int n_datasets, uint32_t table_slots) {
+size_t count_smem_bytes(int k, int mode, int n_datasets, uint32_t table_slots, uint32_t filter_words) {
   const size_t S = table_slots;
   const size_t keyb = k <= 32 ? 8 : 16;
   size_t b = S * keyb;
   b = (b + 15) & ~(size_t)15;
   b += S * (count_slot_bytes(k, mode, n_datasets) - keyb);
+  b = (b + 15) & ~(size_t)15;
+  b += (size_t)filter_words * 4;
   b = (b + 15) & ~(size_t)15;
   return b + count_fixed_smem_bytes(mode, n_datasets);
 }
@@ -125,6 +127,12 @@ __global__ void k_count(CountArgs a) {
   uint32_t* cnt = reinterpret_cast<uint32_t*>(smem + off);                     // MODE 0
   unsigned long long* msk = reinterpret_cast<unsigned long long*>(smem + off);  // MODE 1
   off += MODE == 0 ? (size_t)S * 4 : (size_t)S * 8 * W;
+  off = (off + 15) & ~(size_t)15;
+  const uint32_t fwords = a.filter_words;  // 0: single-pass rounds
+  const bool filtered = fwords > 0;
+  const uint64_t fbits = (uint64_t)fwords * 32;
+  uint32_t* bmap = reinterpret_cast<uint32_t*>(smem + off);
+  off += (size_t)fwords * 4;
   off = (off + 15) & ~(size_t)15;
   uint32_t* occ = reinterpret_cast<uint32_t*>(smem + off);   // NP2 + 1, becomes occupancy prefix
   off += (NP2 + 1) * sizeof(uint32_t);
@@ -227,7 +235,10 @@ __global__ void k_count(CountArgs a) {
     }
 
     // ---- cut bins into rounds: round id of a bin = floor(occ_prefix / budget)
-    const float budget_f = a.fill * (float)S / s_rho;
+    // single pass: distinct keys of a round must fit the table; filtered:
+    // only repeated keys are stored, and the bitmap holds >= 8 bits per window
+    float budget_f = a.fill * (float)S / s_rho;
+    if (filtered) budget_f = fminf(budget_f, (float)fbits / 8.0f);
     const uint32_t budget = budget_f < 1.0f ? 1u : (uint32_t)budget_f;
     if (tid == 0) s_nrounds = 0;
     __syncthreads();
@@ -268,12 +279,13 @@ __global__ void k_count(CountArgs a) {
         if (tid == 0) { s_sp--; s_nused = 0; s_over = 0; }
         const uint32_t dlo = dst[rr.bl], dhi = dst[rr.bh];
         if (dhi == dlo) { __syncthreads(); continue; }
-        // clear the table
+        // clear the table (and the filter bitmap)
         for (uint32_t i = tid; i < S; i += nth) {
           keys[i] = EMPTY;
           if (MODE == 0) cnt[i] = 0;
           else for (int q = 0; q < W; q++) msk[(size_t)i * W + q] = 0ull;
         }
+        for (uint32_t i = tid; i < fwords; i += nth) bmap[i] = 0u;
         __syncthreads();
         const bool full_range = (rr.hlo == 0u && rr.hhi == 0xffffffffu);
         uint32_t claimed = 0;  // slots this thread claimed in this round
@@ -282,92 +294,125 @@ __global__ void k_count(CountArgs a) {
         // the chunks are spread over all threads, so long and short superkmers
         // keep every lane busy.  A chunk extracts its first k-mer from the
         // packed stream and rolls through the rest.
-        for (uint64_t bb = dlo; bb < dhi; bb += (uint64_t)nth) {
-          const bool has = bb + (uint64_t)tid < dhi;
-          uint64_t dsc = 0;
-          uint32_t nch = 0;
-          if (has) {
-            dsc = a.desc[lo + bb + (uint64_t)tid];
-            const uint32_t len = (uint32_t)(dsc & 0xffffffu) + 1u;
-            nch = (len + chunk - 1) / chunk;
-            if (MODE == 1) {
-              const uint64_t s0 = dsc >> 24;
-              int l2 = 0, h2 = a.n_datasets;  // largest i with dsbase[i] <= s0
-              while (h2 - l2 > 1) { const int mid = (l2 + h2) >> 1; if (dsbase[mid] <= s0) l2 = mid; else h2 = mid; }
-              sh_dset[tid] = (uint16_t)l2;
-            }
-          }
-          sh_desc[tid] = dsc;
-          uint32_t total;
-          sh_cpre[tid] = block_excl_scan_u32(nch, &total, warp_tmp);
-          if (tid == 0) sh_cpre[nth] = total;
-          __syncthreads();
-          const int nd = (int)min((uint64_t)nth, dhi - bb);
-          for (uint32_t c = tid; c < total; c += nth) {
-            if (*(volatile uint32_t*)&s_over) break;
-            int lo2 = 0, hi2 = nd;  // descriptor j: sh_cpre[j] <= c < sh_cpre[j + 1]
-            while (hi2 - lo2 > 1) { const int mid = (lo2 + hi2) >> 1; if (sh_cpre[mid] <= c) lo2 = mid; else hi2 = mid; }
-            const uint64_t d2 = sh_desc[lo2];
-            const uint32_t len = (uint32_t)(d2 & 0xffffffu) + 1u;
-            const uint32_t w0 = (c - sh_cpre[lo2]) * chunk;
-            const uint32_t w1 = min(w0 + chunk, len);
-            const uint32_t dset = MODE == 1 ? (uint32_t)sh_dset[lo2] : 0u;
-            const uint64_t s0 = (d2 >> 24) + w0;
-            R roll;
-            roll.init(k);
-            if constexpr (sizeof(K) == 8) {
-              roll.set(field64(a.packed, s0, k), k);
-            } else {
-              if (k > 32) roll.set(field64(a.packed, s0, k - 32), field64(a.packed, s0 + (uint64_t)(k - 32), 32), k);
-              else roll.set(0ull, field64(a.packed, s0, k), k);
-            }
-            uint64_t p = s0 + (uint64_t)k;
-            uint32_t word = a.packed[p >> 4];
-            for (uint32_t j = w0; j < w1; j++) {
-              if (j > w0) {
-                if ((p & 15) == 0) word = a.packed[p >> 4];
-                roll.push((word >> (30 - 2 * (uint32_t)(p & 15))) & 3u);
-                p++;
+        //   single pass (ph 0): claim-or-count every window;
+        //   filtered (ph 1, 2): pass 1 sets one bitmap bit per window and claims
+        //   a slot only when the bit was already set (a repeat -- or a bitmap
+        //   collision, harmless); pass 2 counts every occurrence of the claimed
+        //   keys with plain-load lookups.  A k-mer seen once is never stored,
+        //   and a k-mer seen twice or more always is, so for x >= 1 the
+        //   emitted set and counts are the same as the single pass.
+        for (int ph = filtered ? 1 : 0; ph <= (filtered ? 2 : 0); ph++) {
+          if (ph == 2) __syncthreads();
+          for (uint64_t bb = dlo; bb < dhi; bb += (uint64_t)nth) {
+            const bool has = bb + (uint64_t)tid < dhi;
+            uint64_t dsc = 0;
+            uint32_t nch = 0;
+            if (has) {
+              dsc = a.desc[lo + bb + (uint64_t)tid];
+              const uint32_t len = (uint32_t)(dsc & 0xffffffu) + 1u;
+              nch = (len + chunk - 1) / chunk;
+              if (MODE == 1) {
+                const uint64_t s0 = dsc >> 24;
+                int l2 = 0, h2 = a.n_datasets;  // largest i with dsbase[i] <= s0
+                while (h2 - l2 > 1) { const int mid = (l2 + h2) >> 1; if (dsbase[mid] <= s0) l2 = mid; else h2 = mid; }
+                sh_dset[tid] = (uint16_t)l2;
               }
-              const K key = roll.canon();
-              const uint64_t hv = key_hash(key);
-              if (!full_range) {
-                const uint32_t hk = (uint32_t)(hv >> 32);
-                if (hk < rr.hlo || hk > rr.hhi) continue;
+            }
+            sh_desc[tid] = dsc;
+            uint32_t total;
+            sh_cpre[tid] = block_excl_scan_u32(nch, &total, warp_tmp);
+            if (tid == 0) sh_cpre[nth] = total;
+            __syncthreads();
+            const int nd = (int)min((uint64_t)nth, dhi - bb);
+            for (uint32_t c = tid; c < total; c += nth) {
+              if (*(volatile uint32_t*)&s_over) break;
+              int lo2 = 0, hi2 = nd;  // descriptor j: sh_cpre[j] <= c < sh_cpre[j + 1]
+              while (hi2 - lo2 > 1) { const int mid = (lo2 + hi2) >> 1; if (sh_cpre[mid] <= c) lo2 = mid; else hi2 = mid; }
+              const uint64_t d2 = sh_desc[lo2];
+              const uint32_t len = (uint32_t)(d2 & 0xffffffu) + 1u;
+              const uint32_t w0 = (c - sh_cpre[lo2]) * chunk;
+              const uint32_t w1 = min(w0 + chunk, len);
+              const uint32_t dset = MODE == 1 ? (uint32_t)sh_dset[lo2] : 0u;
+              const uint64_t s0 = (d2 >> 24) + w0;
+              R roll;
+              roll.init(k);
+              if constexpr (sizeof(K) == 8) {
+                roll.set(field64(a.packed, s0, k), k);
+              } else {
+                if (k > 32) roll.set(field64(a.packed, s0, k - 32), field64(a.packed, s0 + (uint64_t)(k - 32), 32), k);
+                else roll.set(0ull, field64(a.packed, s0, k), k);
               }
-              uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
-              bool done = false;
-              // Probe with plain loads; CAS only on a slot that looks empty.
-              // A slot goes from EMPTY to a key exactly once, so a load that
-              // shows a complete key (no all-ones half) is final; anything
-              // else is resolved by the CAS's atomic snapshot.  The claiming
-              // thread's own occurrence is implicit: a slot's stored count is
-              // (occurrences - 1).  A probe run longer than PROBE_LIMIT means
-              // the table is far past its target fill: the round is split.
-              for (uint32_t probe = 0; probe < PROBE_LIMIT; probe++) {
-                K cur = keys[s];
-                if (KeyOps<K>::maybe_partial(cur)) {
-                  const K prev = KeyOps<K>::cas(&keys[s], EMPTY, key);
-                  if (key_eq(prev, EMPTY)) {
-                    claimed++;
-                    if (MODE == 1) atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
+              uint64_t p = s0 + (uint64_t)k;
+              uint32_t word = a.packed[p >> 4];
+              for (uint32_t j = w0; j < w1; j++) {
+                if (j > w0) {
+                  if ((p & 15) == 0) word = a.packed[p >> 4];
+                  roll.push((word >> (30 - 2 * (uint32_t)(p & 15))) & 3u);
+                  p++;
+                }
+                const K key = roll.canon();
+                const uint64_t hv = key_hash(key);
+                if (!full_range) {
+                  const uint32_t hk = (uint32_t)(hv >> 32);
+                  if (hk < rr.hlo || hk > rr.hhi) continue;
+                }
+                uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
+                if (ph == 2) {
+                  // keys are final during pass 2: plain loads, stop at EMPTY
+                  for (uint32_t probe = 0; probe < PROBE_LIMIT; probe++) {
+                    const K cur = keys[s];
+                    if (key_eq(cur, key)) {
+                      if (MODE == 0) atomicAdd(&cnt[s], 1u);
+                      else atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
+                      break;
+                    }
+                    if (key_eq(cur, EMPTY)) break;
+                    s = (s + 1 == S) ? 0u : s + 1;
+                  }
+                  continue;
+                }
+                if (ph == 1) {
+                  const uint32_t bp = (uint32_t)((((hv * 0x9E3779B97F4A7C15ull) >> 32) * (uint64_t)fbits) >> 32);
+                  const uint32_t bit = 1u << (bp & 31);
+                  if (!(atomicOr(&bmap[bp >> 5], bit) & bit)) continue;  // first sight: not stored
+                }
+                bool done = false;
+                // Probe with plain loads; CAS only on a slot that looks empty.
+                // A slot goes from EMPTY to a key exactly once, so a load that
+                // shows a complete key (no all-ones half) is final; anything
+                // else is resolved by the CAS's atomic snapshot.  In the single
+                // pass the claiming thread's own occurrence is implicit: a
+                // slot's stored count is (occurrences - 1).  A probe run longer
+                // than PROBE_LIMIT means the table is far past its target
+                // fill: the round is split.
+                for (uint32_t probe = 0; probe < PROBE_LIMIT; probe++) {
+                  K cur = keys[s];
+                  if (KeyOps<K>::maybe_partial(cur)) {
+                    const K prev = KeyOps<K>::cas(&keys[s], EMPTY, key);
+                    if (key_eq(prev, EMPTY)) {
+                      claimed++;
+                      if (MODE == 1 && ph == 0) atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
+                      done = true;
+                      break;
+                    }
+                    cur = prev;
+                  }
+                  if (key_eq(cur, key)) {
+                    if (ph == 0) {
+                      if (MODE == 0) atomicAdd(&cnt[s], 1u);
+                      else atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
+                    }
                     done = true;
                     break;
                   }
-                  cur = prev;
+                  s = (s + 1 == S) ? 0u : s + 1;
                 }
-                if (key_eq(cur, key)) {
-                  if (MODE == 0) atomicAdd(&cnt[s], 1u);
-                  else atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
-                  done = true;
-                  break;
-                }
-                s = (s + 1 == S) ? 0u : s + 1;
+                if (!done) { s_over = 1; break; }
               }
-              if (!done) { s_over = 1; break; }
             }
+            __syncthreads();
+            if (s_over) break;
           }
-          __syncthreads();
           if (s_over) break;
         }
         // distinct keys of the round (for the distinct/occurrence estimate)
@@ -408,7 +453,7 @@ __global__ void k_count(CountArgs a) {
           if (s < S) {
             key = keys[s];
             if (!key_eq(key, EMPTY)) {
-              c = MODE == 0 ? cnt[s] + 1u : popc_words(&msk[(size_t)s * W], W);
+              c = MODE == 0 ? cnt[s] + (filtered ? 0u : 1u) : popc_words(&msk[(size_t)s * W], W);
               emit = (uint64_t)c > a.threshold;
             }
           }
@@ -450,7 +495,7 @@ __global__ void k_count(CountArgs a) {
 
 template <class K, class R, int MODE>
 static void launch_one(const CountArgs& a, cudaStream_t s) {
-  const size_t smem = count_smem_bytes(a.k, a.mode, a.n_datasets, a.table_slots);
+  const size_t smem = count_smem_bytes(a.k, a.mode, a.n_datasets, a.table_slots, a.filter_words);
   cudaFuncSetAttribute(k_count<K, R, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k_count<K, R, MODE><<<a.ctas, a.threads, smem, s>>>(a);
 }

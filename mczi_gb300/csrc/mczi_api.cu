@@ -318,10 +318,24 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
     // kernel's static shared memory counts against the same budget
     const size_t stat = count_static_smem(k, mode);
     size_t per_cta = std::min(budget, (size_t)(228 * 1024) / (size_t)cps - 1024) - stat - 64;
-    uint32_t slots = ctx->count_slots > 0 ? (uint32_t)ctx->count_slots
-                                           : (uint32_t)((per_cta - fixed - 64) / slotb);
+    // two-pass (bitmap-filtered) rounds store only repeated k-mers; they need
+    // x >= 1 and leave part of shared memory to the bitmap
+    // auto: long k-mers (k > 32) are mostly singletons in sequencing data, so
+    // storing only repeats pays; short ones mostly repeat (measured on GB300)
+    const bool filt = x >= 1 && (ctx->count_filter > 0 || (ctx->count_filter < 0 && wide));
+    const size_t avail = per_cta - fixed - 128;
+    uint32_t slots, fwords = 0;
+    if (filt) {
+      const double share = wide ? 0.6 : 0.5;
+      slots = ctx->count_slots > 0 ? (uint32_t)ctx->count_slots : (uint32_t)(avail * share / slotb);
+      const size_t used = ((size_t)slots * slotb + 64);
+      fwords = used < avail ? (uint32_t)((avail - used) / 4) & ~31u : 0u;
+      if (fwords < 1024) fwords = 0;  // too small to help: single pass
+    } else {
+      slots = ctx->count_slots > 0 ? (uint32_t)ctx->count_slots : (uint32_t)(avail / slotb);
+    }
     if (slots < (uint32_t)threads) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "counting table smaller than the CTA");
-    if (count_smem_bytes(k, mode, n_in, slots) > budget)
+    if (count_smem_bytes(k, mode, n_in, slots, fwords) > budget)
       return fail(ctx, MCZI_ERR_INVALID_CONFIG, "counting table does not fit in shared memory");
     for (int attempt = 0; attempt < 3; attempt++) {
       CKA(ctx->out_lo, out_cap * 8);
@@ -356,6 +370,7 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       ca.work_counter = reinterpret_cast<unsigned int*>(sc + SC_WORK);
       ca.fill = ctx->count_fill > 0.f ? ctx->count_fill : (wide ? 0.4f : 0.6f);
       ca.chunk = ctx->count_chunk > 0 ? (uint32_t)ctx->count_chunk : 2u;
+      ca.filter_words = fwords;
       launch_count(ca, s);
       p.launches += 1;
       CK(cudaGetLastError());
@@ -666,6 +681,13 @@ int32_t mczi_set_count_options(mczi_ctx* ctx, int32_t chunk, float fill) {
   if (fill < 0.f || fill > 0.85f) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "fill must be in (0, 0.85]");
   ctx->count_chunk = chunk;
   ctx->count_fill = fill;
+  return MCZI_OK;
+}
+
+int32_t mczi_set_count_filter(mczi_ctx* ctx, int32_t mode) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (mode < -1 || mode > 1) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "filter mode must be -1, 0 or 1");
+  ctx->count_filter = mode;
   return MCZI_OK;
 }
 

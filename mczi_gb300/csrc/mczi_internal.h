@@ -125,9 +125,10 @@ struct CountArgs {
   unsigned int* work_counter;
   float fill;                 // target fill of a round's table
   uint32_t chunk;             // windows per work item in the insert phase
+  uint32_t filter_words;      // > 0: two-pass rounds with a bitmap of this many u32 words (needs x >= 1)
 };
 void launch_count(const CountArgs& a, cudaStream_t s);
-size_t count_smem_bytes(int k, int mode, int n_datasets, uint32_t table_slots);
+size_t count_smem_bytes(int k, int mode, int n_datasets, uint32_t table_slots, uint32_t filter_words);
 size_t count_fixed_smem_bytes(int mode, int n_datasets);
 size_t count_slot_bytes(int k, int mode, int n_datasets);
 size_t scan_smem_bytes();

@@ -200,6 +200,10 @@ class Context:
     def set_count_options(self, chunk: int = 0, fill: float = 0.0) -> None:
         self._ck(self._lib.mczi_set_count_options(self._h, chunk, fill))
 
+    def set_count_filter(self, mode: int) -> None:
+        """-1 auto (two-pass rounds when threshold >= 1), 0 single pass, 1 two-pass."""
+        self._ck(self._lib.mczi_set_count_filter(self._h, mode))
+
     def set_minimizer_precount(self, enable: bool) -> None:
         self._ck(self._lib.mczi_set_minimizer_precount(self._h, 1 if enable else 0))
 

@@ -144,8 +144,11 @@ def test_tuning_invariance(gpu_ctx, oracle):
             gpu_ctx.set_count_tuning(threads, slots, cps)
             for chunk, fill in ((1, 0.3), (2, 0.6), (7, 0.85)):
                 gpu_ctx.set_count_options(chunk, fill)
-                assert gpu_dict(gpu_ctx, [data], 31, 21, 1) == ref, (threads, slots, cps, chunk, fill)
+                for filt in (0, 1):
+                    gpu_ctx.set_count_filter(filt)
+                    assert gpu_dict(gpu_ctx, [data], 31, 21, 1) == ref, (threads, slots, cps, chunk, fill, filt)
         gpu_ctx.set_count_options(0, 0.0)
+        gpu_ctx.set_count_filter(-1)
     finally:
         gpu_ctx.set_count_tuning(0, 0, 0)
 
@@ -160,8 +163,13 @@ def test_c1_shape_parity(gpu_ctx, oracle):
 def test_c2_shape_parity(gpu_ctx, oracle):
     from mczi_gb300 import gen
     data = gen.c2_reads(scale=0.002)
-    for x in (3, 0):
-        assert gpu_dict(gpu_ctx, [data], 63, 21, x) == oracle_dict(oracle, [data], 63, x)
+    try:
+        for filt in (-1, 0, 1):
+            gpu_ctx.set_count_filter(filt)
+            for x in (3, 1, 0):
+                assert gpu_dict(gpu_ctx, [data], 63, 21, x) == oracle_dict(oracle, [data], 63, x), (filt, x)
+    finally:
+        gpu_ctx.set_count_filter(-1)
 
 
 def test_fof_parity(gpu_ctx, oracle):
