@@ -117,7 +117,9 @@ size_t count_smem_bytes(int k, int mode, int n_datasets, uint32_t table_slots, u
   return b + count_fixed_smem_bytes(mode, n_datasets);
 }
 
-template <class K, class R, int MODE>
+// KC > 0 compiles the kernel for one k (the shifts and masks of the rolling
+// k-mer become constants); KC == 0 takes k from the arguments
+template <class K, class R, int MODE, int KC>
 __global__ void k_count(CountArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   const uint32_t S = a.table_slots;
@@ -154,7 +156,7 @@ __global__ void k_count(CountArgs a) {
 
   const int tid = threadIdx.x, nth = blockDim.x;
   const int lane = tid & 31;
-  const int k = a.k;
+  const int k = KC > 0 ? KC : a.k;
   const K EMPTY = key_empty<K>();
 
   if (MODE == 1) {
@@ -493,28 +495,38 @@ __global__ void k_count(CountArgs a) {
   }
 }
 
-template <class K, class R, int MODE>
+template <class K, class R, int MODE, int KC>
 static void launch_one(const CountArgs& a, cudaStream_t s) {
   const size_t smem = count_smem_bytes(a.k, a.mode, a.n_datasets, a.table_slots, a.filter_words);
-  cudaFuncSetAttribute(k_count<K, R, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  k_count<K, R, MODE><<<a.ctas, a.threads, smem, s>>>(a);
+  cudaFuncSetAttribute(k_count<K, R, MODE, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_count<K, R, MODE, KC><<<a.ctas, a.threads, smem, s>>>(a);
 }
 
 size_t count_static_smem(int k, int mode) {
   cudaFuncAttributes fa{};
   cudaError_t e;
-  if (k <= 32) e = mode == 0 ? cudaFuncGetAttributes(&fa, k_count<K64, Roll64, 0>) : cudaFuncGetAttributes(&fa, k_count<K64, Roll64, 1>);
-  else e = mode == 0 ? cudaFuncGetAttributes(&fa, k_count<K128, Roll128, 0>) : cudaFuncGetAttributes(&fa, k_count<K128, Roll128, 1>);
+  // every instantiation of a (key width, mode) has the same static shared memory
+  if (k <= 32) e = mode == 0 ? cudaFuncGetAttributes(&fa, k_count<K64, Roll64, 0, 0>) : cudaFuncGetAttributes(&fa, k_count<K64, Roll64, 1, 0>);
+  else e = mode == 0 ? cudaFuncGetAttributes(&fa, k_count<K128, Roll128, 0, 0>) : cudaFuncGetAttributes(&fa, k_count<K128, Roll128, 1, 0>);
   return e == cudaSuccess ? fa.sharedSizeBytes : 4096;
 }
 
 void launch_count(const CountArgs& a, cudaStream_t s) {
   if (a.k <= 32) {
-    if (a.mode == 0) launch_one<K64, Roll64, 0>(a, s);
-    else launch_one<K64, Roll64, 1>(a, s);
+    if (a.mode == 0) {
+      if (a.k == 31) launch_one<K64, Roll64, 0, 31>(a, s);
+      else launch_one<K64, Roll64, 0, 0>(a, s);
+    } else {
+      if (a.k == 31) launch_one<K64, Roll64, 1, 31>(a, s);
+      else launch_one<K64, Roll64, 1, 0>(a, s);
+    }
   } else {
-    if (a.mode == 0) launch_one<K128, Roll128, 0>(a, s);
-    else launch_one<K128, Roll128, 1>(a, s);
+    if (a.mode == 0) {
+      if (a.k == 63) launch_one<K128, Roll128, 0, 63>(a, s);
+      else launch_one<K128, Roll128, 0, 0>(a, s);
+    } else {
+      launch_one<K128, Roll128, 1, 0>(a, s);
+    }
   }
 }
 

@@ -22,6 +22,8 @@ namespace mczi {
 
 namespace {
 
+constexpr int PART_U = 8;  // elements per thread per step
+
 struct SumU32 {
   static __device__ uint32_t identity() { return 0u; }
   static __device__ uint32_t combine(const uint32_t& a, const uint32_t& b) { return a + b; }
@@ -80,7 +82,20 @@ __global__ void __launch_bounds__(PART_THREADS) k_part1_hist(PartArgs a) {
   if (n > a.desc_cap) n = a.desc_cap;
   uint64_t lo, hi;
   slice(n, lo, hi);
-  for (uint64_t i = lo + threadIdx.x; i < hi; i += PART_THREADS) atomicAdd(&h[a.key_in[i] >> (32 - P1_BITS)], 1u);
+  // U independent loads in flight per thread (the loop is latency-bound otherwise)
+  for (uint64_t i0 = lo; i0 < hi; i0 += (uint64_t)PART_THREADS * PART_U) {
+    uint32_t kk[PART_U];
+#pragma unroll
+    for (int u = 0; u < PART_U; u++) {
+      const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
+      kk[u] = i < hi ? a.key_in[i] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < PART_U; u++) {
+      const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
+      if (i < hi) atomicAdd(&h[kk[u] >> (32 - P1_BITS)], 1u);
+    }
+  }
   __syncthreads();
   for (int i = threadIdx.x; i < NP1; i += PART_THREADS) a.hist[(uint64_t)i * PART_CTAS + blockIdx.x] = h[i];
 }
@@ -98,11 +113,24 @@ __global__ void __launch_bounds__(PART_THREADS) k_part1_scatter(PartArgs a, cons
   if (n > a.desc_cap) n = a.desc_cap;
   uint64_t lo, hi;
   slice(n, lo, hi);
-  for (uint64_t i = lo + threadIdx.x; i < hi; i += PART_THREADS) {
-    const uint32_t key = a.key_in[i];
-    const uint32_t pos = atomicAdd(&cur[key >> (32 - P1_BITS)], 1u);
-    a.desc_out[pos] = a.desc_in[i];
-    a.key_out[pos] = key;
+  for (uint64_t i0 = lo; i0 < hi; i0 += (uint64_t)PART_THREADS * PART_U) {
+    uint32_t kk[PART_U];
+    uint64_t dd[PART_U];
+#pragma unroll
+    for (int u = 0; u < PART_U; u++) {
+      const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
+      kk[u] = i < hi ? a.key_in[i] : 0u;
+      dd[u] = i < hi ? a.desc_in[i] : 0ull;
+    }
+#pragma unroll
+    for (int u = 0; u < PART_U; u++) {
+      const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
+      if (i < hi) {
+        const uint32_t pos = atomicAdd(&cur[kk[u] >> (32 - P1_BITS)], 1u);
+        a.desc_out[pos] = dd[u];
+        a.key_out[pos] = kk[u];
+      }
+    }
   }
 }
 
@@ -114,15 +142,39 @@ __global__ void __launch_bounds__(PART_THREADS) k_part2(PartArgs a) {
   if (hi <= lo) return;
   for (int i = threadIdx.x; i < NP2; i += PART_THREADS) h[i] = 0;
   __syncthreads();
-  for (uint64_t i = lo + threadIdx.x; i < hi; i += PART_THREADS)
-    atomicAdd(&h[(a.key_out[i] >> (32 - P1_BITS - P2_BITS)) & (NP2 - 1)], 1u);
+  for (uint64_t i0 = lo; i0 < hi; i0 += (uint64_t)PART_THREADS * PART_U) {
+    uint32_t kk[PART_U];
+#pragma unroll
+    for (int u = 0; u < PART_U; u++) {
+      const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
+      kk[u] = i < hi ? a.key_out[i] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < PART_U; u++) {
+      const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
+      if (i < hi) atomicAdd(&h[(kk[u] >> (32 - P1_BITS - P2_BITS)) & (NP2 - 1)], 1u);
+    }
+  }
   __syncthreads();
   smem_exclusive_scan<NP2>(h, nullptr);
-  for (uint64_t i = lo + threadIdx.x; i < hi; i += PART_THREADS) {
-    const uint32_t key = a.key_out[i];
-    const uint32_t pos = atomicAdd(&h[(key >> (32 - P1_BITS - P2_BITS)) & (NP2 - 1)], 1u);
-    const_cast<uint64_t*>(a.desc_in)[lo + pos] = a.desc_out[i];
-    const_cast<uint32_t*>(a.key_in)[lo + pos] = key;
+  for (uint64_t i0 = lo; i0 < hi; i0 += (uint64_t)PART_THREADS * PART_U) {
+    uint32_t kk[PART_U];
+    uint64_t dd[PART_U];
+#pragma unroll
+    for (int u = 0; u < PART_U; u++) {
+      const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
+      kk[u] = i < hi ? a.key_out[i] : 0u;
+      dd[u] = i < hi ? a.desc_out[i] : 0ull;
+    }
+#pragma unroll
+    for (int u = 0; u < PART_U; u++) {
+      const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
+      if (i < hi) {
+        const uint32_t pos = atomicAdd(&h[(kk[u] >> (32 - P1_BITS - P2_BITS)) & (NP2 - 1)], 1u);
+        const_cast<uint64_t*>(a.desc_in)[lo + pos] = dd[u];
+        const_cast<uint32_t*>(a.key_in)[lo + pos] = kk[u];
+      }
+    }
   }
 }
 

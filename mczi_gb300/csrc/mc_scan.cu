@@ -69,7 +69,10 @@ __device__ __forceinline__ uint64_t bits64(const uint32_t* sfb, uint32_t q) {
 
 }  // namespace
 
-size_t scan_smem_bytes() { return (size_t)(PKW + FBW + 3 * HL) * sizeof(uint32_t); }
+constexpr int MVL = SCAN_TILE + SCAN_TILE / 32 + 2;  // padded minimizer values
+constexpr int VBW = SCAN_TILE / 32;                   // validity bitmask words
+
+size_t scan_smem_bytes() { return (size_t)(PKW + FBW + 3 * HL + MVL + VBW) * sizeof(uint32_t); }
 
 __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   extern __shared__ __align__(16) uint32_t dyn[];
@@ -78,6 +81,8 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   uint32_t* sh_h = sfb + FBW;
   uint32_t* sh_pl = sh_h + HL;
   uint32_t* sh_sr = sh_pl + HL;
+  uint32_t* sh_mv = sh_sr + HL;
+  uint32_t* sh_vb = sh_mv + MVL;
   uint32_t* ev = sh_h;  // reused once the minima are known: pos | start << 13 | rank << 14
   __shared__ Cnt2 shc[SCAN_THREADS + 1];
   __shared__ unsigned long long s_base;
@@ -117,20 +122,28 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   }
   __syncthreads();
 
-  // per window: minimizer value, validity, run events
+  // per window: minimizer value and validity, computed with consecutive
+  // threads on consecutive windows (conflict-free), kept as a padded array and
+  // a bitmask for the per-thread run logic below
+  const uint64_t vmask = (k - 1) >= 64 ? ~0ull : ((1ull << (k - 1)) - 1);
+  for (int r = tid; r < SCAN_TILE; r += SCANK_THREADS) {
+    const uint64_t gi = t0 + (uint64_t)r;
+    bool v = (gi + (uint64_t)k <= nb);
+    if (v && k > 1) v = (bits64(sfb, (uint32_t)(r + 1)) & vmask) == 0;
+    const unsigned bal = __ballot_sync(0xffffffffu, v);
+    if ((tid & 31) == 0) sh_vb[r >> 5] = bal;
+    sh_mv[r + (r >> 5)] = min(sh_sr[r], sh_pl[r + w - 1]);
+  }
+  __syncthreads();
   const int r0 = tid * WPT;
   uint32_t mv[WPT + 1];
   bool vd[WPT + 1];
-  const uint64_t vmask = (k - 1) >= 64 ? ~0ull : ((1ull << (k - 1)) - 1);
 #pragma unroll
   for (int i = 0; i <= WPT; i++) {
     const int r = r0 + i - 1;  // i = 0 is the window before this thread's range
     if (r < 0) { vd[i] = false; mv[i] = 0; continue; }
-    const uint64_t gi = t0 + (uint64_t)r;
-    bool v = (gi + (uint64_t)k <= nb);
-    if (v && k > 1) v = (bits64(sfb, (uint32_t)(r + 1)) & vmask) == 0;
-    vd[i] = v;
-    mv[i] = min(sh_sr[r], sh_pl[r + w - 1]);
+    vd[i] = (sh_vb[r >> 5] >> (r & 31)) & 1u;
+    mv[i] = sh_mv[r + (r >> 5)];
   }
   Cnt2 c{0, 0};
 #pragma unroll
@@ -173,7 +186,7 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
     const uint32_t r = v & 0x1fffu;
     const uint32_t end = ev[e + 1] & 0x1fffu;
     const uint32_t len = end - r;
-    const uint32_t mval = min(sh_sr[r], sh_pl[r + w - 1]);
+    const uint32_t mval = sh_mv[r + (r >> 5)];
     const uint64_t d = base + (v >> 14);
     a.desc[d] = ((t0 + r) << 24) | (uint64_t)(len - 1);
     a.key[d] = mix32(mval);
