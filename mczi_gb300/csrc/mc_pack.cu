@@ -65,6 +65,12 @@ struct NlOp {
   }
 };
 
+// exact per-byte zero test: high bit of each byte set where the byte is 0
+__device__ __forceinline__ uint32_t zero_bytes(uint32_t x) {
+  const uint32_t y = ((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x;
+  return ~y & 0x80808080u;
+}
+
 __device__ __forceinline__ void load_tile(const uint8_t* __restrict__ text, uint64_t tile, uint8_t* sb) {
   const uint4* src = reinterpret_cast<const uint4*>(text + tile * PACK_TILE);
   uint4* dst = reinterpret_cast<uint4*>(sb);
@@ -79,10 +85,18 @@ __device__ __forceinline__ uint32_t thread_state(const uint8_t* sb, bool fastq, 
                                                  uint32_t tile_line4, int first) {
   __shared__ NlSum sh[SCAN_THREADS + 1];
   NlSum mine{-1, 0};
-  for (int i = 0; i < PACK_PER_THREAD; i++) {
-    if (sb[first + i] == '\n') {
-      mine.last = first + i;
-      mine.nl++;
+  {
+    // newlines of this thread's 32 bytes, four at a time
+    const uint4 v0 = *reinterpret_cast<const uint4*>(sb + first);
+    const uint4 v1 = *reinterpret_cast<const uint4*>(sb + first + 16);
+    const uint32_t w[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const uint32_t z = zero_bytes(w[j] ^ 0x0a0a0a0au);
+      if (z) {
+        mine.nl += __popc(z);
+        mine.last = first + 4 * j + (31 - __clz(z)) / 8;
+      }
     }
   }
   NlSum tot;
@@ -123,6 +137,30 @@ __device__ __forceinline__ uint32_t step_fastq(uint32_t c, uint32_t& line) {
   if (c == '\r') return 5;
   int8_t code = code_of(c);
   return code < 0 ? 4u : (uint32_t)code;
+}
+
+// Fast path for 32 bytes that are all A/C/G/T (either case): returns true and
+// the 32 MC codes MSB-first in *codes.  One u32 holds 4 bytes, first byte in
+// the low bits.
+__device__ __forceinline__ bool acgt32(const uint8_t* src, uint64_t* codes) {
+  const uint4 v0 = *reinterpret_cast<const uint4*>(src);
+  const uint4 v1 = *reinterpret_cast<const uint4*>(src + 16);
+  const uint32_t w[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+  uint32_t ok = 0x80808080u;
+  uint64_t c = 0;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const uint32_t l = w[j] | 0x20202020u;
+    ok &= zero_bytes(l ^ 0x61616161u) | zero_bytes(l ^ 0x63636363u) | zero_bytes(l ^ 0x67676767u) |
+          zero_bytes(l ^ 0x74747474u);
+    // a0 c1 g3 t2 from bits 1-2, then MC's A0 C1 G2 T3 by x ^ (x >> 1)
+    const uint32_t t = (w[j] >> 1) & 0x03030303u;
+    const uint32_t mc = t ^ ((t >> 1) & 0x01010101u);
+    const uint32_t v8 = ((mc & 3u) << 6) | (((mc >> 8) & 3u) << 4) | (((mc >> 16) & 3u) << 2) | ((mc >> 24) & 3u);
+    c |= (uint64_t)v8 << (56 - 8 * j);
+  }
+  *codes = c;
+  return ok == 0x80808080u;
 }
 
 __device__ __forceinline__ void tile_line_state(const uint8_t* __restrict__ text, const uint32_t* __restrict__ tile_info,
@@ -217,11 +255,17 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_count(const uint8_t* __re
   const int first = threadIdx.x * PACK_PER_THREAD;
   uint32_t st = thread_state(sb, fastq, tst, tl4, first);
   BaseSum s{0, 0, 0, 0};
-  for (int i = 0; i < PACK_PER_THREAD; i++) {
-    uint32_t c = sb[first + i];
-    uint32_t r = fastq ? step_fastq(c, st) : step_fasta(c, st);
-    if (r < 4) { s.nb++; s.lb = 0; }
-    else if (r == 4) { if (s.nb == 0) s.fb = 1; s.lb = 1; }
+  uint64_t codes;
+  const bool seq_line = fastq ? ((st & 3u) == 1u) : (st != HDR);
+  if (seq_line && acgt32(sb + first, &codes)) {
+    s.nb = PACK_PER_THREAD;  // 32 bases, no break
+  } else {
+    for (int i = 0; i < PACK_PER_THREAD; i++) {
+      uint32_t c = sb[first + i];
+      uint32_t r = fastq ? step_fastq(c, st) : step_fasta(c, st);
+      if (r < 4) { s.nb++; s.lb = 0; }
+      else if (r == 4) { if (s.nb == 0) s.fb = 1; s.lb = 1; }
+    }
   }
   // for nb == 0 lb means "any break"; for nb > 0 fb is a break before the first base
   BaseSum tot;
@@ -238,7 +282,7 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __re
                                                              uint64_t* __restrict__ input_base) {
   __shared__ __align__(16) uint8_t sb[PACK_TILE];
   __shared__ BaseSum shs[SCAN_THREADS + 1];
-  __shared__ uint32_t spk[PACK_TILE / 16 + 2];
+  __shared__ uint32_t spk[PACK_TILE / 16 + 3];
   __shared__ uint32_t sfb[PACK_TILE / 32 + 2];
   const uint64_t tile = blockIdx.x;
   if (tile >= n_tiles) return;
@@ -251,13 +295,20 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __re
   __syncthreads();
   const int first = threadIdx.x * PACK_PER_THREAD;
   const uint32_t st0 = thread_state(sb, fastq, tst, tl4, first);
-  // pass A: this thread's summary
+  // pass A: this thread's summary (all-ACGT chunks take the fast path)
   uint32_t st = st0;
   BaseSum s{0, 0, 0, 0};
-  for (int i = 0; i < PACK_PER_THREAD; i++) {
-    uint32_t r = fastq ? step_fastq(sb[first + i], st) : step_fasta(sb[first + i], st);
-    if (r < 4) { s.nb++; s.lb = 0; }
-    else if (r == 4) { if (s.nb == 0) s.fb = 1; s.lb = 1; }
+  uint64_t codes = 0;
+  const bool seq_line = fastq ? ((st & 3u) == 1u) : (st != HDR);
+  const bool fast = seq_line && acgt32(sb + first, &codes);
+  if (fast) {
+    s.nb = PACK_PER_THREAD;
+  } else {
+    for (int i = 0; i < PACK_PER_THREAD; i++) {
+      uint32_t r = fastq ? step_fastq(sb[first + i], st) : step_fasta(sb[first + i], st);
+      if (r < 4) { s.nb++; s.lb = 0; }
+      else if (r == 4) { if (s.nb == 0) s.fb = 1; s.lb = 1; }
+    }
   }
   BaseSum tot;
   const BaseSum tile_pre = base_pre[tile];
@@ -269,15 +320,25 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __re
   uint64_t p = excl.nb;
   uint32_t pending = (excl.nb == 0) ? 1u : excl.lb;
   st = st0;
-  for (int i = 0; i < PACK_PER_THREAD; i++) {
-    uint32_t r = fastq ? step_fastq(sb[first + i], st) : step_fasta(sb[first + i], st);
-    if (r < 4) {
-      atomicOr(&spk[(p >> 4) - w0], r << (30 - 2 * (uint32_t)(p & 15)));
-      if (pending) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
-      pending = 0;
-      p++;
-    } else if (r == 4) {
-      pending = 1;
+  if (fast) {
+    // 32 bases at p: spread the 64 code bits over (up to) three staging words
+    const uint64_t q = (p >> 4) - w0;
+    const uint32_t r2 = 2 * (uint32_t)(p & 15);
+    atomicOr(&spk[q], (uint32_t)(codes >> (32 + r2)));
+    atomicOr(&spk[q + 1], (uint32_t)(codes >> r2));
+    if (r2) atomicOr(&spk[q + 2], (uint32_t)(codes << (32 - r2)));
+    if (pending) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
+  } else {
+    for (int i = 0; i < PACK_PER_THREAD; i++) {
+      uint32_t r = fastq ? step_fastq(sb[first + i], st) : step_fasta(sb[first + i], st);
+      if (r < 4) {
+        atomicOr(&spk[(p >> 4) - w0], r << (30 - 2 * (uint32_t)(p & 15)));
+        if (pending) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
+        pending = 0;
+        p++;
+      } else if (r == 4) {
+        pending = 1;
+      }
     }
   }
   __syncthreads();

@@ -17,25 +17,48 @@ constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_PER_THREAD = 8;
 constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_PER_THREAD;
 
-// Exclusive block scan of one value per thread; returns the exclusive prefix
-// for this thread and writes the block total to *total (all threads).
+// shuffle of a small trivially-copyable struct, 32 bits at a time
+template <class T>
+__device__ __forceinline__ T shfl_up_T(const T& v, int d) {
+  static_assert(sizeof(T) % 4 == 0, "scan element must be a multiple of 4 bytes");
+  T r;
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(&v);
+  uint32_t* dst = reinterpret_cast<uint32_t*>(&r);
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(T) / 4); i++) dst[i] = __shfl_up_sync(0xffffffffu, src[i], d);
+  return r;
+}
+
+// Exclusive block scan of one value per thread (warp shuffles, then the warp
+// totals); returns this thread's exclusive prefix and writes the block total
+// to *total (all threads).  sh needs SCAN_THREADS / 32 + 1 entries.
 template <class T, class Op>
-__device__ T block_exclusive_scan(T v, T* total, T* sh /* SCAN_THREADS + 1 */) {
-  const int t = threadIdx.x;
-  sh[t] = v;
-  __syncthreads();
-  // Hillis-Steele inclusive scan in shared memory (256 entries, 8 steps)
-  for (int d = 1; d < SCAN_THREADS; d <<= 1) {
-    T other = (t >= d) ? sh[t - d] : Op::identity();
-    __syncthreads();
-    if (t >= d) sh[t] = Op::combine(other, sh[t]);
-    __syncthreads();
+__device__ T block_exclusive_scan(T v, T* total, T* sh) {
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  constexpr int NW = SCAN_THREADS / 32;
+  T incl = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const T o = shfl_up_T(incl, d);
+    if (lane >= d) incl = Op::combine(o, incl);
   }
-  T incl = sh[t];
-  T excl = (t == 0) ? Op::identity() : sh[t - 1];
-  *total = sh[SCAN_THREADS - 1];
+  if (lane == 31) sh[wid] = incl;
   __syncthreads();
-  (void)incl;
+  if (t == 0) {
+    T run = Op::identity();
+    for (int w = 0; w < NW; w++) {
+      const T x = sh[w];
+      sh[w] = run;
+      run = Op::combine(run, x);
+    }
+    sh[NW] = run;
+  }
+  __syncthreads();
+  T excl = shfl_up_T(incl, 1);
+  if (lane == 0) excl = Op::identity();
+  excl = Op::combine(sh[wid], excl);
+  *total = sh[NW];
+  __syncthreads();
   return excl;
 }
 
