@@ -182,8 +182,9 @@ __global__ void k_count(CountArgs a) {
     for (int i = tid; i <= NP2; i += nth) { occ[i] = 0; dst[i] = 0; }
     __syncthreads();
     for (uint64_t i = lo + tid; i < hi; i += nth) {
-      const uint32_t bin = (a.key[i] >> (32 - P1_BITS - P2_BITS)) & (NP2 - 1);
-      const uint32_t len = (uint32_t)(a.desc[i] & 0xffffffu) + 1u;
+      const uint64_t bd = a.desc[i];
+      const uint32_t bin = bd_p2(bd);
+      const uint32_t len = bd_windows(bd);
       atomicAdd(&occ[bin], len);
       atomicAdd(&dst[bin], 1u);
     }
@@ -311,10 +312,10 @@ __global__ void k_count(CountArgs a) {
             uint32_t nch = 0;
             if (has) {
               dsc = a.desc[lo + bb + (uint64_t)tid];
-              const uint32_t len = (uint32_t)(dsc & 0xffffffu) + 1u;
+              const uint32_t len = bd_windows(dsc);
               nch = (len + chunk - 1) / chunk;
               if (MODE == 1) {
-                const uint64_t s0 = dsc >> 24;
+                const uint64_t s0 = bd_start(dsc);
                 int l2 = 0, h2 = a.n_datasets;  // largest i with dsbase[i] <= s0
                 while (h2 - l2 > 1) { const int mid = (l2 + h2) >> 1; if (dsbase[mid] <= s0) l2 = mid; else h2 = mid; }
                 sh_dset[tid] = (uint16_t)l2;
@@ -331,11 +332,11 @@ __global__ void k_count(CountArgs a) {
               int lo2 = 0, hi2 = nd;  // descriptor j: sh_cpre[j] <= c < sh_cpre[j + 1]
               while (hi2 - lo2 > 1) { const int mid = (lo2 + hi2) >> 1; if (sh_cpre[mid] <= c) lo2 = mid; else hi2 = mid; }
               const uint64_t d2 = sh_desc[lo2];
-              const uint32_t len = (uint32_t)(d2 & 0xffffffu) + 1u;
+              const uint32_t len = bd_windows(d2);
               const uint32_t w0 = (c - sh_cpre[lo2]) * chunk;
               const uint32_t w1 = min(w0 + chunk, len);
               const uint32_t dset = MODE == 1 ? (uint32_t)sh_dset[lo2] : 0u;
-              const uint64_t s0 = (d2 >> 24) + w0;
+              const uint64_t s0 = bd_start(d2) + w0;
               R roll;
               roll.init(k);
               if constexpr (sizeof(K) == 8) {
@@ -374,7 +375,9 @@ __global__ void k_count(CountArgs a) {
                   continue;
                 }
                 if (ph == 1) {
-                  const uint32_t bp = (uint32_t)((((hv * 0x9E3779B97F4A7C15ull) >> 32) * (uint64_t)fbits) >> 32);
+                  // bitmap position from hash bits 20..51 (the slot uses the low
+                  // 32 bits, range splits bits 32..63)
+                  const uint32_t bp = (uint32_t)((((hv >> 20) & 0xffffffffull) * (uint64_t)fbits) >> 32);
                   const uint32_t bit = 1u << (bp & 31);
                   if (!(atomicOr(&bmap[bp >> 5], bit) & bit)) continue;  // first sight: not stored
                 }

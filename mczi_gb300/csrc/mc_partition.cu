@@ -4,16 +4,17 @@
 // Replaces MC's superkmer partition writers (src/lib.rs:3483-3560,
 // 4821-4925: partition = spread_hash_u32(minimizer) % P, one temp file per
 // partition).  Here the buckets stay in HBM.  The key (mix32 of the minimizer
-// value) is consumed as two 12-bit digits:
+// value) is consumed as two digits (12 + 11 bits):
 //   pass 1 (global): p1 = key >> 20.  A fixed grid of PART_CTAS CTAs each owns a
 //           contiguous slice; per-CTA shared-memory histograms are written as
 //           hist[p1][cta], scanned, and each CTA scatters its slice with
 //           shared-memory cursors (no global atomics on the data path).
-//   pass 2 (per bucket): p2 = (key >> 8) & 0xfff, one CTA per p1 bucket,
+//   pass 2 (per bucket): p2 = the next 11 key bits, one CTA per p1 bucket,
 //           histogram + scan + scatter inside the bucket's range, back into
 //           the original buffers.
 // The descriptors end up grouped by (p1, p2); the counting kernel carves
-// each p1 bucket into rounds of consecutive p2 bins.
+// each p1 bucket into rounds of consecutive p2 bins.  Pass 1 drops the key:
+// each superkmer becomes one u64 (start, windows, p2) -- see bd_make.
 #include "mczi_internal.h"
 #include "mczi_common.cuh"
 #include "scan.cuh"
@@ -127,14 +128,15 @@ __global__ void __launch_bounds__(PART_THREADS) k_part1_scatter(PartArgs a, cons
       const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
       if (i < hi) {
         const uint32_t pos = atomicAdd(&cur[kk[u] >> (32 - P1_BITS)], 1u);
-        a.desc_out[pos] = dd[u];
-        a.key_out[pos] = kk[u];
+        // one u64 per superkmer from here on: the p1 digit is the bucket
+        a.desc_out[pos] = bd_make(dd[u] >> 24, (uint32_t)(dd[u] & 0xffffffu) + 1u,
+                                  (kk[u] >> (32 - P1_BITS - P2_BITS)) & (NP2 - 1));
       }
     }
   }
 }
 
-// pass 2: one CTA per p1 bucket, from (desc_out, key_out) back to (desc_in, key_in)
+// pass 2: one CTA per p1 bucket, from desc_out back to desc_in (u64 records)
 __global__ void __launch_bounds__(PART_THREADS) k_part2(PartArgs a) {
   __shared__ uint32_t h[NP2];
   const int b = blockIdx.x;
@@ -143,36 +145,33 @@ __global__ void __launch_bounds__(PART_THREADS) k_part2(PartArgs a) {
   for (int i = threadIdx.x; i < NP2; i += PART_THREADS) h[i] = 0;
   __syncthreads();
   for (uint64_t i0 = lo; i0 < hi; i0 += (uint64_t)PART_THREADS * PART_U) {
-    uint32_t kk[PART_U];
+    uint64_t dd[PART_U];
 #pragma unroll
     for (int u = 0; u < PART_U; u++) {
       const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
-      kk[u] = i < hi ? a.key_out[i] : 0u;
+      dd[u] = i < hi ? a.desc_out[i] : 0ull;
     }
 #pragma unroll
     for (int u = 0; u < PART_U; u++) {
       const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
-      if (i < hi) atomicAdd(&h[(kk[u] >> (32 - P1_BITS - P2_BITS)) & (NP2 - 1)], 1u);
+      if (i < hi) atomicAdd(&h[bd_p2(dd[u])], 1u);
     }
   }
   __syncthreads();
   smem_exclusive_scan<NP2>(h, nullptr);
   for (uint64_t i0 = lo; i0 < hi; i0 += (uint64_t)PART_THREADS * PART_U) {
-    uint32_t kk[PART_U];
     uint64_t dd[PART_U];
 #pragma unroll
     for (int u = 0; u < PART_U; u++) {
       const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
-      kk[u] = i < hi ? a.key_out[i] : 0u;
       dd[u] = i < hi ? a.desc_out[i] : 0ull;
     }
 #pragma unroll
     for (int u = 0; u < PART_U; u++) {
       const uint64_t i = i0 + (uint64_t)u * PART_THREADS + threadIdx.x;
       if (i < hi) {
-        const uint32_t pos = atomicAdd(&h[(kk[u] >> (32 - P1_BITS - P2_BITS)) & (NP2 - 1)], 1u);
+        const uint32_t pos = atomicAdd(&h[bd_p2(dd[u])], 1u);
         const_cast<uint64_t*>(a.desc_in)[lo + pos] = dd[u];
-        const_cast<uint32_t*>(a.key_in)[lo + pos] = kk[u];
       }
     }
   }

@@ -163,6 +163,17 @@ __device__ __forceinline__ uint64_t field64_s(const uint32_t* w, uint32_t rel, i
   return n == 32 ? top : (top >> (64 - 2 * n));
 }
 
+// Superkmer descriptors.  Before the partition: u64 start << 24 | (windows-1)
+// plus a u32 key.  From partition pass 1 on, the bucket (p1 digit) is implicit
+// and one u64 carries start << 23 | (windows-1) << 11 | p2 (windows <= 4096,
+// p2 < 2048, start < 2^41).
+__host__ __device__ __forceinline__ uint64_t bd_make(uint64_t start, uint32_t windows, uint32_t p2) {
+  return (start << 23) | ((uint64_t)(windows - 1) << 11) | (uint64_t)p2;
+}
+__host__ __device__ __forceinline__ uint64_t bd_start(uint64_t bd) { return bd >> 23; }
+__host__ __device__ __forceinline__ uint32_t bd_windows(uint64_t bd) { return (uint32_t)((bd >> 11) & 0xfffu) + 1u; }
+__host__ __device__ __forceinline__ uint32_t bd_p2(uint64_t bd) { return (uint32_t)(bd & 0x7ffu); }
+
 // canonical m-mer hash: the minimizer order (strand-symmetric by construction)
 __device__ __forceinline__ uint32_t mmer_hash64(uint64_t canon) {
   uint64_t x = canon * 0x9E3779B97F4A7C15ull;
