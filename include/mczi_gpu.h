@@ -138,6 +138,12 @@ int32_t mczi_set_count_options(mczi_ctx* ctx, int32_t chunk, float fill);
  * pass; -1 (default) picks two passes for k > 32.  Results are identical. */
 int32_t mczi_set_count_filter(mczi_ctx* ctx, int32_t mode);
 
+/* Inputs with more superkmers than one pass holds are counted in passes over
+ * disjoint ranges of the minimizer key (each pass rescans the packed stream).
+ * 0 (default) picks the number from the input size and free HBM; 1..64 forces
+ * it.  Results are identical. */
+int32_t mczi_set_key_range_passes(mczi_ctx* ctx, int32_t passes);
+
 /* Pass-1 minimizer pre-count (MC's CompactMinimizerTable / DatasetMinimizerTable,
  * src/lib.rs:4171-4370, filter :4625-4629): when enabled, superkmers whose
  * minimizer count (windows, or datasets in fof mode) is <= threshold are dropped

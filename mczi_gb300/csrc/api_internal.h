@@ -30,6 +30,22 @@ struct DevBuf {
     if (e == cudaSuccess) cap = want;
     return e;
   }
+  // grows like ensure() but keeps the first `keep` bytes
+  cudaError_t grow_keep(size_t bytes, size_t keep, cudaStream_t s) {
+    if (bytes <= cap) return cudaSuccess;
+    if (!p || keep == 0) return ensure(bytes);
+    const size_t want = bytes < cap + cap / 2 ? cap + cap / 2 : bytes;
+    void* np = nullptr;
+    cudaError_t e = cudaMalloc(&np, want);
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(np, p, keep, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { cudaFree(np); return e; }
+    cudaFree(p);
+    p = np;
+    cap = want;
+    return cudaSuccess;
+  }
   void release() {
     if (p) cudaFree(p);
     p = nullptr;
@@ -108,7 +124,8 @@ struct mczi_ctx {
   int count_ctas_per_sm = 0;
   float count_fill = 0.f;
   int count_chunk = 0;
-  int count_filter = -1;  // two-pass bitmap-filtered rounds: -1 auto (when x >= 1), 0 off, 1 on
+  int count_filter = -1;
+  int key_passes = 0;  // 0 = chosen from the input size and free HBM  // two-pass bitmap-filtered rounds: -1 auto (when x >= 1), 0 off, 1 on
 
   mczi::ZiIndex zi;
 };
@@ -140,19 +157,26 @@ struct Pipe {
   uint64_t launches = 0;
   uint64_t desc_cap = 0;
   uint64_t n_desc = 0;
+  uint64_t n_desc_total = 0;
   uint64_t pwords = 0;
   const uint64_t* d_nbases = nullptr;
   float pre_ms = 0.f;
+  float ms[mczi::N_PHASES] = {0, 0, 0, 0, 0};  // accumulated over key-range passes
 };
 
 int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n);
 int32_t pipe_pack(mczi_ctx* ctx, Pipe& p);
-int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m);
+int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m, uint32_t p1_lo = 0, uint32_t p1_hi = 1u << 12,
+                  uint32_t passes = 1);
 int32_t pipe_precount(mczi_ctx* ctx, Pipe& p, int mode, uint64_t x);
 int32_t pipe_partition(mczi_ctx* ctx, Pipe& p);
 // emit_masks: presence mode only; result records then carry one mask word per
 // 64 inputs (which inputs contain the k-mer)
-int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emit_masks, uint64_t* n_out);
+// append: keep the records of earlier key-range passes (out_base of them)
+int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emit_masks, uint64_t* n_out,
+                   bool append = false);
+// number of key-range passes a staged batch needs (descriptor memory, 32-bit counters)
+uint32_t key_range_passes(mczi_ctx* ctx, int k, int m);
 int32_t pipe_finish(mczi_ctx* ctx, Pipe& p, int mode, int k, int m, uint64_t x, uint64_t n_out);
 
 }  // namespace mczi

@@ -145,14 +145,18 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
     vd[i] = (sh_vb[r >> 5] >> (r & 31)) & 1u;
     mv[i] = sh_mv[r + (r >> 5)];
   }
+  // key-range pass: only superkmers whose p1 digit is in [p1_lo, p1_hi) are
+  // emitted; every start still ends the run before it
+  const uint32_t p1_lo = a.p1_lo, p1_hi = a.p1_hi;
   Cnt2 c{0, 0};
 #pragma unroll
   for (int i = 1; i <= WPT; i++) {
     const int r = r0 + i - 1;
     const bool start = vd[i] && (r == 0 || !vd[i - 1] || mv[i] != mv[i - 1]);
     const bool term = !vd[i] && r > 0 && vd[i - 1];
+    const uint32_t p1 = mix32(mv[i]) >> (32 - P1_BITS);
     c.ev += (start || term);
-    c.st += start;
+    c.st += start && p1 >= p1_lo && p1 < p1_hi;
   }
   Cnt2 tot;
   const Cnt2 pre = block_exclusive_scan<Cnt2, Cnt2Op>(c, &tot, shc);
@@ -164,11 +168,13 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
       const int r = r0 + i - 1;
       const bool start = vd[i] && (r == 0 || !vd[i - 1] || mv[i] != mv[i - 1]);
       const bool term = !vd[i] && r > 0 && vd[i - 1];
+      const uint32_t p1 = mix32(mv[i]) >> (32 - P1_BITS);
+      const bool emit = start && p1 >= p1_lo && p1 < p1_hi;
       if (start || term) {
-        ev[e] = (uint32_t)r | ((uint32_t)start << 13) | (sr << 14);
+        ev[e] = (uint32_t)r | ((uint32_t)emit << 13) | (sr << 14);
         e++;
       }
-      sr += start;
+      sr += emit;
     }
   }
   if (tid == 0) {

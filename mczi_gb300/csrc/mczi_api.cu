@@ -16,6 +16,7 @@
 #include "scan.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
@@ -176,12 +177,24 @@ int32_t pipe_pack(mczi_ctx* ctx, Pipe& p) {
   return MCZI_OK;
 }
 
-int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m) {
+uint32_t key_range_passes(mczi_ctx* ctx, int k, int m) {
+  if (ctx->key_passes > 0) return (uint32_t)ctx->key_passes;
+  const int w = k - m + 1;
+  const double est = (double)ctx->text_len * 2.0 / (double)(w + 1);  // expected superkmers
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { cudaGetLastError(); free_b = 8ull << 30; }
+  // descriptors (12 B) + their pass-1 copy (8 B) + precount/partition slack
+  const double per_pass = std::min((double)(1u << 30) * 1.5, (double)free_b * 0.45 / 24.0);
+  uint32_t r = (uint32_t)std::ceil(est * 1.3 / per_pass);
+  return std::max(1u, std::min(r, 64u));
+}
+
+int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m, uint32_t p1_lo, uint32_t p1_hi, uint32_t passes) {
   cudaStream_t s = ctx->stream;
   uint64_t* sc = ctx->scalars.as<uint64_t>();
   const uint64_t text_len = ctx->text_len;
   const int w = k - m + 1;
-  uint64_t desc_cap = text_len * 3 / (uint64_t)(w + 1) + (1u << 20);
+  uint64_t desc_cap = text_len * 3 / (uint64_t)(w + 1) / passes + (1u << 20);
   if (desc_cap > text_len + 1024) desc_cap = text_len + 1024;
   for (int attempt = 0; attempt < 3; attempt++) {
     if (desc_cap >= 0xffffffffull) return fail(ctx, MCZI_ERR_OOM, "input batch too large: more than 2^32 superkmers");
@@ -202,6 +215,8 @@ int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m) {
     sa.n_desc = reinterpret_cast<unsigned long long*>(sc + SC_NDESC);
     sa.desc_cap = desc_cap;
     sa.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
+    sa.p1_lo = p1_lo;
+    sa.p1_hi = p1_hi;
     launch_scan(sa, s);
     p.launches += 1;
     CK(cudaGetLastError());
@@ -299,15 +314,27 @@ int32_t pipe_partition(mczi_ctx* ctx, Pipe& p) {
   return MCZI_OK;
 }
 
-int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emit_masks, uint64_t* n_out_ret) {
+int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emit_masks, uint64_t* n_out_ret,
+                   bool append) {
   cudaStream_t s = ctx->stream;
   uint64_t* sc = ctx->scalars.as<uint64_t>();
   const bool wide = k > 32;
   const int n_in = ctx->n_inputs;
   const int W = (n_in + 63) / 64;
   const uint64_t est_out = ctx->text_len / (x + 1) + 1024;
-  uint64_t out_cap = std::min<uint64_t>(est_out, 1ull << 25);
-  uint64_t n_out = 0;
+  const uint64_t prior = append ? *n_out_ret : 0;  // records of earlier key-range passes
+  uint64_t out_cap = std::max<uint64_t>(std::min<uint64_t>(est_out, 1ull << 25), prior + (1u << 20));
+  if (append && ctx->out_lo.cap / 8 > out_cap) out_cap = ctx->out_lo.cap / 8;
+  uint64_t n_out = prior;
+#define CKG(buf, bytes, keep)                                                            \
+  do {                                                                                   \
+    cudaError_t e_ = (buf).grow_keep((bytes), (keep), s);                                \
+    if (e_ != cudaSuccess) {                                                             \
+      cudaGetLastError();                                                                \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? MCZI_ERR_OOM : MCZI_ERR_DEVICE, \
+                  std::string("device allocation failed: ") + cudaGetErrorString(e_));  \
+    }                                                                                    \
+  } while (0)
   if (p.n_desc > 0) {
     int threads = ctx->count_threads > 0 ? ctx->count_threads : (wide ? 1024 : 512);
     int cps = ctx->count_ctas_per_sm > 0 ? ctx->count_ctas_per_sm : (wide ? 1 : 2);
@@ -338,11 +365,12 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
     if (count_smem_bytes(k, mode, n_in, slots, fwords) > budget)
       return fail(ctx, MCZI_ERR_INVALID_CONFIG, "counting table does not fit in shared memory");
     for (int attempt = 0; attempt < 3; attempt++) {
-      CKA(ctx->out_lo, out_cap * 8);
-      if (wide) CKA(ctx->out_hi, out_cap * 8);
-      CKA(ctx->out_cnt, out_cap * 4);
-      if (emit_masks) CKA(ctx->out_mask, out_cap * 8 * (uint64_t)W);
-      CK(cudaMemsetAsync(sc + SC_NOUT, 0, 8, s));
+      // grow the result buffers keeping earlier passes' records
+      CKG(ctx->out_lo, out_cap * 8, prior * 8);
+      if (wide) CKG(ctx->out_hi, out_cap * 8, prior * 8);
+      CKG(ctx->out_cnt, out_cap * 4, prior * 4);
+      if (emit_masks) CKG(ctx->out_mask, out_cap * 8 * (uint64_t)W, prior * 8 * (uint64_t)W);
+      CK(cudaMemcpyAsync(sc + SC_NOUT, &prior, 8, cudaMemcpyHostToDevice, s));
       CK(cudaMemsetAsync(sc + SC_STATS, 0, 8 * 8, s));
       CK(cudaMemsetAsync(sc + SC_STATUS, 0, 8, s));
       CK(cudaMemsetAsync(sc + SC_WORK, 0, 8, s));
@@ -380,14 +408,14 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       const uint32_t st = (uint32_t)h[SC_STATUS];
       if (st & ST_TABLE_STUCK) return fail(ctx, MCZI_ERR_DEVICE, "counting round could not be split further");
       if (st & ST_OUT_OVERFLOW) {
-        out_cap = h[SC_NOUT] + 1024;
+        out_cap = h[SC_NOUT] + (1u << 20);
         continue;
       }
       n_out = h[SC_NOUT];
-      ctx->stats[2] = h[SC_STATS + 2];
-      ctx->stats[3] = h[SC_STATS + 3];
-      ctx->stats[4] = h[SC_STATS + 1];
-      ctx->stats[6] = h[SC_STATS + 0];
+      ctx->stats[2] += h[SC_STATS + 2];
+      ctx->stats[3] += h[SC_STATS + 3];
+      ctx->stats[4] += h[SC_STATS + 1];
+      ctx->stats[6] += h[SC_STATS + 0];
       break;
     }
   }
@@ -401,13 +429,18 @@ int32_t pipe_finish(mczi_ctx* ctx, Pipe& p, int mode, int k, int m, uint64_t x, 
   cudaStream_t s = ctx->stream;
   CK(cudaEventRecord(ctx->ev[5], s));
   CK(cudaStreamSynchronize(s));
-  for (int i = 0; i < 4; i++) CK(cudaEventElapsedTime(&ctx->phase_ms[i], ctx->ev[i], ctx->ev[i + 1]));
-  ctx->phase_ms[1] -= p.pre_ms;  // the scan phase window also spans the pre-count
-  ctx->phase_ms[4] = p.pre_ms;
+  for (int i = 0; i < 4; i++) {
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, ctx->ev[i], ctx->ev[i + 1]));
+    p.ms[i] += t;
+  }
+  p.ms[1] -= p.pre_ms;  // the scan phase window also spans the pre-count
+  p.ms[4] += p.pre_ms;
+  for (int i = 0; i < N_PHASES; i++) ctx->phase_ms[i] = p.ms[i];
   uint64_t nb = 0;
   CK(cudaMemcpy(&nb, p.d_nbases, 8, cudaMemcpyDeviceToHost));
   ctx->stats[0] = nb;
-  ctx->stats[1] = p.n_desc;  // superkmers counted (after the pre-count filter, when on)
+  ctx->stats[1] = p.n_desc_total;  // superkmers counted (after the pre-count filter, when on)
   ctx->stats[5] = n_out;
   ctx->stats[7] = ctx->skipped;
   ctx->stats[8] = p.launches;
@@ -442,12 +475,36 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
     return MCZI_OK;
   }
   Pipe p;
+  std::memset(ctx->stats, 0, sizeof ctx->stats);
+  // inputs with more superkmers than one pass can hold are counted in passes
+  // over disjoint ranges of the partition key (disjoint sets of k-mers);
+  // decided before any launch (it queries free memory)
+  const uint32_t passes = key_range_passes(ctx, k, m);
   if ((rc = pipe_pack(ctx, p))) return rc;
-  if ((rc = pipe_scan(ctx, p, k, m))) return rc;
-  if (ctx->precount && (rc = pipe_precount(ctx, p, mode, cfg->threshold))) return rc;
-  if ((rc = pipe_partition(ctx, p))) return rc;
   uint64_t n_out = 0;
-  if ((rc = pipe_count(ctx, p, k, cfg->threshold, mode, false, &n_out))) return rc;
+  for (uint32_t r = 0; r < passes; r++) {
+    const uint32_t lo = (uint32_t)((uint64_t)NP1 * r / passes), hi = (uint32_t)((uint64_t)NP1 * (r + 1) / passes);
+    if (r > 0) {
+      // time each pass's phases; the pack ran once
+      for (int i = 0; i < 4; i++) {
+        float t = 0.f;
+        CK(cudaEventSynchronize(ctx->ev[i + 1]));
+        CK(cudaEventElapsedTime(&t, ctx->ev[i], ctx->ev[i + 1]));
+        p.ms[i] += t;
+      }
+      p.ms[1] -= p.pre_ms;
+      p.ms[4] += p.pre_ms;
+      p.pre_ms = 0.f;
+      // later passes have no pack: their pack window is empty
+      CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+      CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+    }
+    if ((rc = pipe_scan(ctx, p, k, m, lo, hi, passes))) return rc;
+    if (ctx->precount && (rc = pipe_precount(ctx, p, mode, cfg->threshold))) return rc;
+    if ((rc = pipe_partition(ctx, p))) return rc;
+    if ((rc = pipe_count(ctx, p, k, cfg->threshold, mode, false, &n_out, r > 0))) return rc;
+    p.n_desc_total += p.n_desc;
+  }
   if ((rc = pipe_finish(ctx, p, mode, k, m, cfg->threshold, n_out))) return rc;
   if (n_records) *n_records = n_out;
   return MCZI_OK;
@@ -681,6 +738,13 @@ int32_t mczi_set_count_options(mczi_ctx* ctx, int32_t chunk, float fill) {
   if (fill < 0.f || fill > 0.85f) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "fill must be in (0, 0.85]");
   ctx->count_chunk = chunk;
   ctx->count_fill = fill;
+  return MCZI_OK;
+}
+
+int32_t mczi_set_key_range_passes(mczi_ctx* ctx, int32_t passes) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (passes < 0 || passes > 64) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "passes must be in [0, 64]");
+  ctx->key_passes = passes;
   return MCZI_OK;
 }
 

@@ -38,6 +38,10 @@ struct PackArgs {
 };
 void launch_pack(const PackArgs& a, cudaStream_t s);
 
+// partition digits of the superkmer key (mix32 of the minimizer value)
+constexpr int P1_BITS = 12;
+constexpr int P2_BITS = 11;
+
 // ---------------------------------------------------------------- K2 scan
 constexpr int SCAN_TILE = 4096;     // windows per CTA
 constexpr int SCANK_THREADS = 256;
@@ -54,12 +58,11 @@ struct ScanArgs {
   unsigned long long* n_desc;  // device counter
   uint64_t desc_cap;
   uint32_t* status;
+  uint32_t p1_lo, p1_hi;     // emit superkmers with key >> (32 - P1_BITS) in [p1_lo, p1_hi)
 };
 void launch_scan(const ScanArgs& a, cudaStream_t s);
 
 // ---------------------------------------------------------------- K3 partition
-constexpr int P1_BITS = 12;
-constexpr int P2_BITS = 11;
 constexpr int NP1 = 1 << P1_BITS;
 constexpr int NP2 = 1 << P2_BITS;
 constexpr int PART_CTAS = 304;   // 2 per SM on a 152-SM GB300

@@ -417,6 +417,7 @@ int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, u
   ctx->have_result = false;
   ctx->mask_words = 0;
   for (int i = 0; i < N_PHASES; i++) ctx->phase_ms[i] = 0.f;
+  std::memset(ctx->stats, 0, sizeof ctx->stats);
   cudaStream_t s = ctx->stream;
   Pipe p;
   if ((rc = pipe_pack(ctx, p))) return rc;
@@ -482,6 +483,7 @@ int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, u
   ctx->phase_ms[4] = probe_ms;
   ctx->stats[1] = n_runs;
   if (n_out) *n_out = out;
+  (void)p.n_desc_total;
   return MCZI_OK;
 }
 

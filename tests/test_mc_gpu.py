@@ -265,3 +265,25 @@ def test_minimizer_precount_is_conservative(gpu_ctx, oracle):
             assert on == oracle_dict(oracle, ds, 31, x, mode=1)
     finally:
         gpu_ctx.set_minimizer_precount(False)
+
+
+def test_key_range_passes_identical(gpu_ctx, oracle):
+    """Counting in passes over disjoint minimizer-key ranges gives the same
+    records (abundance and fof, filtered and single-pass rounds)."""
+    from mczi_gb300 import gen
+    data = gen.c1_reads(scale=0.003)
+    ds = gen.c3_datasets(n_datasets=4, genome_len=60_000, coverage=(2.0, 4.0))
+    ref31 = oracle_dict(oracle, [data], 31, 1)
+    ref63 = oracle_dict(oracle, [data], 63, 0)
+    reff = oracle_dict(oracle, ds, 31, 1, mode=1)
+    try:
+        for passes in (1, 2, 3, 7):
+            gpu_ctx.set_key_range_passes(passes)
+            for filt in (0, 1):
+                gpu_ctx.set_count_filter(filt)
+                assert gpu_dict(gpu_ctx, [data], 31, 21, 1) == ref31, (passes, filt)
+                assert gpu_dict(gpu_ctx, ds, 31, 21, 1, mode=1) == reff, (passes, filt)
+            assert gpu_dict(gpu_ctx, [data], 63, 21, 0) == ref63, passes
+    finally:
+        gpu_ctx.set_key_range_passes(0)
+        gpu_ctx.set_count_filter(-1)
