@@ -287,3 +287,19 @@ def test_key_range_passes_identical(gpu_ctx, oracle):
     finally:
         gpu_ctx.set_key_range_passes(0)
         gpu_ctx.set_count_filter(-1)
+
+
+def test_autotuner_keeps_results(gpu_ctx, oracle, tmp_path, monkeypatch):
+    from mczi_gb300 import autotune, gen
+    from mczi_gb300.mc import CounterConfig
+    monkeypatch.setenv("MCZI_TUNE_CACHE", str(tmp_path / "tune.json"))
+    data = gen.c2_reads(scale=0.001)
+    cfg = CounterConfig(63, 21, 3)
+    best, rep = autotune.tune(gpu_ctx, [data], cfg, 0, repeats=1)
+    assert rep["candidates"] > 5 and rep["best_ms"] <= rep["default_ms"]
+    try:
+        assert gpu_dict(gpu_ctx, [data], 63, 21, 3) == oracle_dict(oracle, [data], 63, 3)
+        best2, rep2 = autotune.tune(gpu_ctx, [data], cfg, 0)
+        assert rep2["cached"] and best2 == best
+    finally:
+        autotune.DEFAULT.apply(gpu_ctx)
