@@ -337,16 +337,28 @@ def run_zi(args):
     ctx.set_stream(stream.cuda_stream)
     zi.build_dictionary(index, k, m, ctx=ctx)
     info = zi.info(ctx)
-    # batched: all files in one set of launches, a result per file (input masks)
+    # batched: files in balanced groups of at most 64 (one mask word per
+    # record), each group one set of launches with a result per file
+    ngroups = -(-nfiles // 64)
+    groups = [files[i * nfiles // ngroups:(i + 1) * nfiles // ngroups] for i in range(ngroups)]
     for _ in range(args.warmup):
-        zi.query_per_input(ctx, files)
+        for g in groups:
+            zi.query_per_input(ctx, g)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    phases = [0.0] * 5
     for _ in range(args.steps):
-        n_rec = zi.query_per_input(ctx, files)
+        n_rec = 0
+        for g in groups:
+            n_rec += zi.query_per_input(ctx, g)
+            phases = [a + b for a, b in zip(phases, ctx.phase_times())]
     torch.cuda.synchronize()
     batched_s = (time.perf_counter() - t0) / args.steps
-    phases = ctx.phase_times()
+    phases = [x / args.steps for x in phases]
+    # per-file result lists of the last group, split on the device
+    t0 = time.perf_counter()
+    split = zi.batch_results(ctx, len(groups[-1]))
+    split_s = time.perf_counter() - t0
     # plain: one pipeline per file, a result per file
     lat = []
     sizes = []
@@ -373,6 +385,8 @@ def run_zi(args):
                        "mphf_levels": info["mphf_levels"], "minimizers": info["minimizers"],
                        "index_build_ms": info["build_us"] / 1000.0, "records_batched": n_rec},
             "batched": {"s": round(batched_s, 4), "lookups_per_s": round(windows / batched_s, 1),
+                        "groups": ngroups, "split_last_group_ms": round(split_s * 1e3, 3),
+                        "split_last_group_kmers": int(sum(len(x) for x in split)),
                         "phases_ms": dict(zip(["pack", "scan", "partition", "dedup_count", "probe"],
                                               [round(x, 3) for x in phases]))},
             "plain": {"s": round(plain_s, 4), "lookups_per_s": round(windows / plain_s, 1),

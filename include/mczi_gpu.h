@@ -138,6 +138,15 @@ int32_t mczi_set_count_options(mczi_ctx* ctx, int32_t chunk, float fill);
  * pass; -1 (default) picks two passes for k > 32.  Results are identical. */
 int32_t mczi_set_count_filter(mczi_ctx* ctx, int32_t mode);
 
+/* CUDA-graph replay of the counting pipeline.  When enabled, a count runs the
+ * plain path once and captures its launches; later counts of staged inputs
+ * with the same layout and configuration replay the graph (one launch, no
+ * host synchronisation between phases) and fall back to the plain path --
+ * and recapture -- if the inputs outgrow the captured buffer sizes.  With the
+ * graph, mczi_phase_times reports the whole device time as the counting
+ * phase.  Off by default; not used with the minimizer pre-count. */
+int32_t mczi_set_graph_replay(mczi_ctx* ctx, int32_t enable);
+
 /* Inputs with more superkmers than one pass holds are counted in passes over
  * disjoint ranges of the minimizer key (each pass rescans the packed stream).
  * 0 (default) picks the number from the input size and free HBM; 1..64 forces

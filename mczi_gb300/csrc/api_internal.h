@@ -59,7 +59,7 @@ struct DevBuf {
 
 // device scalars, in u64 slots
 enum { SC_NDESC = 0, SC_NOUT = 1, SC_STATS = 2, SC_STATUS = 10, SC_WORK = 11, SC_NKEPT = 12, SC_NRUNS = 13,
-       SC_COUNT = 16 };
+       SC_SCANST = 14, SC_COUNT = 16 };
 
 constexpr int N_PHASES = 5;
 constexpr int MPHF_MAX_LEVELS = 40;
@@ -79,6 +79,26 @@ struct ZiIndex {
   uint64_t lvl_off[MPHF_MAX_LEVELS + 1] = {};
   uint64_t lvl_size[MPHF_MAX_LEVELS] = {};
   float build_ms = 0.f;
+};
+
+// what a captured pipeline depends on; replay only when it matches
+struct GraphSig {
+  uint64_t text_len = 0, n_tiles = 0, x = 0, desc_cap = 0, out_cap = 0;
+  int n_inputs = 0, k = 0, m = 0, mode = 0;
+  uint32_t passes = 0, slots = 0, fwords = 0;
+  int threads = 0, cps = 0, chunk = 0, filter = 0;
+  float fill = 0.f;
+  const void* ptrs[12] = {};
+  bool operator==(const GraphSig& o) const {
+    if (text_len != o.text_len || n_tiles != o.n_tiles || x != o.x || desc_cap != o.desc_cap || out_cap != o.out_cap ||
+        n_inputs != o.n_inputs || k != o.k || m != o.m || mode != o.mode || passes != o.passes || slots != o.slots ||
+        fwords != o.fwords || threads != o.threads || cps != o.cps || chunk != o.chunk || filter != o.filter ||
+        fill != o.fill)
+      return false;
+    for (int i = 0; i < 12; i++)
+      if (ptrs[i] != o.ptrs[i]) return false;
+    return true;
+  }
 };
 
 }  // namespace mczi
@@ -128,6 +148,16 @@ struct mczi_ctx {
   int key_passes = 0;  // 0 = chosen from the input size and free HBM  // two-pass bitmap-filtered rounds: -1 auto (when x >= 1), 0 off, 1 on
 
   mczi::ZiIndex zi;
+
+  // CUDA-graph replay of the counting pipeline (mczi_set_graph_replay)
+  bool graph_mode = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  mczi::GraphSig graph_sig;
+  uint64_t cap_desc = 0, cap_out = 0;  // sizes of the last uncaptured run
+  uint32_t cap_slots = 0, cap_fwords = 0, cap_passes = 0;
+  uint64_t graph_replays = 0, graph_captures = 0, graph_launches_per_replay = 0;
+  cudaEvent_t ev_graph[2] = {};
 };
 
 namespace mczi {
@@ -162,7 +192,13 @@ struct Pipe {
   const uint64_t* d_nbases = nullptr;
   float pre_ms = 0.f;
   float ms[mczi::N_PHASES] = {0, 0, 0, 0, 0};  // accumulated over key-range passes
+  // graph capture: enqueue only (no host synchronisation, no event records),
+  // with the buffer sizes of the preceding uncaptured run
+  bool capture = false;
+  uint32_t pass = 0;
 };
+
+
 
 int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n);
 int32_t pipe_pack(mczi_ctx* ctx, Pipe& p);

@@ -59,6 +59,11 @@ __device__ __forceinline__ uint32_t mmer_hash_at(const uint32_t* spk, uint32_t r
   return mmer_hash64(clo ^ (chi * 0xD6E8FEB86659FD93ull + 0x2545F4914F6CDD1Dull));
 }
 
+__device__ __forceinline__ bool in_range(uint32_t mval, uint32_t lo, uint32_t hi) {
+  const uint32_t p1 = mix32(mval) >> (32 - P1_BITS);
+  return p1 >= lo && p1 < hi;
+}
+
 // 64 fragment-start bits beginning at relative bit q
 __device__ __forceinline__ uint64_t bits64(const uint32_t* sfb, uint32_t q) {
   const uint32_t i = q >> 5, o = q & 31;
@@ -148,15 +153,15 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   // key-range pass: only superkmers whose p1 digit is in [p1_lo, p1_hi) are
   // emitted; every start still ends the run before it
   const uint32_t p1_lo = a.p1_lo, p1_hi = a.p1_hi;
+  const bool ranged = p1_lo > 0 || p1_hi < (uint32_t)NP1;  // uniform: one pass needs no check
   Cnt2 c{0, 0};
 #pragma unroll
   for (int i = 1; i <= WPT; i++) {
     const int r = r0 + i - 1;
     const bool start = vd[i] && (r == 0 || !vd[i - 1] || mv[i] != mv[i - 1]);
     const bool term = !vd[i] && r > 0 && vd[i - 1];
-    const uint32_t p1 = mix32(mv[i]) >> (32 - P1_BITS);
     c.ev += (start || term);
-    c.st += start && p1 >= p1_lo && p1 < p1_hi;
+    if (start) c.st += !ranged || in_range(mv[i], p1_lo, p1_hi);
   }
   Cnt2 tot;
   const Cnt2 pre = block_exclusive_scan<Cnt2, Cnt2Op>(c, &tot, shc);
@@ -168,8 +173,7 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
       const int r = r0 + i - 1;
       const bool start = vd[i] && (r == 0 || !vd[i - 1] || mv[i] != mv[i - 1]);
       const bool term = !vd[i] && r > 0 && vd[i - 1];
-      const uint32_t p1 = mix32(mv[i]) >> (32 - P1_BITS);
-      const bool emit = start && p1 >= p1_lo && p1 < p1_hi;
+      const bool emit = start && (!ranged || in_range(mv[i], p1_lo, p1_hi));
       if (start || term) {
         ev[e] = (uint32_t)r | ((uint32_t)emit << 13) | (sr << 14);
         e++;

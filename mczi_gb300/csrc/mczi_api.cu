@@ -152,7 +152,7 @@ int32_t pipe_pack(mczi_ctx* ctx, Pipe& p) {
   CKA(ctx->input_base, ((size_t)n_in + 1) * sizeof(uint64_t));
   CK(cudaMemsetAsync(ctx->packed.p, 0, pwords * 4, s));
   CK(cudaMemsetAsync(ctx->fbits.p, 0, fwords * 4, s));
-  CK(cudaEventRecord(ctx->ev[0], s));
+  if (!p.capture) CK(cudaEventRecord(ctx->ev[0], s));
   PackArgs pa;
   pa.text = ctx->text.as<uint8_t>();
   pa.tile_info = ctx->tile_info.as<uint32_t>();
@@ -173,7 +173,7 @@ int32_t pipe_pack(mczi_ctx* ctx, Pipe& p) {
   p.d_nbases = reinterpret_cast<const uint64_t*>(ctx->base_pre.as<BaseSum>() + n_tiles);
   CK(cudaMemcpyAsync(ctx->input_base.as<uint64_t>() + n_in, p.d_nbases, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
   CK(cudaGetLastError());
-  CK(cudaEventRecord(ctx->ev[1], s));
+  if (!p.capture) CK(cudaEventRecord(ctx->ev[1], s));
   return MCZI_OK;
 }
 
@@ -196,12 +196,13 @@ int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m, uint32_t p1_lo, uint32_t
   const int w = k - m + 1;
   uint64_t desc_cap = text_len * 3 / (uint64_t)(w + 1) / passes + (1u << 20);
   if (desc_cap > text_len + 1024) desc_cap = text_len + 1024;
+  if (p.capture) desc_cap = ctx->cap_desc;
   for (int attempt = 0; attempt < 3; attempt++) {
     if (desc_cap >= 0xffffffffull) return fail(ctx, MCZI_ERR_OOM, "input batch too large: more than 2^32 superkmers");
     CKA(ctx->desc, desc_cap * 8);
     CKA(ctx->key, desc_cap * 4);
     CK(cudaMemsetAsync(sc + SC_NDESC, 0, 8, s));
-    CK(cudaMemsetAsync(sc + SC_STATUS, 0, 8, s));
+    if (!p.capture) CK(cudaMemsetAsync(sc + SC_STATUS, 0, 8, s));
     ScanArgs sa;
     sa.packed = ctx->packed.as<uint32_t>();
     sa.fbits = ctx->fbits.as<uint32_t>();
@@ -214,12 +215,17 @@ int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m, uint32_t p1_lo, uint32_t
     sa.key = ctx->key.as<uint32_t>();
     sa.n_desc = reinterpret_cast<unsigned long long*>(sc + SC_NDESC);
     sa.desc_cap = desc_cap;
-    sa.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
+    sa.status = reinterpret_cast<uint32_t*>(sc + (p.capture ? SC_SCANST : SC_STATUS));
     sa.p1_lo = p1_lo;
     sa.p1_hi = p1_hi;
     launch_scan(sa, s);
     p.launches += 1;
     CK(cudaGetLastError());
+    if (p.capture) {  // sizes come from the uncaptured run; overflow is checked after replay
+      p.n_desc = desc_cap;
+      p.desc_cap = desc_cap;
+      return MCZI_OK;
+    }
     uint64_t h[2];
     CK(cudaMemcpyAsync(h, sc + SC_NDESC, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(h + 1, sc + SC_STATUS, 8, cudaMemcpyDeviceToHost, s));
@@ -227,6 +233,7 @@ int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m, uint32_t p1_lo, uint32_t
     if (!(h[1] & ST_DESC_OVERFLOW)) {
       p.n_desc = h[0];
       p.desc_cap = desc_cap;
+      ctx->cap_desc = std::max(ctx->cap_desc, desc_cap);
       return MCZI_OK;
     }
     desc_cap = h[0] + 1024;
@@ -287,7 +294,7 @@ int32_t pipe_precount(mczi_ctx* ctx, Pipe& p, int mode, uint64_t x) {
 int32_t pipe_partition(mczi_ctx* ctx, Pipe& p) {
   cudaStream_t s = ctx->stream;
   uint64_t* sc = ctx->scalars.as<uint64_t>();
-  CK(cudaEventRecord(ctx->ev[2], s));
+  if (!p.capture) CK(cudaEventRecord(ctx->ev[2], s));
   CKA(ctx->desc2, p.desc_cap * 8);
   CKA(ctx->key2, p.desc_cap * 4);
   const uint64_t nh = (uint64_t)NP1 * PART_CTAS;
@@ -310,7 +317,7 @@ int32_t pipe_partition(mczi_ctx* ctx, Pipe& p) {
     p.launches += 7;
   }
   CK(cudaGetLastError());
-  CK(cudaEventRecord(ctx->ev[3], s));
+  if (!p.capture) CK(cudaEventRecord(ctx->ev[3], s));
   return MCZI_OK;
 }
 
@@ -325,6 +332,7 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
   const uint64_t prior = append ? *n_out_ret : 0;  // records of earlier key-range passes
   uint64_t out_cap = std::max<uint64_t>(std::min<uint64_t>(est_out, 1ull << 25), prior + (1u << 20));
   if (append && ctx->out_lo.cap / 8 > out_cap) out_cap = ctx->out_lo.cap / 8;
+  if (p.capture) out_cap = ctx->cap_out;
   uint64_t n_out = prior;
 #define CKG(buf, bytes, keep)                                                            \
   do {                                                                                   \
@@ -370,9 +378,14 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       if (wide) CKG(ctx->out_hi, out_cap * 8, prior * 8);
       CKG(ctx->out_cnt, out_cap * 4, prior * 4);
       if (emit_masks) CKG(ctx->out_mask, out_cap * 8 * (uint64_t)W, prior * 8 * (uint64_t)W);
-      CK(cudaMemcpyAsync(sc + SC_NOUT, &prior, 8, cudaMemcpyHostToDevice, s));
+      if (p.capture) {
+        // the record counter runs on across passes; statuses accumulate
+        if (p.pass == 0) CK(cudaMemsetAsync(sc + SC_NOUT, 0, 8, s));
+      } else {
+        CK(cudaMemcpyAsync(sc + SC_NOUT, &prior, 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(sc + SC_STATUS, 0, 8, s));
+      }
       CK(cudaMemsetAsync(sc + SC_STATS, 0, 8 * 8, s));
-      CK(cudaMemsetAsync(sc + SC_STATUS, 0, 8, s));
       CK(cudaMemsetAsync(sc + SC_WORK, 0, 8, s));
       CountArgs ca;
       ca.packed = ctx->packed.as<uint32_t>();
@@ -402,6 +415,9 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       launch_count(ca, s);
       p.launches += 1;
       CK(cudaGetLastError());
+      if (p.capture) break;
+      ctx->cap_slots = slots;
+      ctx->cap_fwords = fwords;
       uint64_t h[SC_COUNT];
       CK(cudaMemcpyAsync(h, sc, sizeof h, cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
@@ -412,6 +428,7 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
         continue;
       }
       n_out = h[SC_NOUT];
+      ctx->cap_out = std::max(ctx->cap_out, out_cap);
       ctx->stats[2] += h[SC_STATS + 2];
       ctx->stats[3] += h[SC_STATS + 3];
       ctx->stats[4] += h[SC_STATS + 1];
@@ -419,7 +436,7 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       break;
     }
   }
-  CK(cudaEventRecord(ctx->ev[4], s));
+  if (!p.capture) CK(cudaEventRecord(ctx->ev[4], s));
   ctx->mask_words = emit_masks ? W : 0;
   *n_out_ret = n_out;
   return MCZI_OK;
@@ -510,6 +527,137 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
   return MCZI_OK;
 }
 
+
+GraphSig make_sig(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint32_t passes) {
+  GraphSig g;
+  g.text_len = ctx->text_len;
+  g.n_tiles = ctx->n_tiles;
+  g.x = cfg->threshold;
+  g.desc_cap = ctx->cap_desc;
+  g.out_cap = ctx->cap_out;
+  g.n_inputs = ctx->n_inputs;
+  g.k = (int)cfg->k;
+  g.m = (int)cfg->minimizer;
+  g.mode = mode;
+  g.passes = passes;
+  g.slots = ctx->cap_slots;
+  g.fwords = ctx->cap_fwords;
+  g.threads = ctx->count_threads;
+  g.cps = ctx->count_ctas_per_sm;
+  g.chunk = ctx->count_chunk;
+  g.filter = ctx->count_filter;
+  g.fill = ctx->count_fill;
+  const void* ptrs[12] = {ctx->text.p, ctx->packed.p, ctx->fbits.p, ctx->desc.p, ctx->key.p, ctx->desc2.p,
+                          ctx->key2.p, ctx->out_lo.p, ctx->out_hi.p, ctx->out_cnt.p, ctx->scalars.p,
+                          ctx->part_hist.p};
+  for (int i = 0; i < 12; i++) g.ptrs[i] = ptrs[i];
+  return g;
+}
+
+void drop_graph(mczi_ctx* ctx) {
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  ctx->graph_exec = nullptr;
+  ctx->graph = nullptr;
+}
+
+// Enqueues the whole counting pipeline on the capturing stream: no host
+// synchronisation, the buffer sizes of the uncaptured run just before.
+int32_t capture_pipeline(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint32_t passes) {
+  cudaStream_t s = ctx->stream;
+  drop_graph(ctx);
+  if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return MCZI_OK;  // no graph: the plain path keeps working
+  }
+  const int k = (int)cfg->k, m = (int)cfg->minimizer;
+  Pipe p;
+  p.capture = true;
+  int32_t rc = MCZI_OK;
+  uint64_t n_out = 0;
+  uint64_t* sc = ctx->scalars.as<uint64_t>();
+  cudaMemsetAsync(sc + SC_STATUS, 0, 8, s);
+  cudaMemsetAsync(sc + SC_SCANST, 0, 8, s);
+  rc = pipe_pack(ctx, p);
+  for (uint32_t r = 0; r < passes && rc == MCZI_OK; r++) {
+    p.pass = r;
+    const uint32_t lo = (uint32_t)((uint64_t)NP1 * r / passes), hi = (uint32_t)((uint64_t)NP1 * (r + 1) / passes);
+    if ((rc = pipe_scan(ctx, p, k, m, lo, hi, passes))) break;
+    if ((rc = pipe_partition(ctx, p))) break;
+    rc = pipe_count(ctx, p, k, cfg->threshold, mode, false, &n_out, r > 0);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (rc != MCZI_OK || e != cudaSuccess || !g) {
+    cudaGetLastError();
+    if (g) cudaGraphDestroy(g);
+    return MCZI_OK;
+  }
+  cudaGraphExec_t ex = nullptr;
+  if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) {
+    cudaGetLastError();
+    cudaGraphDestroy(g);
+    return MCZI_OK;
+  }
+  ctx->graph = g;
+  ctx->graph_exec = ex;
+  ctx->graph_sig = make_sig(ctx, cfg, mode, passes);
+  ctx->graph_captures++;
+  ctx->graph_launches_per_replay = p.launches;
+  return MCZI_OK;
+}
+
+// Replays the captured pipeline when it matches the staged inputs and the
+// configuration; otherwise runs the plain path and captures it for next time.
+int32_t run_count_graph(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint64_t* n_records) {
+  int32_t rc = validate(ctx, cfg, mode);
+  if (rc) return rc;
+  if (!ctx->staged) return fail(ctx, MCZI_ERR_STATE, "no staged inputs");
+  if (ctx->precount || (mode == MCZI_MODE_PRESENCE && cfg->threshold >= (uint64_t)ctx->n_inputs))
+    return run_count(ctx, cfg, mode, n_records);
+  const uint32_t passes = key_range_passes(ctx, (int)cfg->k, (int)cfg->minimizer);
+  if (ctx->graph_exec && make_sig(ctx, cfg, mode, passes) == ctx->graph_sig) {
+    cudaStream_t s = ctx->stream;
+    CK(cudaEventRecord(ctx->ev_graph[0], s));
+    CK(cudaGraphLaunch(ctx->graph_exec, s));
+    CK(cudaEventRecord(ctx->ev_graph[1], s));
+    uint64_t h[SC_COUNT];
+    CK(cudaMemcpyAsync(h, ctx->scalars.p, sizeof h, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const uint32_t st = (uint32_t)(h[SC_STATUS] | h[SC_SCANST]);
+    if (st & (ST_DESC_OVERFLOW | ST_OUT_OVERFLOW | ST_TABLE_STUCK)) {
+      drop_graph(ctx);  // these inputs outgrew the captured sizes
+      rc = run_count(ctx, cfg, mode, n_records);
+      if (rc == MCZI_OK) capture_pipeline(ctx, cfg, mode, passes);
+      return rc;
+    }
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev_graph[0], ctx->ev_graph[1]));
+    for (int i = 0; i < N_PHASES; i++) ctx->phase_ms[i] = 0.f;
+    ctx->phase_ms[3] = ms;  // one graph: the whole pipeline's device time
+    std::memset(ctx->stats, 0, sizeof ctx->stats);
+    const uint64_t* nb = reinterpret_cast<const uint64_t*>(ctx->base_pre.as<BaseSum>() + ctx->n_tiles);
+    CK(cudaMemcpy(&ctx->stats[0], nb, 8, cudaMemcpyDeviceToHost));
+    ctx->stats[5] = h[SC_NOUT];
+    ctx->stats[7] = ctx->skipped;
+    ctx->stats[8] = ctx->graph_launches_per_replay;
+    ctx->stats[9] = ctx->h2d_bytes;
+    ctx->mode = mode;
+    ctx->k = (int)cfg->k;
+    ctx->m = (int)cfg->minimizer;
+    ctx->x = cfg->threshold;
+    ctx->n_out = h[SC_NOUT];
+    ctx->mask_words = 0;
+    ctx->have_result = true;
+    ctx->graph_replays++;
+    if (n_records) *n_records = h[SC_NOUT];
+    return MCZI_OK;
+  }
+  rc = run_count(ctx, cfg, mode, n_records);
+  if (rc == MCZI_OK) capture_pipeline(ctx, cfg, mode, passes);
+  return rc;
+}
+
 int32_t fetch_records(mczi_ctx* ctx, HostRecords* r) {
   const uint64_t n = ctx->n_out;
   r->lo.resize(n);
@@ -579,6 +727,7 @@ int32_t mczi_open(int32_t device, mczi_ctx** out) {
   ctx->stream = ctx->own_stream;
   for (auto& ev : ctx->ev) cudaEventCreate(&ev);
   for (auto& ev : ctx->ev_pre) cudaEventCreate(&ev);
+  for (auto& ev : ctx->ev_graph) cudaEventCreate(&ev);
   *out = ctx;
   return MCZI_OK;
 }
@@ -597,6 +746,8 @@ int32_t mczi_close(mczi_ctx* ctx) {
   for (DevBuf* b : bufs) b->release();
   for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
   for (auto& ev : ctx->ev_pre) if (ev) cudaEventDestroy(ev);
+  for (auto& ev : ctx->ev_graph) if (ev) cudaEventDestroy(ev);
+  drop_graph(ctx);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return MCZI_OK;
@@ -623,7 +774,7 @@ int32_t mczi_stage(mczi_ctx* ctx, const mczi_input* inputs, size_t n_inputs) {
 int32_t mczi_count_staged(mczi_ctx* ctx, const mczi_counter_config* cfg, int32_t mode, uint64_t* n_records) {
   if (!ctx) return MCZI_ERR_STATE;
   cudaSetDevice(ctx->device);
-  return run_count(ctx, cfg, mode, n_records);
+  return ctx->graph_mode ? run_count_graph(ctx, cfg, mode, n_records) : run_count(ctx, cfg, mode, n_records);
 }
 
 int32_t mczi_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int32_t mode, const mczi_input* inputs,
@@ -634,7 +785,7 @@ int32_t mczi_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int32_t mode, 
   if (rc) return rc;
   rc = stage_inputs(ctx, inputs, n_inputs);
   if (rc) return rc;
-  return run_count(ctx, cfg, mode, n_records);
+  return ctx->graph_mode ? run_count_graph(ctx, cfg, mode, n_records) : run_count(ctx, cfg, mode, n_records);
 }
 
 int32_t mczi_result_copy(mczi_ctx* ctx, uint64_t* key_lo, uint64_t* key_hi, uint64_t* counts, uint64_t cap,
@@ -738,6 +889,13 @@ int32_t mczi_set_count_options(mczi_ctx* ctx, int32_t chunk, float fill) {
   if (fill < 0.f || fill > 0.85f) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "fill must be in (0, 0.85]");
   ctx->count_chunk = chunk;
   ctx->count_fill = fill;
+  return MCZI_OK;
+}
+
+int32_t mczi_set_graph_replay(mczi_ctx* ctx, int32_t enable) {
+  if (!ctx) return MCZI_ERR_STATE;
+  ctx->graph_mode = enable != 0;
+  if (!ctx->graph_mode) drop_graph(ctx);
   return MCZI_OK;
 }
 

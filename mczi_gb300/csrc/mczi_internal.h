@@ -41,6 +41,8 @@ void launch_pack(const PackArgs& a, cudaStream_t s);
 // partition digits of the superkmer key (mix32 of the minimizer value)
 constexpr int P1_BITS = 12;
 constexpr int P2_BITS = 11;
+constexpr int NP1 = 1 << P1_BITS;
+constexpr int NP2 = 1 << P2_BITS;
 
 // ---------------------------------------------------------------- K2 scan
 constexpr int SCAN_TILE = 4096;     // windows per CTA
@@ -63,8 +65,6 @@ struct ScanArgs {
 void launch_scan(const ScanArgs& a, cudaStream_t s);
 
 // ---------------------------------------------------------------- K3 partition
-constexpr int NP1 = 1 << P1_BITS;
-constexpr int NP2 = 1 << P2_BITS;
 constexpr int PART_CTAS = 304;   // 2 per SM on a 152-SM GB300
 constexpr int PART_THREADS = 512;
 

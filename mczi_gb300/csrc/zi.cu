@@ -247,6 +247,58 @@ __global__ void __launch_bounds__(ZI_THREADS) k_zi_probe(ProbeArgs a) {
   }
 }
 
+
+// ---- per-input split of a batch result (records x masks -> per-input lists)
+constexpr int SPLIT_CHUNK = 4096;
+constexpr int SPLIT_MAX_INPUTS = 4096;
+
+__global__ void __launch_bounds__(ZI_THREADS) k_zi_split_count(const unsigned long long* __restrict__ masks,
+                                                               uint64_t n, int W, int n_inputs,
+                                                               unsigned long long* __restrict__ cnt) {
+  __shared__ uint32_t c[SPLIT_MAX_INPUTS];
+  for (int i = threadIdx.x; i < n_inputs; i += blockDim.x) c[i] = 0;
+  __syncthreads();
+  const uint64_t c0 = (uint64_t)blockIdx.x * SPLIT_CHUNK;
+  const uint64_t c1 = c0 + SPLIT_CHUNK < n ? c0 + SPLIT_CHUNK : n;
+  for (uint64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x)
+    for (int q = 0; q < W; q++)
+      for (unsigned long long m = masks[i * W + q]; m; m &= m - 1) atomicAdd(&c[q * 64 + __ffsll((long long)m) - 1], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < n_inputs; i += blockDim.x)
+    if (c[i]) atomicAdd(&cnt[i], (unsigned long long)c[i]);
+}
+
+__global__ void __launch_bounds__(ZI_THREADS) k_zi_split_fill(const unsigned long long* __restrict__ masks,
+                                                              const uint64_t* __restrict__ lo,
+                                                              const uint64_t* __restrict__ hi, uint64_t n, int W,
+                                                              int n_inputs, unsigned long long* __restrict__ cursor,
+                                                              uint64_t* __restrict__ out_lo,
+                                                              uint64_t* __restrict__ out_hi) {
+  __shared__ uint32_t c[SPLIT_MAX_INPUTS];
+  __shared__ unsigned long long base[SPLIT_MAX_INPUTS];
+  for (int i = threadIdx.x; i < n_inputs; i += blockDim.x) c[i] = 0;
+  __syncthreads();
+  const uint64_t c0 = (uint64_t)blockIdx.x * SPLIT_CHUNK;
+  const uint64_t c1 = c0 + SPLIT_CHUNK < n ? c0 + SPLIT_CHUNK : n;
+  for (uint64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x)
+    for (int q = 0; q < W; q++)
+      for (unsigned long long m = masks[i * W + q]; m; m &= m - 1) atomicAdd(&c[q * 64 + __ffsll((long long)m) - 1], 1u);
+  __syncthreads();
+  for (int i = threadIdx.x; i < n_inputs; i += blockDim.x) {
+    base[i] = c[i] ? atomicAdd(&cursor[i], (unsigned long long)c[i]) : 0ull;
+    c[i] = 0;
+  }
+  __syncthreads();
+  for (uint64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x)
+    for (int q = 0; q < W; q++)
+      for (unsigned long long m = masks[i * W + q]; m; m &= m - 1) {
+        const int r = q * 64 + __ffsll((long long)m) - 1;
+        const uint64_t o = base[r] + atomicAdd(&c[r], 1u);
+        out_lo[o] = lo[i];
+        if (out_hi) out_hi[o] = hi ? hi[i] : 0ull;
+      }
+}
+
 int grid_for(mczi_ctx* ctx, uint64_t n) {
   const uint64_t g = (n + ZI_THREADS - 1) / ZI_THREADS;
   const uint64_t cap = (uint64_t)ctx->sm_count * 16;
@@ -564,35 +616,44 @@ int32_t mczi_zi_batch_split(mczi_ctx* ctx, uint64_t* key_lo, uint64_t* key_hi, u
                             uint64_t* total) {
   if (!ctx) return MCZI_ERR_STATE;
   if (!ctx->have_result || ctx->mask_words == 0) return fail(ctx, MCZI_ERR_STATE, "no per-input ZI result");
+  const int ni = ctx->n_inputs;
+  if (ni > SPLIT_MAX_INPUTS) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "more than 4096 inputs in one batch");
   cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
   const uint64_t nr = ctx->n_out;
   const int W = ctx->mask_words;
-  const int ni = ctx->n_inputs;
-  std::vector<uint64_t> lo(nr), hi(ctx->k > 32 ? nr : 0), msk(nr * (uint64_t)W);
-  if (nr) {
-    CK(cudaMemcpyAsync(lo.data(), ctx->out_lo.p, nr * 8, cudaMemcpyDeviceToHost, ctx->stream));
-    if (ctx->k > 32) CK(cudaMemcpyAsync(hi.data(), ctx->out_hi.p, nr * 8, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaMemcpyAsync(msk.data(), ctx->out_mask.p, nr * 8 * W, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
-  }
-  // counting pass: per-input sizes and offsets
+  const bool wide = ctx->k > 32;
+  // per-input sizes on the device (block-aggregated), offsets on the host
+  CKA(ctx->zi_tmp0, ((size_t)ni + 1) * 8 * 2);
+  unsigned long long* cnt = ctx->zi_tmp0.as<unsigned long long>();
+  unsigned long long* cursor = cnt + ni + 1;
+  CK(cudaMemsetAsync(cnt, 0, ((size_t)ni + 1) * 8, s));
+  const unsigned blocks = (unsigned)((nr + SPLIT_CHUNK - 1) / SPLIT_CHUNK);
+  if (nr) k_zi_split_count<<<blocks, ZI_THREADS, 0, s>>>(ctx->out_mask.as<unsigned long long>(), nr, W, ni, cnt);
+  CK(cudaGetLastError());
   std::vector<uint64_t> off((size_t)ni + 1, 0);
-  for (uint64_t i = 0; i < nr; i++)
-    for (int q = 0; q < W; q++)
-      for (uint64_t m = msk[i * W + q]; m; m &= m - 1) off[(size_t)q * 64 + __builtin_ctzll(m) + 1]++;
+  CK(cudaMemcpyAsync(off.data() + 1, cnt, (size_t)ni * 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
   for (int i = 0; i < ni; i++) off[i + 1] += off[i];
   if (total) *total = off[ni];
   if (offsets) std::copy(off.begin(), off.end(), offsets);
   if (!key_lo) return MCZI_OK;
   if (cap < off[ni]) return fail(ctx, MCZI_ERR_STATE, "result buffer too small");
-  std::vector<uint64_t> cur(off.begin(), off.end() - 1);
-  for (uint64_t i = 0; i < nr; i++)
-    for (int q = 0; q < W; q++)
-      for (uint64_t m = msk[i * W + q]; m; m &= m - 1) {
-        const uint64_t o = cur[(size_t)q * 64 + __builtin_ctzll(m)]++;
-        key_lo[o] = lo[i];
-        if (key_hi) key_hi[o] = ctx->k > 32 ? hi[i] : 0;
-      }
+  if (off[ni] == 0) return MCZI_OK;
+  CKA(ctx->zi_tmp1, off[ni] * 8 * (wide ? 2 : 1));
+  uint64_t* dlo = ctx->zi_tmp1.as<uint64_t>();
+  uint64_t* dhi = wide ? dlo + off[ni] : nullptr;
+  CK(cudaMemcpyAsync(cursor, off.data(), (size_t)ni * 8, cudaMemcpyHostToDevice, s));
+  k_zi_split_fill<<<blocks, ZI_THREADS, 0, s>>>(ctx->out_mask.as<unsigned long long>(), ctx->out_lo.as<uint64_t>(),
+                                                wide ? ctx->out_hi.as<uint64_t>() : nullptr, nr, W, ni, cursor, dlo,
+                                                dhi);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(key_lo, dlo, off[ni] * 8, cudaMemcpyDeviceToHost, s));
+  if (key_hi) {
+    if (wide) CK(cudaMemcpyAsync(key_hi, dhi, off[ni] * 8, cudaMemcpyDeviceToHost, s));
+    else std::fill(key_hi, key_hi + off[ni], 0ull);
+  }
+  CK(cudaStreamSynchronize(s));
   return MCZI_OK;
 }
 

@@ -204,6 +204,10 @@ class Context:
         """-1 auto (two-pass rounds when threshold >= 1), 0 single pass, 1 two-pass."""
         self._ck(self._lib.mczi_set_count_filter(self._h, mode))
 
+    def set_graph_replay(self, enable: bool) -> None:
+        """Replay the counting pipeline from a captured CUDA graph."""
+        self._ck(self._lib.mczi_set_graph_replay(self._h, 1 if enable else 0))
+
     def set_key_range_passes(self, passes: int) -> None:
         """0 = automatic; n forces n passes over disjoint minimizer-key ranges."""
         self._ck(self._lib.mczi_set_key_range_passes(self._h, passes))

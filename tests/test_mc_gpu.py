@@ -303,3 +303,24 @@ def test_autotuner_keeps_results(gpu_ctx, oracle, tmp_path, monkeypatch):
         assert rep2["cached"] and best2 == best
     finally:
         autotune.DEFAULT.apply(gpu_ctx)
+
+
+def test_graph_replay_identical(gpu_ctx, oracle):
+    """Counts replayed from a captured CUDA graph equal the plain path, also
+    for new inputs of the same layout and across key-range passes."""
+    from mczi_gb300 import gen
+    a = gen.c1_reads(scale=0.002, seed=11)
+    b = gen.c1_reads(scale=0.002, seed=12)  # same size and layout, other reads
+    try:
+        gpu_ctx.set_graph_replay(True)
+        for passes in (1, 2):
+            gpu_ctx.set_key_range_passes(passes)
+            for data in (a, b, a):
+                for _ in range(2):
+                    assert gpu_dict(gpu_ctx, [data], 31, 21, 1) == oracle_dict(oracle, [data], 31, 1), passes
+        big = gen.c1_reads(scale=0.004, seed=13)  # other layout: plain path, then a new capture
+        assert gpu_dict(gpu_ctx, [big], 31, 21, 1) == oracle_dict(oracle, [big], 31, 1)
+        assert gpu_dict(gpu_ctx, [big], 31, 21, 1) == oracle_dict(oracle, [big], 31, 1)
+    finally:
+        gpu_ctx.set_graph_replay(False)
+        gpu_ctx.set_key_range_passes(0)
