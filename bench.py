@@ -327,6 +327,10 @@ def run_zi(args):
     glen = int(60_000_000 * args.scale)
     qbases = int(2_000_000_000 * args.scale)
     index, query = gen.c4_index_and_query(genome_len=glen, query_bases=qbases, k=k)
+    # the query sits in pinned host memory, as a server's receive buffers would
+    pinned = torch.empty(query.size, dtype=torch.uint8, pin_memory=True)
+    pinned.numpy()[:] = query
+    query = pinned.numpy()
     starts = _record_starts(query)
     nfiles = args.zi_files
     cuts = [int(starts[int(i * len(starts) / nfiles)]) for i in range(nfiles)] + [query.size]

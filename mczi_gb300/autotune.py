@@ -64,7 +64,7 @@ def candidates(k: int, threshold: int) -> list[Tuning]:
     wide = k > 32
     shapes = [(1024, 1), (512, 2), (768, 1)] if wide else [(512, 2), (1024, 1), (256, 4)]
     fills = [0.4, 0.6]
-    chunks = [2, 1]
+    chunks = [4, 2] if wide else [2, 4]
     filters = [1, 0] if threshold >= 1 else [0]
     out = [DEFAULT]
     for (t, c), f, ch, fl in itertools.product(shapes, fills, chunks, filters):

@@ -150,6 +150,8 @@ __global__ void k_count(CountArgs a) {
   __shared__ uint32_t warp_tmp[32];
   __shared__ float s_rho;
   __shared__ uint32_t sh_cpre[MAX_THREADS + 1];
+  __shared__ uint32_t sh_cpre32[MAX_THREADS / 32];
+  __shared__ uint32_t s_step;
   __shared__ uint64_t sh_desc[MAX_THREADS];
   __shared__ uint16_t sh_dset[MODE == 1 ? MAX_THREADS : 1];
   const uint32_t chunk = a.chunk;
@@ -322,15 +324,39 @@ __global__ void k_count(CountArgs a) {
               }
             }
             sh_desc[tid] = dsc;
+            if (tid == 0) s_step = 0;  // the previous batch's steps all ended before its closing barrier
             uint32_t total;
-            sh_cpre[tid] = block_excl_scan_u32(nch, &total, warp_tmp);
+            const uint32_t cp = block_excl_scan_u32(nch, &total, warp_tmp);
+            sh_cpre[tid] = cp;
+            if (lane == 0) sh_cpre32[tid >> 5] = cp;
             if (tid == 0) sh_cpre[nth] = total;
             __syncthreads();
             const int nd = (int)min((uint64_t)nth, dhi - bb);
-            for (uint32_t c = tid; c < total; c += nth) {
-              if (*(volatile uint32_t*)&s_over) break;
-              int lo2 = 0, hi2 = nd;  // descriptor j: sh_cpre[j] <= c < sh_cpre[j + 1]
-              while (hi2 - lo2 > 1) { const int mid = (lo2 + hi2) >> 1; if (sh_cpre[mid] <= c) lo2 = mid; else hi2 = mid; }
+            // Warps take steps of 32 chunks (one per lane) from a shared
+            // counter, so a batch ends with at most one step of imbalance.  The
+            // descriptor of the step's first chunk comes from a two-level
+            // 32-ary search (every 32nd prefix is kept apart, conflict-free);
+            // every descriptor holds >= 1 chunk, so at most 32 descriptor
+            // starts fall inside a step and a lane's descriptor is jw + (starts
+            // at or before its chunk).
+            for (;;) {
+              uint32_t c0 = 0;
+              if (lane == 0) c0 = atomicAdd(&s_step, 32u);
+              c0 = __shfl_sync(0xffffffffu, c0, 0);
+              if (c0 >= total || __any_sync(0xffffffffu, *(volatile uint32_t*)&s_over)) break;
+              const int i1 = lane << 5;
+              const unsigned b1 = __ballot_sync(0xffffffffu, i1 < nd && sh_cpre32[lane] <= c0);
+              const int seg = (31 - __clz(b1)) << 5;
+              const int i2 = seg + lane;
+              const unsigned b2 = __ballot_sync(0xffffffffu, i2 < nd && sh_cpre[i2] <= c0);
+              const int jw = seg + 31 - __clz(b2);
+              const int bi = jw + 1 + lane;
+              const uint32_t rel = bi < nd ? sh_cpre[bi] - c0 : 0xffffffffu;  // >= 1
+              const uint32_t starts = __reduce_or_sync(0xffffffffu, rel < 32u ? (1u << rel) : 0u);
+              const int lo2 = jw + __popc(starts & (0xffffffffu >> (31 - lane)));
+              const uint32_t cend = total;
+              const uint32_t c = c0 + (uint32_t)lane;
+              if (c >= cend) continue;
               const uint64_t d2 = sh_desc[lo2];
               const uint32_t len = bd_windows(d2);
               const uint32_t w0 = (c - sh_cpre[lo2]) * chunk;
@@ -345,16 +371,27 @@ __global__ void k_count(CountArgs a) {
                 if (k > 32) roll.set(field64(a.packed, s0, k - 32), field64(a.packed, s0 + (uint64_t)(k - 32), 32), k);
                 else roll.set(0ull, field64(a.packed, s0, k), k);
               }
-              uint64_t p = s0 + (uint64_t)k;
-              uint32_t word = a.packed[p >> 4];
+              // next base: the top two bits of `word` (pre-shifted), q = its
+              // index inside the packed word at wp
+              const uint64_t p = s0 + (uint64_t)k;
+              const uint32_t* wp = a.packed + (p >> 4);
+              uint32_t q = (uint32_t)(p & 15);
+              uint32_t word = *wp << (2 * q);
+              // software pipeline: the key and hash of window j + 1 are made
+              // before window j probes the table (independent work for the
+              // scheduler while the probe's shared-memory loads are in flight)
+              K key_n = roll.canon();
+              uint64_t hv_n = key_hash(key_n);
               for (uint32_t j = w0; j < w1; j++) {
-                if (j > w0) {
-                  if ((p & 15) == 0) word = a.packed[p >> 4];
-                  roll.push((word >> (30 - 2 * (uint32_t)(p & 15))) & 3u);
-                  p++;
+                const K key = key_n;
+                const uint64_t hv = hv_n;
+                if (j + 1 < w1) {
+                  roll.push(word >> 30);
+                  word <<= 2;
+                  if (++q == 16) { q = 0; word = *++wp; }
+                  key_n = roll.canon();
+                  hv_n = key_hash(key_n);
                 }
-                const K key = roll.canon();
-                const uint64_t hv = key_hash(key);
                 if (!full_range) {
                   const uint32_t hk = (uint32_t)(hv >> 32);
                   if (hk < rr.hlo || hk > rr.hhi) continue;

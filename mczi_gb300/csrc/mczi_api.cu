@@ -410,7 +410,7 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       ca.ctas = ctx->sm_count * cps;
       ca.work_counter = reinterpret_cast<unsigned int*>(sc + SC_WORK);
       ca.fill = ctx->count_fill > 0.f ? ctx->count_fill : (wide ? 0.4f : 0.6f);
-      ca.chunk = ctx->count_chunk > 0 ? (uint32_t)ctx->count_chunk : 2u;
+      ca.chunk = ctx->count_chunk > 0 ? (uint32_t)ctx->count_chunk : (wide ? 4u : 2u);
       ca.filter_words = fwords;
       launch_count(ca, s);
       p.launches += 1;

@@ -63,8 +63,12 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
 }
 
 __device__ __forceinline__ uint64_t key_hash(K64 k) { return mix64(k.v); }
+// 128-bit keys: fold of the 128-bit product of the two (offset) halves --
+// one wide multiply on the FMA pipe instead of two rounds of shifts and xors
+// on the integer ALU, which bounds the counting kernel
 __device__ __forceinline__ uint64_t key_hash(K128 k) {
-  return mix64(k.lo ^ (k.hi * 0x9e3779b97f4a7c15ull));
+  const uint64_t a = k.lo ^ 0x2d358dccaa6c78a5ull, b = k.hi ^ 0x8bb84b93962eacc9ull;
+  return (a * b) ^ __umul64hi(a, b);
 }
 
 // reverse the order of 2-bit groups and complement (x ^ 3 per base)
