@@ -13,9 +13,13 @@
 // consecutive valid windows with the same minimizer value, cut at tile edges.
 //
 // One CTA scans SCAN_TILE windows of the concatenated base stream, so reads of
-// any length (150 bp .. 100 kbp) are load-balanced by construction.  The
-// sliding minimum uses van Herk / Gil-Werman blocks of w in shared memory
-// (a constant number of shared-memory accesses per position, whatever w is).
+// any length (150 bp .. 100 kbp) are load-balanced by construction.  Each
+// thread owns 16 consecutive positions: it rolls their m-mers (forward and
+// reverse complement, one base per step) into a shared hash array, then takes
+// the minima of its 16 windows in registers -- for w >= 16 all 16 windows
+// contain the thread's last position, so each minimum is min(suffix minimum
+// up to that position, prefix minimum after it) (van Herk / Gil-Werman with
+// one split per thread); for w < 16 directly.
 #include "mczi_internal.h"
 #include "mczi_common.cuh"
 #include "scan.cuh"
@@ -26,6 +30,7 @@ namespace {
 
 constexpr int MAXW = 64;
 constexpr int HL = SCAN_TILE + MAXW;                 // hashes per tile
+constexpr int HLP = HL + HL / 16 + 1;                // padded: position j at j + j / 16
 constexpr int PKW = (SCAN_TILE + 128) / 16 + 4;      // packed words staged
 constexpr int FBW = (SCAN_TILE + 128) / 32 + 4;      // fragment-bit words staged
 constexpr int WPT = SCAN_TILE / SCANK_THREADS;       // windows per thread
@@ -59,6 +64,32 @@ __device__ __forceinline__ uint32_t mmer_hash_at(const uint32_t* spk, uint32_t r
   return mmer_hash64(clo ^ (chi * 0xD6E8FEB86659FD93ull + 0x2545F4914F6CDD1Dull));
 }
 
+// (lo, hi) |= (lo, hi) >> s as one 128-bit value, 1 <= s < 64
+__device__ __forceinline__ void smear128(uint64_t& lo, uint64_t& hi, int s) {
+  lo |= (lo >> s) | (hi << (64 - s));
+  hi |= hi >> s;
+}
+
+// padded shared index: 16 consecutive positions per thread -> stride 17 words
+__device__ __forceinline__ int hp(int j) { return j + (j >> 4); }
+
+// hashes of the m-mers at [j0, j0 + n) (m <= 32), rolled one base at a time
+__device__ __forceinline__ void hash_run(const uint32_t* spk, uint32_t* sh_h, int j0, int n, int m) {
+  const uint64_t mask = m == 32 ? ~0ull : ((1ull << (2 * m)) - 1);
+  const int hs = 2 * (m - 1);
+  uint64_t f = field64_s(spk, (uint32_t)j0, m);
+  uint64_t r = rc64_full(f) >> (64 - 2 * m);
+  uint64_t nxt = field64_s(spk, (uint32_t)(j0 + m), 32);  // bases j0 + m .., MSB-first
+  sh_h[hp(j0)] = mmer_hash64(f < r ? f : r);
+  for (int i = 1; i < n; i++) {
+    const uint32_t b = (uint32_t)(nxt >> 62);
+    nxt <<= 2;
+    f = ((f << 2) | b) & mask;
+    r = (r >> 2) | ((uint64_t)(b ^ 3u) << hs);
+    sh_h[hp(j0 + i)] = mmer_hash64(f < r ? f : r);
+  }
+}
+
 __device__ __forceinline__ bool in_range(uint32_t mval, uint32_t lo, uint32_t hi) {
   const uint32_t p1 = mix32(mval) >> (32 - P1_BITS);
   return p1 >= lo && p1 < hi;
@@ -74,19 +105,19 @@ __device__ __forceinline__ uint64_t bits64(const uint32_t* sfb, uint32_t q) {
 
 }  // namespace
 
-constexpr int MVL = SCAN_TILE + SCAN_TILE / 32 + 2;  // padded minimizer values
+constexpr int MVL = SCAN_TILE + SCAN_TILE / 16 + 2;  // minimizer values, padded like hp()
 constexpr int VBW = SCAN_TILE / 32;                   // validity bitmask words
+static_assert(WPT == 16, "one thread owns 16 windows");
+static_assert(HLP >= SCAN_TILE + 2, "events reuse the hash array");
 
-size_t scan_smem_bytes() { return (size_t)(PKW + FBW + 3 * HL + MVL + VBW) * sizeof(uint32_t); }
+size_t scan_smem_bytes() { return (size_t)(PKW + FBW + HLP + MVL + VBW) * sizeof(uint32_t); }
 
 __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   extern __shared__ __align__(16) uint32_t dyn[];
   uint32_t* spk = dyn;
   uint32_t* sfb = spk + PKW;
   uint32_t* sh_h = sfb + FBW;
-  uint32_t* sh_pl = sh_h + HL;
-  uint32_t* sh_sr = sh_pl + HL;
-  uint32_t* sh_mv = sh_sr + HL;
+  uint32_t* sh_mv = sh_h + HLP;
   uint32_t* sh_vb = sh_mv + MVL;
   uint32_t* ev = sh_h;  // reused once the minima are known: pos | start << 13 | rank << 14
   __shared__ Cnt2 shc[SCAN_THREADS + 1];
@@ -111,74 +142,110 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   }
   __syncthreads();
 
-  // m-mer hashes for positions [t0, t0 + SCAN_TILE + w - 1)
+  // m-mer hashes for positions [t0, t0 + SCAN_TILE + w - 1): 16 per thread,
+  // then the tail of w - 1 positions in runs of 16
   const int L = SCAN_TILE + w - 1;
-  for (int j = tid; j < L; j += SCANK_THREADS) sh_h[j] = mmer_hash_at(spk, (uint32_t)j, m);
-  __syncthreads();
-
-  // van Herk / Gil-Werman: prefix and suffix minima inside blocks of w
-  const int nblk = (L + w - 1) / w;
-  for (int b = tid; b < nblk; b += SCANK_THREADS) {
-    const int lo = b * w, hi = min(lo + w, L);
-    uint32_t run = 0xffffffffu;
-    for (int j = lo; j < hi; j++) { run = min(run, sh_h[j]); sh_pl[j] = run; }
-    run = 0xffffffffu;
-    for (int j = hi - 1; j >= lo; j--) { run = min(run, sh_h[j]); sh_sr[j] = run; }
-  }
-  __syncthreads();
-
-  // per window: minimizer value and validity, computed with consecutive
-  // threads on consecutive windows (conflict-free), kept as a padded array and
-  // a bitmask for the per-thread run logic below
-  const uint64_t vmask = (k - 1) >= 64 ? ~0ull : ((1ull << (k - 1)) - 1);
-  for (int r = tid; r < SCAN_TILE; r += SCANK_THREADS) {
-    const uint64_t gi = t0 + (uint64_t)r;
-    bool v = (gi + (uint64_t)k <= nb);
-    if (v && k > 1) v = (bits64(sfb, (uint32_t)(r + 1)) & vmask) == 0;
-    const unsigned bal = __ballot_sync(0xffffffffu, v);
-    if ((tid & 31) == 0) sh_vb[r >> 5] = bal;
-    sh_mv[r + (r >> 5)] = min(sh_sr[r], sh_pl[r + w - 1]);
-  }
-  __syncthreads();
   const int r0 = tid * WPT;
-  uint32_t mv[WPT + 1];
-  bool vd[WPT + 1];
-#pragma unroll
-  for (int i = 0; i <= WPT; i++) {
-    const int r = r0 + i - 1;  // i = 0 is the window before this thread's range
-    if (r < 0) { vd[i] = false; mv[i] = 0; continue; }
-    vd[i] = (sh_vb[r >> 5] >> (r & 31)) & 1u;
-    mv[i] = sh_mv[r + (r >> 5)];
+  if (m <= 32) {
+    hash_run(spk, sh_h, r0, WPT, m);
+    for (int j0 = SCAN_TILE + tid * WPT; j0 < L; j0 += SCANK_THREADS * WPT) hash_run(spk, sh_h, j0, min(WPT, L - j0), m);
+  } else {
+    for (int j = tid; j < L; j += SCANK_THREADS) sh_h[hp(j)] = mmer_hash_at(spk, (uint32_t)j, m);
   }
+  __syncthreads();
+
+  // minima of this thread's windows r0 .. r0 + 15 (window r spans h[r .. r + w - 1]):
+  // van Herk / Gil-Werman blocks of w aligned at r0.  Window i is block
+  // floor(i / w) when w divides i, else the suffix of that block from i plus
+  // the prefix of the next block up to i + w - 1.
+  uint32_t mvv[WPT];
+  {
+    const int nb_end = ((WPT - 1) / w + 1) * w;  // end of the block holding position 15
+    uint32_t run = 0xffffffffu;
+    for (int j = nb_end - 1; j >= WPT; j--) run = min(run, sh_h[hp(r0 + j)]);
+    int rem = (WPT - 1) % w;  // position within its block, counting down
+#pragma unroll
+    for (int i = WPT - 1; i >= 0; i--) {
+      run = min(run, sh_h[hp(r0 + i)]);
+      mvv[i] = run;  // suffix minimum of the block, from i
+      if (rem == 0) { run = 0xffffffffu; rem = w - 1; } else rem--;
+    }
+    int rb = 0;  // i mod w
+#pragma unroll
+    for (int i = 0; i < WPT; i++) {
+      const uint32_t hy = sh_h[hp(r0 + i + w - 1)];
+      if (rb == 0) run = 0xffffffffu;   // the window is one whole block
+      else if (rb == 1) run = hy;       // first position of the next block
+      else run = min(run, hy);
+      if (w == 1) run = 0xffffffffu;
+      mvv[i] = min(mvv[i], run);
+      if (++rb == w) rb = 0;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < WPT; i++) sh_mv[hp(r0 + i)] = mvv[i];
+
+  // validity, 32 windows per thread (threads 0 .. VBW-1): window r is valid iff
+  // t0 + r + k <= n_bases and no fragment starts at r + 1 .. r + k - 1.  With
+  // Y = fragment bits from position 32g + 1 on, the invalid windows are the
+  // OR of Y over k - 1 consecutive bits, built by doubling shifts (fragment
+  // starts are rare: most words skip it).
+  if (tid < VBW) {
+    const int g = tid;
+    const uint64_t xlo = (uint64_t)sfb[g] | ((uint64_t)sfb[g + 1] << 32);
+    const uint64_t xhi = (uint64_t)sfb[g + 2] | ((uint64_t)sfb[g + 3] << 32);
+    uint64_t ylo = (xlo >> 1) | (xhi << 63), yhi = xhi >> 1;
+    uint32_t inv = 0;
+    const int span = k - 1;
+    if (span > 0 && (ylo | yhi)) {
+      int c = 1;
+      while (2 * c <= span) { smear128(ylo, yhi, c); c *= 2; }
+      if (c < span) smear128(ylo, yhi, span - c);
+      inv = (uint32_t)ylo;
+    }
+    const uint64_t first = t0 + 32u * (uint64_t)g;
+    uint32_t inb;
+    if (first + 31u + (uint64_t)k <= nb) inb = 0xffffffffu;
+    else if (first + (uint64_t)k > nb) inb = 0u;
+    else inb = (1u << (uint32_t)(nb - (uint64_t)k - first + 1u)) - 1u;  // 1 .. 31 valid
+    sh_vb[g] = ~inv & inb;
+  }
+  __syncthreads();
+  uint32_t mv[WPT + 1];
+  mv[0] = r0 > 0 ? sh_mv[hp(r0 - 1)] : 0u;  // the window before this thread's range
+#pragma unroll
+  for (int i = 1; i <= WPT; i++) mv[i] = mvv[i - 1];
+  // 16-bit masks over this thread's windows (bit i = window r0 + i)
+  const uint32_t vb = (sh_vb[r0 >> 5] >> (r0 & 31)) & 0xffffu;
+  const uint32_t vbefore = r0 > 0 ? (sh_vb[(r0 - 1) >> 5] >> ((r0 - 1) & 31)) & 1u : 0u;
+  const uint32_t vprev = ((vb << 1) | vbefore) & 0xffffu;  // validity of the window before
+  uint32_t diff = 0;
+#pragma unroll
+  for (int i = 0; i < WPT; i++) diff |= (uint32_t)(mv[i + 1] != mv[i]) << i;
+  const uint32_t starts = vb & (~vprev | diff);  // a run begins
+  const uint32_t terms = ~vb & vprev;            // a run ends at an invalid window
   // key-range pass: only superkmers whose p1 digit is in [p1_lo, p1_hi) are
   // emitted; every start still ends the run before it
   const uint32_t p1_lo = a.p1_lo, p1_hi = a.p1_hi;
   const bool ranged = p1_lo > 0 || p1_hi < (uint32_t)NP1;  // uniform: one pass needs no check
-  Cnt2 c{0, 0};
+  uint32_t emitm = starts;
+  if (ranged) {
+    uint32_t inr = 0;
 #pragma unroll
-  for (int i = 1; i <= WPT; i++) {
-    const int r = r0 + i - 1;
-    const bool start = vd[i] && (r == 0 || !vd[i - 1] || mv[i] != mv[i - 1]);
-    const bool term = !vd[i] && r > 0 && vd[i - 1];
-    c.ev += (start || term);
-    if (start) c.st += !ranged || in_range(mv[i], p1_lo, p1_hi);
+    for (int i = 0; i < WPT; i++) inr |= (uint32_t)in_range(mv[i + 1], p1_lo, p1_hi) << i;
+    emitm &= inr;
   }
+  const Cnt2 c{(uint32_t)__popc(starts | terms), (uint32_t)__popc(emitm)};
   Cnt2 tot;
   const Cnt2 pre = block_exclusive_scan<Cnt2, Cnt2Op>(c, &tot, shc);
   // sh_h is free from here on (all reads of it finished before the scan's barriers)
   {
-    uint32_t e = pre.ev, sr = pre.st;
-#pragma unroll
-    for (int i = 1; i <= WPT; i++) {
-      const int r = r0 + i - 1;
-      const bool start = vd[i] && (r == 0 || !vd[i - 1] || mv[i] != mv[i - 1]);
-      const bool term = !vd[i] && r > 0 && vd[i - 1];
-      const bool emit = start && (!ranged || in_range(mv[i], p1_lo, p1_hi));
-      if (start || term) {
-        ev[e] = (uint32_t)r | ((uint32_t)emit << 13) | (sr << 14);
-        e++;
-      }
-      sr += emit;
+    uint32_t e = pre.ev;
+    for (uint32_t evm = starts | terms; evm; evm &= evm - 1) {
+      const int i = __ffs(evm) - 1;
+      const uint32_t emit = (emitm >> i) & 1u;
+      const uint32_t sr = pre.st + (uint32_t)__popc(emitm & ((1u << i) - 1u));
+      ev[e++] = (uint32_t)(r0 + i) | (emit << 13) | (sr << 14);
     }
   }
   if (tid == 0) {
@@ -196,7 +263,7 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
     const uint32_t r = v & 0x1fffu;
     const uint32_t end = ev[e + 1] & 0x1fffu;
     const uint32_t len = end - r;
-    const uint32_t mval = sh_mv[r + (r >> 5)];
+    const uint32_t mval = sh_mv[hp((int)r)];
     const uint64_t d = base + (v >> 14);
     a.desc[d] = ((t0 + r) << 24) | (uint64_t)(len - 1);
     a.key[d] = mix32(mval);
