@@ -115,6 +115,7 @@ struct mczi_ctx {
   mczi::DevBuf packed, fbits, input_base;
   mczi::DevBuf desc, key, desc2, key2, part_hist, part_tmp, bucket_off;
   mczi::DevBuf out_lo, out_hi, out_cnt, out_mask;
+  mczi::DevBuf cnt64;  // counts widened to u64 for direct copies to the caller
   mczi::DevBuf scalars;
   mczi::DevBuf mintab, pairtab;
   mczi::DevBuf zi_tmp0, zi_tmp1, zi_tmp2;

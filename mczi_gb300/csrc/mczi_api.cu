@@ -658,6 +658,11 @@ int32_t run_count_graph(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode,
   return rc;
 }
 
+__global__ void k_widen_counts(const uint32_t* __restrict__ in, uint64_t n, unsigned long long* __restrict__ out) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = in[i];
+}
+
 int32_t fetch_records(mczi_ctx* ctx, HostRecords* r) {
   const uint64_t n = ctx->n_out;
   r->lo.resize(n);
@@ -794,6 +799,27 @@ int32_t mczi_result_copy(mczi_ctx* ctx, uint64_t* key_lo, uint64_t* key_hi, uint
   if (!ctx->have_result) return fail(ctx, MCZI_ERR_STATE, "no result");
   if (cap < ctx->n_out) return fail(ctx, MCZI_ERR_STATE, "result buffer too small");
   cudaSetDevice(ctx->device);
+  if (!sorted) {
+    // emission order: straight into the caller's buffers (counts widened on
+    // the device), no host-side pass over the records
+    const uint64_t n = ctx->n_out;
+    cudaStream_t s = ctx->stream;
+    if (n == 0) return MCZI_OK;
+    if (key_lo) CK(cudaMemcpyAsync(key_lo, ctx->out_lo.p, n * 8, cudaMemcpyDeviceToHost, s));
+    if (key_hi) {
+      if (ctx->k > 32) CK(cudaMemcpyAsync(key_hi, ctx->out_hi.p, n * 8, cudaMemcpyDeviceToHost, s));
+      else std::fill(key_hi, key_hi + n, 0ull);
+    }
+    if (counts) {
+      CKA(ctx->cnt64, n * 8);
+      const unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx->sm_count * 8);
+      k_widen_counts<<<grid, 256, 0, s>>>(ctx->out_cnt.as<uint32_t>(), n, ctx->cnt64.as<unsigned long long>());
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(counts, ctx->cnt64.p, n * 8, cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    return MCZI_OK;
+  }
   HostRecords r;
   int32_t rc = fetch_records(ctx, &r);
   if (rc) return rc;

@@ -166,13 +166,22 @@ class Context:
         self.k = config.k
         return n.value
 
-    def records(self, n: int | None = None, sorted: bool = True) -> Records:
+    def records(self, n: int | None = None, sorted: bool = True, out=None) -> Records:
+        """The last result's records.  sorted=False keeps the kernels' emission
+        order and copies straight from the device into the arrays; `out` =
+        (lo, hi, counts) uint64 arrays of >= n entries (e.g. views of pinned
+        host memory, reused across calls; hi may be None for k <= 32)."""
         if n is None:
             st = self.run_stats()
             n = int(st[5])
-        lo = np.empty(n, dtype=np.uint64)
-        cnt = np.empty(n, dtype=np.uint64)
-        hi = np.empty(n, dtype=np.uint64) if self.k > 32 else None
+        if out is not None:
+            lo, hi, cnt = out
+            lo, cnt = lo[:n], cnt[:n]
+            hi = hi[:n] if (hi is not None and self.k > 32) else None
+        else:
+            lo = np.empty(n, dtype=np.uint64)
+            cnt = np.empty(n, dtype=np.uint64)
+            hi = np.empty(n, dtype=np.uint64) if self.k > 32 else None
         self._ck(self._lib.mczi_result_copy(self._h, lo.ctypes.data if n else None,
                                             hi.ctypes.data if (hi is not None and n) else None,
                                             cnt.ctypes.data if n else None, n, 1 if sorted else 0))

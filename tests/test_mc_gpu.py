@@ -324,3 +324,24 @@ def test_graph_replay_identical(gpu_ctx, oracle):
     finally:
         gpu_ctx.set_graph_replay(False)
         gpu_ctx.set_key_range_passes(0)
+
+
+@pytest.mark.parametrize("k,m", [(31, 15), (45, 17)])
+def test_records_into_caller_buffers(gpu_ctx, k, m):
+    """Unsorted records copied straight into caller-owned (oversized, reused)
+    arrays equal the sorted host path, record for record."""
+    from mczi_gb300.mc import CounterConfig
+    rng = np.random.default_rng(k)
+    data = random_fasta(rng, 300, 100, 900)
+    n = gpu_ctx.count([data], CounterConfig(k, m, 1))
+    ref = gpu_ctx.records(n, sorted=True)
+    bufs = [np.full(n + 17, 7, dtype=np.uint64) for _ in range(3)]
+    for _ in range(2):
+        r = gpu_ctx.records(n, sorted=False, out=(bufs[0], bufs[1] if k > 32 else None, bufs[2]))
+        assert len(r.lo) == n and len(r.count) == n
+        hi = r.hi if r.hi is not None else np.zeros_like(r.lo)
+        rhi = ref.hi if ref.hi is not None else np.zeros_like(ref.lo)
+        order = np.lexsort((r.lo, hi))
+        assert np.array_equal(r.lo[order], ref.lo) and np.array_equal(hi[order], rhi)
+        assert np.array_equal(r.count[order], ref.count)
+        assert (bufs[0][n:] == 7).all() and (bufs[2][n:] == 7).all()
