@@ -116,8 +116,10 @@ int32_t mczi_count_datasets_to_fasta_path(mczi_ctx* ctx, const char* const* inpu
 
 /* Per-phase device times (ms) of the last run, measured with CUDA events on
  * the context's stream: [0] pack, [1] minimizer scan, [2] partition,
- * [3] k-mer counting, [4] minimizer pre-count (0 when not run).
- * Returns the number of phases written. */
+ * [3] k-mer counting, [4] minimizer pre-count (0 when not run).  After a
+ * streamed mczi_count, [0] spans the overlapped staging + pack + scan and
+ * [1] only a rescan, if one was needed.  Returns the number of phases
+ * written. */
 int32_t mczi_phase_times(mczi_ctx* ctx, float* ms, int32_t cap);
 /* Statistics of the last run: [0] bases, [1] superkmers, [2] counting rounds,
  * [3] round splits, [4] distinct k-mers inserted, [5] kept records,
@@ -160,6 +162,15 @@ int32_t mczi_set_key_range_passes(mczi_ctx* ctx, int32_t passes);
  * before counting.  The filter is conservative, so results are identical with
  * it on or off; it only changes the work done.  Default off. */
 int32_t mczi_set_minimizer_precount(mczi_ctx* ctx, int32_t enable);
+
+/* Streamed staging of mczi_count (no reference counterpart: MC reads its
+ * inputs from files): the input bytes are copied to the device in segments
+ * while earlier segments are packed and scanned.  enable 0 stages everything
+ * first; segment_bytes (a multiple of 8192) sets the segment size, 0 =
+ * automatic (>= 32 MiB, about 16 segments).  Results are identical either way.
+ * Default on.  Batches that need several key-range passes or the pre-count,
+ * and graph replay, always stage first. */
+int32_t mczi_set_streamed_staging(mczi_ctx* ctx, int32_t enable, uint64_t segment_bytes);
 
 /* Packer parity hook: after mczi_count/mczi_count_staged, copies the 2-bit
  * codes (one byte per base) and fragment-start flags (one byte per base) of

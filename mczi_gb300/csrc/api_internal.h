@@ -5,6 +5,7 @@
 #include "mczi_internal.h"
 
 #include <string>
+#include <vector>
 
 namespace mczi {
 
@@ -116,6 +117,11 @@ struct mczi_ctx {
   mczi::DevBuf desc, key, desc2, key2, part_hist, part_tmp, bucket_off;
   mczi::DevBuf out_lo, out_hi, out_cnt, out_mask;
   mczi::DevBuf cnt64;  // counts widened to u64 for direct copies to the caller
+  mczi::DevBuf stream_scratch;     // streamed staging: pack carries, scan tile range
+  cudaStream_t copy_stream = nullptr;  // host-to-device copies of the streamed staging
+  cudaEvent_t ev_copy = nullptr;       // last copied segment
+  int streamed = 1;                    // one-shot counts overlap staging with pack + scan
+  uint64_t stream_seg_tiles = 0;       // segment size in pack tiles (0 = automatic)
   mczi::DevBuf scalars;
   mczi::DevBuf mintab, pairtab;
   mczi::DevBuf zi_tmp0, zi_tmp1, zi_tmp2;
@@ -201,7 +207,18 @@ struct Pipe {
 
 
 
+struct InputPlan {
+  std::vector<uint64_t> off, len;  // per input: text offset (tile-aligned), bytes
+  std::vector<uint32_t> tinfo;     // per tile
+  std::vector<uint64_t> tile0;     // per input: first tile
+  uint64_t text_len = 0, n_tiles = 0, skipped = 0, h2d_bytes = 0;
+};
+int32_t plan_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n, InputPlan& pl);
+int32_t stage_layout(mczi_ctx* ctx, const InputPlan& pl, size_t n);
+int32_t copy_text_range(mczi_ctx* ctx, const mczi_input* inputs, size_t n, const InputPlan& pl, uint64_t b0,
+                        uint64_t b1, cudaStream_t s);
 int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n);
+int32_t pack_prepare(mczi_ctx* ctx, Pipe& p, mczi::PackArgs& pa);
 int32_t pipe_pack(mczi_ctx* ctx, Pipe& p);
 int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m, uint32_t p1_lo = 0, uint32_t p1_hi = 1u << 12,
                   uint32_t passes = 1);

@@ -15,6 +15,8 @@
 //                     line state from the scan of pass 1
 //   3. k_pack_write : 2-bit codes and fragment-start bits, staged in shared
 //                     memory, interior words stored, edge words OR-ed.
+#include <algorithm>
+
 #include "mczi_internal.h"
 #include "scan.cuh"
 
@@ -187,9 +189,10 @@ __device__ __forceinline__ void tile_line_state(const uint8_t* __restrict__ text
 
 __global__ void __launch_bounds__(PACK_THREADS) k_pack_lines(const uint8_t* __restrict__ text,
                                                              const uint32_t* __restrict__ tile_info,
-                                                             uint64_t n_tiles, LineSum* __restrict__ out) {
-  const uint64_t tile = blockIdx.x;
-  if (tile >= n_tiles) return;
+                                                             uint64_t tile_lo, uint64_t tile_hi,
+                                                             LineSum* __restrict__ out) {
+  const uint64_t tile = tile_lo + blockIdx.x;
+  if (tile >= tile_hi) return;
   const uint4* src = reinterpret_cast<const uint4*>(text + tile * PACK_TILE);
   int32_t last = -1;
   uint32_t nl = 0;
@@ -241,12 +244,12 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_lines(const uint8_t* __re
 __global__ void __launch_bounds__(PACK_THREADS) k_pack_count(const uint8_t* __restrict__ text,
                                                              const uint32_t* __restrict__ tile_info,
                                                              const uint64_t* __restrict__ input_tile0,
-                                                             const LineSum* __restrict__ line_pre, uint64_t n_tiles,
-                                                             BaseSum* __restrict__ out) {
+                                                             const LineSum* __restrict__ line_pre, uint64_t tile_lo,
+                                                             uint64_t tile_hi, BaseSum* __restrict__ out) {
   __shared__ __align__(16) uint8_t sb[PACK_TILE];
   __shared__ BaseSum shs[SCAN_THREADS + 1];
-  const uint64_t tile = blockIdx.x;
-  if (tile >= n_tiles) return;
+  const uint64_t tile = tile_lo + blockIdx.x;
+  if (tile >= tile_hi) return;
   load_tile(text, tile, sb);
   bool fastq;
   uint32_t tst, tl4;
@@ -277,15 +280,16 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __re
                                                              const uint32_t* __restrict__ tile_info,
                                                              const uint64_t* __restrict__ input_tile0,
                                                              const LineSum* __restrict__ line_pre,
-                                                             const BaseSum* __restrict__ base_pre, uint64_t n_tiles,
-                                                             uint32_t* __restrict__ packed, uint32_t* __restrict__ fbits,
+                                                             const BaseSum* __restrict__ base_pre, uint64_t tile_lo,
+                                                             uint64_t tile_hi, uint32_t* __restrict__ packed,
+                                                             uint32_t* __restrict__ fbits,
                                                              uint64_t* __restrict__ input_base) {
   __shared__ __align__(16) uint8_t sb[PACK_TILE];
   __shared__ BaseSum shs[SCAN_THREADS + 1];
   __shared__ uint32_t spk[PACK_TILE / 16 + 3];
   __shared__ uint32_t sfb[PACK_TILE / 32 + 2];
-  const uint64_t tile = blockIdx.x;
-  if (tile >= n_tiles) return;
+  const uint64_t tile = tile_lo + blockIdx.x;
+  if (tile >= tile_hi) return;
   load_tile(text, tile, sb);
   for (int i = threadIdx.x; i < PACK_TILE / 16 + 2; i += PACK_THREADS) spk[i] = 0;
   for (int i = threadIdx.x; i < PACK_TILE / 32 + 2; i += PACK_THREADS) sfb[i] = 0;
@@ -357,16 +361,36 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __re
   }
 }
 
-void launch_pack(const PackArgs& a, cudaStream_t s) {
-  if (a.n_tiles == 0) return;
-  k_pack_lines<<<(unsigned)a.n_tiles, PACK_THREADS, 0, s>>>(a.text, a.tile_info, a.n_tiles, a.line_sum);
-  exclusive_scan<LineSum, LineOp>(a.line_sum, a.line_pre, a.n_tiles, a.line_tmp, s);
-  k_pack_count<<<(unsigned)a.n_tiles, PACK_THREADS, 0, s>>>(a.text, a.tile_info, a.input_tile0, a.line_pre,
-                                                             a.n_tiles, a.base_sum);
-  exclusive_scan<BaseSum, BaseOp>(a.base_sum, a.base_pre, a.n_tiles, a.base_tmp, s);
-  k_pack_write<<<(unsigned)a.n_tiles, PACK_THREADS, 0, s>>>(a.text, a.tile_info, a.input_tile0, a.line_pre,
-                                                             a.base_pre, a.n_tiles, a.packed, a.fbits,
-                                                             a.input_base);
+// pre[i] = carry (+) pre[i] for i < n: a segment's local exclusive prefix
+// made global (the carry is the total of all earlier segments)
+template <class T, class Op>
+__global__ void k_apply_carry(T* __restrict__ pre, uint64_t n, const T* __restrict__ carry) {
+  const T c = *carry;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    pre[i] = Op::combine(c, pre[i]);
+}
+
+void launch_pack(const PackArgs& a, cudaStream_t s) { launch_pack_segment(a, 0, a.n_tiles, nullptr, nullptr, s); }
+
+void launch_pack_segment(const PackArgs& a, uint64_t t0, uint64_t t1, LineSum* carry_line, BaseSum* carry_base,
+                         cudaStream_t s) {
+  if (t1 <= t0) return;
+  const uint64_t n = t1 - t0;
+  const unsigned grid = (unsigned)n;
+  const unsigned cgrid = (unsigned)std::min<uint64_t>((n + 1 + 255) / 256, 1024);
+  // a later segment saves the running totals (written at its first tile by the
+  // previous segment) before its local scans overwrite them
+  const bool chained = t0 > 0;
+  k_pack_lines<<<grid, PACK_THREADS, 0, s>>>(a.text, a.tile_info, t0, t1, a.line_sum);
+  if (chained) cudaMemcpyAsync(carry_line, a.line_pre + t0, sizeof(LineSum), cudaMemcpyDeviceToDevice, s);
+  exclusive_scan<LineSum, LineOp>(a.line_sum + t0, a.line_pre + t0, n, a.line_tmp, s);
+  if (chained) k_apply_carry<LineSum, LineOp><<<cgrid, 256, 0, s>>>(a.line_pre + t0, n + 1, carry_line);
+  k_pack_count<<<grid, PACK_THREADS, 0, s>>>(a.text, a.tile_info, a.input_tile0, a.line_pre, t0, t1, a.base_sum);
+  if (chained) cudaMemcpyAsync(carry_base, a.base_pre + t0, sizeof(BaseSum), cudaMemcpyDeviceToDevice, s);
+  exclusive_scan<BaseSum, BaseOp>(a.base_sum + t0, a.base_pre + t0, n, a.base_tmp, s);
+  if (chained) k_apply_carry<BaseSum, BaseOp><<<cgrid, 256, 0, s>>>(a.base_pre + t0, n + 1, carry_base);
+  k_pack_write<<<grid, PACK_THREADS, 0, s>>>(a.text, a.tile_info, a.input_tile0, a.line_pre, a.base_pre, t0, t1,
+                                             a.packed, a.fbits, a.input_base);
 }
 
 }  // namespace mczi

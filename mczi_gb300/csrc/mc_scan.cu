@@ -124,7 +124,12 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   __shared__ unsigned long long s_base;
 
   const uint64_t nb = *a.n_bases;
-  const uint64_t t0 = (uint64_t)blockIdx.x * SCAN_TILE;
+  uint64_t tile = blockIdx.x;
+  if (a.tile_range) {
+    tile += a.tile_range[0];
+    if (tile >= a.tile_range[1]) return;
+  }
+  const uint64_t t0 = tile * SCAN_TILE;
   const int k = a.k, m = a.m, w = k - m + 1;
   if (t0 + (uint64_t)k > nb) return;  // no valid window in this tile (uniform per CTA)
   const int tid = threadIdx.x;
@@ -270,16 +275,50 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   }
 }
 
+// packed bases a tile reads past its first window: the staged words and bits
+constexpr uint64_t SCAN_NEED = (uint64_t)(PKW * 16 > FBW * 32 ? PKW * 16 : FBW * 32);
+
+__global__ void k_scan_window(const uint64_t* __restrict__ avail, uint64_t* __restrict__ range, int final,
+                              uint64_t max_tiles, uint32_t* __restrict__ status) {
+  const uint64_t nb = *avail, lo = range[1];
+  uint64_t hi;
+  if (final) hi = (nb + SCAN_TILE - 1) / SCAN_TILE;
+  else hi = nb >= SCAN_NEED ? (nb - SCAN_NEED) / SCAN_TILE + 1 : 0;
+  if (hi < lo) hi = lo;
+  if (hi - lo > max_tiles) {
+    // more tiles than this launch covers: the rest waits for the next window,
+    // and a final window that cannot finish sends the host to a full rescan
+    hi = lo + max_tiles;
+    if (final) atomicOr(status, ST_DESC_OVERFLOW);
+  }
+  range[0] = lo;
+  range[1] = hi;
+}
+
+static void scan_attr() {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scan_smem_bytes());
+    attr_set = true;
+  }
+}
+
 void launch_scan(const ScanArgs& a, cudaStream_t s) {
   const uint64_t ntiles = (a.max_bases + SCAN_TILE - 1) / SCAN_TILE;
   if (ntiles == 0) return;
-  const size_t smem = scan_smem_bytes();
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr_set = true;
-  }
-  k_scan<<<(unsigned)ntiles, SCANK_THREADS, smem, s>>>(a);
+  scan_attr();
+  k_scan<<<(unsigned)ntiles, SCANK_THREADS, scan_smem_bytes(), s>>>(a);
+}
+
+void launch_scan_window(const uint64_t* avail, uint64_t* range, bool final, uint64_t max_tiles, uint32_t* status,
+                        cudaStream_t s) {
+  k_scan_window<<<1, 1, 0, s>>>(avail, range, final ? 1 : 0, max_tiles, status);
+}
+
+void launch_scan_range(const ScanArgs& a, uint64_t max_tiles, cudaStream_t s) {
+  if (max_tiles == 0) return;
+  scan_attr();
+  k_scan<<<(unsigned)max_tiles, SCANK_THREADS, scan_smem_bytes(), s>>>(a);
 }
 
 }  // namespace mczi

@@ -74,66 +74,101 @@ int detect_format(const uint8_t* d, uint64_t n) {
 
 }  // namespace
 
-int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n) {
-  ctx->staged = false;
-  ctx->have_result = false;
+// Host-side layout of a batch of inputs in HBM: each input starts on a
+// PACK_TILE boundary, the gaps are '\n'; per tile: input << 2 | fastq << 1 |
+// input starts here.
+int32_t plan_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n, InputPlan& pl) {
   if (n == 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "at least one input file is required");
-  std::vector<uint64_t> off(n), len(n);
+  pl.off.assign(n, 0);
+  pl.len.assign(n, 0);
   std::vector<int> fmt(n);
   uint64_t pos = 0;
-  ctx->skipped = 0;
-  ctx->h2d_bytes = 0;
+  pl.skipped = 0;
+  pl.h2d_bytes = 0;
   for (size_t i = 0; i < n; i++) {
     const uint8_t* d = inputs[i].data;
     uint64_t l = d ? inputs[i].len : 0;
     int f = detect_format(d, l);
     if (f < 0) {
       std::fprintf(stderr, "MC_WARN\tskipped_invalid_fastx_input\tinput\t%zu\terror\tInvalid record start\n", i);
-      ctx->skipped++;
+      pl.skipped++;
       l = 0;
       f = 0;
     }
     if (f == 2) { l = 0; f = 0; }
-    off[i] = pos;
-    len[i] = l;
+    pl.off[i] = pos;
+    pl.len[i] = l;
     fmt[i] = f;
+    pl.h2d_bytes += l;
     const uint64_t tiles = l == 0 ? 1 : (l + PACK_TILE - 1) / PACK_TILE;  // every input owns >= 1 tile
     pos += tiles * PACK_TILE;
   }
-  const uint64_t text_len = pos;
-  const uint64_t n_tiles = text_len / PACK_TILE;
-  std::vector<uint32_t> tinfo(n_tiles);
-  std::vector<uint64_t> tile0(n);
+  pl.text_len = pos;
+  pl.n_tiles = pos / PACK_TILE;
+  pl.tinfo.assign(pl.n_tiles, 0);
+  pl.tile0.assign(n, 0);
   for (size_t i = 0; i < n; i++) {
-    const uint64_t t0 = off[i] / PACK_TILE;
-    const uint64_t t1 = (i + 1 < n ? off[i + 1] : text_len) / PACK_TILE;
-    tile0[i] = t0;
-    for (uint64_t t = t0; t < t1; t++) tinfo[t] = ((uint32_t)i << 2) | ((uint32_t)fmt[i] << 1) | (t == t0 ? 1u : 0u);
+    const uint64_t t0 = pl.off[i] / PACK_TILE;
+    const uint64_t t1 = (i + 1 < n ? pl.off[i + 1] : pl.text_len) / PACK_TILE;
+    pl.tile0[i] = t0;
+    for (uint64_t t = t0; t < t1; t++) pl.tinfo[t] = ((uint32_t)i << 2) | ((uint32_t)fmt[i] << 1) | (t == t0 ? 1u : 0u);
   }
-  CKA(ctx->text, text_len);
-  CKA(ctx->tile_info, n_tiles * sizeof(uint32_t));
+  return MCZI_OK;
+}
+
+// Device buffers for a plan, the tile tables copied (their host vectors are
+// pageable: the copies are staged before return); the text is not copied.
+int32_t stage_layout(mczi_ctx* ctx, const InputPlan& pl, size_t n) {
+  ctx->staged = false;
+  ctx->have_result = false;
+  CKA(ctx->text, pl.text_len);
+  CKA(ctx->tile_info, pl.n_tiles * sizeof(uint32_t));
   CKA(ctx->input_tile0, n * sizeof(uint64_t));
   cudaStream_t s = ctx->stream;
-  for (size_t i = 0; i < n; i++) {
-    uint8_t* dst = ctx->text.as<uint8_t>() + off[i];
-    if (len[i]) CK(cudaMemcpyAsync(dst, inputs[i].data, len[i], cudaMemcpyHostToDevice, s));
-    ctx->h2d_bytes += len[i];
-    const uint64_t end = i + 1 < n ? off[i + 1] : text_len;
-    if (off[i] + len[i] < end) CK(cudaMemsetAsync(dst + len[i], '\n', end - off[i] - len[i], s));
-  }
-  CK(cudaMemcpyAsync(ctx->tile_info.p, tinfo.data(), n_tiles * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(ctx->input_tile0.p, tile0.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
-  // the host vectors above are pageable: the copies complete before return
-  CK(cudaStreamSynchronize(s));
-  ctx->text_len = text_len;
-  ctx->n_tiles = n_tiles;
+  CK(cudaMemcpyAsync(ctx->tile_info.p, pl.tinfo.data(), pl.n_tiles * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ctx->input_tile0.p, pl.tile0.data(), n * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+  ctx->text_len = pl.text_len;
+  ctx->n_tiles = pl.n_tiles;
   ctx->n_inputs = (int)n;
+  ctx->skipped = pl.skipped;
+  ctx->h2d_bytes = pl.h2d_bytes;
+  return MCZI_OK;
+}
+
+// Copies the text bytes [b0, b1) of the batch (inputs and their '\n' gaps)
+// on stream s.
+int32_t copy_text_range(mczi_ctx* ctx, const mczi_input* inputs, size_t n, const InputPlan& pl, uint64_t b0,
+                        uint64_t b1, cudaStream_t s) {
+  uint8_t* text = ctx->text.as<uint8_t>();
+  for (size_t i = 0; i < n; i++) {
+    const uint64_t o = pl.off[i], e = pl.off[i] + pl.len[i];
+    const uint64_t end = i + 1 < n ? pl.off[i + 1] : pl.text_len;
+    if (end <= b0) continue;
+    if (o >= b1) break;
+    const uint64_t c0 = std::max(o, b0), c1 = std::min(e, b1);
+    if (c1 > c0) CK(cudaMemcpyAsync(text + c0, inputs[i].data + (c0 - o), c1 - c0, cudaMemcpyHostToDevice, s));
+    const uint64_t g0 = std::max(e, b0), g1 = std::min(end, b1);
+    if (g1 > g0) CK(cudaMemsetAsync(text + g0, '\n', g1 - g0, s));
+  }
+  return MCZI_OK;
+}
+
+int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n) {
+  ctx->staged = false;
+  ctx->have_result = false;
+  InputPlan pl;
+  int32_t rc = plan_inputs(ctx, inputs, n, pl);
+  if (rc) return rc;
+  if ((rc = stage_layout(ctx, pl, n))) return rc;
+  if ((rc = copy_text_range(ctx, inputs, n, pl, 0, pl.text_len, ctx->stream))) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
   ctx->staged = true;
   return MCZI_OK;
 }
 
 
-int32_t pipe_pack(mczi_ctx* ctx, Pipe& p) {
+// pack buffers (zeroed streams) and arguments for the staged layout
+int32_t pack_prepare(mczi_ctx* ctx, Pipe& p, PackArgs& pa) {
   cudaStream_t s = ctx->stream;
   const uint64_t n_tiles = ctx->n_tiles, text_len = ctx->text_len;
   const int n_in = ctx->n_inputs;
@@ -152,8 +187,7 @@ int32_t pipe_pack(mczi_ctx* ctx, Pipe& p) {
   CKA(ctx->input_base, ((size_t)n_in + 1) * sizeof(uint64_t));
   CK(cudaMemsetAsync(ctx->packed.p, 0, pwords * 4, s));
   CK(cudaMemsetAsync(ctx->fbits.p, 0, fwords * 4, s));
-  if (!p.capture) CK(cudaEventRecord(ctx->ev[0], s));
-  PackArgs pa;
+  pa = PackArgs{};
   pa.text = ctx->text.as<uint8_t>();
   pa.tile_info = ctx->tile_info.as<uint32_t>();
   pa.input_tile0 = ctx->input_tile0.as<uint64_t>();
@@ -167,11 +201,21 @@ int32_t pipe_pack(mczi_ctx* ctx, Pipe& p) {
   pa.packed = ctx->packed.as<uint32_t>();
   pa.fbits = ctx->fbits.as<uint32_t>();
   pa.input_base = ctx->input_base.as<uint64_t>();
-  launch_pack(pa, s);
-  p.launches += 9;
   p.pwords = pwords;
   p.d_nbases = reinterpret_cast<const uint64_t*>(ctx->base_pre.as<BaseSum>() + n_tiles);
-  CK(cudaMemcpyAsync(ctx->input_base.as<uint64_t>() + n_in, p.d_nbases, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+  return MCZI_OK;
+}
+
+int32_t pipe_pack(mczi_ctx* ctx, Pipe& p) {
+  cudaStream_t s = ctx->stream;
+  PackArgs pa;
+  int32_t rc = pack_prepare(ctx, p, pa);
+  if (rc) return rc;
+  if (!p.capture) CK(cudaEventRecord(ctx->ev[0], s));
+  launch_pack(pa, s);
+  p.launches += 9;
+  CK(cudaMemcpyAsync(ctx->input_base.as<uint64_t>() + ctx->n_inputs, p.d_nbases, sizeof(uint64_t),
+                     cudaMemcpyDeviceToDevice, s));
   CK(cudaGetLastError());
   if (!p.capture) CK(cudaEventRecord(ctx->ev[1], s));
   return MCZI_OK;
@@ -203,7 +247,7 @@ int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m, uint32_t p1_lo, uint32_t
     CKA(ctx->key, desc_cap * 4);
     CK(cudaMemsetAsync(sc + SC_NDESC, 0, 8, s));
     if (!p.capture) CK(cudaMemsetAsync(sc + SC_STATUS, 0, 8, s));
-    ScanArgs sa;
+    ScanArgs sa{};
     sa.packed = ctx->packed.as<uint32_t>();
     sa.fbits = ctx->fbits.as<uint32_t>();
     sa.n_bases = p.d_nbases;
@@ -528,6 +572,116 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
 }
 
 
+// One-shot count with the staging overlapped: the text is copied in segments
+// on the copy stream; each segment is packed as soon as it has arrived (the
+// pack's prefix scans continue from the previous segment's totals) and the
+// base tiles whose packed words are complete are scanned right after.  The
+// rest of the pipeline is run_count's.  Inputs that need several key-range
+// passes, the minimizer pre-count or no device work at all take the plain
+// path (stage, then count).
+int32_t run_count_streamed(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, const mczi_input* inputs,
+                           size_t n, uint64_t* n_records) {
+  int32_t rc;
+  InputPlan pl;
+  if ((rc = plan_inputs(ctx, inputs, n, pl))) return rc;
+  if ((rc = stage_layout(ctx, pl, n))) return rc;
+  ctx->mask_words = 0;
+  const int k = (int)cfg->k, m = (int)cfg->minimizer;
+  const uint32_t passes = key_range_passes(ctx, k, m);
+  // segments of >= 32 MiB of text, about 16 per batch
+  const uint64_t seg_min = ctx->stream_seg_tiles > 0 ? ctx->stream_seg_tiles : 4096;
+  const bool plain = passes > 1 || ctx->precount || !ctx->streamed || pl.n_tiles < 2 * seg_min ||
+                     (mode == MCZI_MODE_PRESENCE && cfg->threshold >= (uint64_t)n);
+  if (plain) {
+    if ((rc = copy_text_range(ctx, inputs, n, pl, 0, pl.text_len, ctx->stream))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->staged = true;
+    return run_count(ctx, cfg, mode, n_records);
+  }
+  cudaStream_t s = ctx->stream, cs = ctx->copy_stream;
+  for (int i = 0; i < N_PHASES; i++) ctx->phase_ms[i] = 0.f;
+  Pipe p;
+  std::memset(ctx->stats, 0, sizeof ctx->stats);
+  PackArgs pa;
+  if ((rc = pack_prepare(ctx, p, pa))) return rc;
+  // scan buffers, as pipe_scan sizes them
+  uint64_t* sc = ctx->scalars.as<uint64_t>();
+  const int w = k - m + 1;
+  uint64_t desc_cap = pl.text_len * 3 / (uint64_t)(w + 1) + (1u << 20);
+  if (desc_cap > pl.text_len + 1024) desc_cap = pl.text_len + 1024;
+  CKA(ctx->desc, desc_cap * 8);
+  CKA(ctx->key, desc_cap * 4);
+  CK(cudaMemsetAsync(sc + SC_NDESC, 0, 8, s));
+  CK(cudaMemsetAsync(sc + SC_STATUS, 0, 8, s));
+  CKA(ctx->stream_scratch, 256);
+  uint8_t* scr = ctx->stream_scratch.as<uint8_t>();
+  LineSum* carry_line = reinterpret_cast<LineSum*>(scr);
+  BaseSum* carry_base = reinterpret_cast<BaseSum*>(scr + 64);
+  uint64_t* range = reinterpret_cast<uint64_t*>(scr + 128);
+  CK(cudaMemsetAsync(range, 0, 16, s));
+  ScanArgs sa{};
+  sa.packed = ctx->packed.as<uint32_t>();
+  sa.fbits = ctx->fbits.as<uint32_t>();
+  sa.max_bases = pl.text_len;
+  sa.packed_words = p.pwords;
+  sa.k = k;
+  sa.m = m;
+  sa.desc = ctx->desc.as<uint64_t>();
+  sa.key = ctx->key.as<uint32_t>();
+  sa.n_desc = reinterpret_cast<unsigned long long*>(sc + SC_NDESC);
+  sa.desc_cap = desc_cap;
+  sa.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
+  sa.p1_lo = 0;
+  sa.p1_hi = NP1;
+  sa.tile_range = range;
+  // the copy stream starts after this stream's buffer set-up (the memsets of
+  // the packed streams and the tile tables)
+  CK(cudaEventRecord(ctx->ev_copy, s));
+  CK(cudaStreamWaitEvent(cs, ctx->ev_copy, 0));
+  CK(cudaEventRecord(ctx->ev[0], s));
+  const uint64_t nseg_target = 16;
+  const uint64_t seg = ctx->stream_seg_tiles > 0 ? ctx->stream_seg_tiles
+                                                 : std::max<uint64_t>(seg_min, (pl.n_tiles + nseg_target - 1) / nseg_target);
+  for (uint64_t t0 = 0; t0 < pl.n_tiles; t0 += seg) {
+    const uint64_t t1 = std::min(pl.n_tiles, t0 + seg);
+    const bool last = t1 == pl.n_tiles;
+    if ((rc = copy_text_range(ctx, inputs, n, pl, t0 * PACK_TILE, t1 * PACK_TILE, cs))) return rc;
+    CK(cudaEventRecord(ctx->ev_copy, cs));
+    CK(cudaStreamWaitEvent(s, ctx->ev_copy, 0));
+    launch_pack_segment(pa, t0, t1, carry_line, carry_base, s);
+    p.launches += t0 > 0 ? 11 : 9;
+    // bases packed so far (the running total at the next segment's first tile)
+    const uint64_t* avail = reinterpret_cast<const uint64_t*>(pa.base_pre + t1);
+    sa.n_bases = avail;
+    const uint64_t max_tiles = (t1 - t0) * (PACK_TILE / SCAN_TILE) + 4;  // new bases <= new text bytes
+    launch_scan_window(avail, range, last, max_tiles, sa.status, s);
+    launch_scan_range(sa, max_tiles, s);
+    p.launches += 2;
+    CK(cudaGetLastError());
+  }
+  CK(cudaMemcpyAsync(ctx->input_base.as<uint64_t>() + n, p.d_nbases, sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+  CK(cudaEventRecord(ctx->ev[1], s));
+  ctx->staged = true;
+  uint64_t h[2];
+  CK(cudaMemcpyAsync(h, sc + SC_NDESC, 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(h + 1, sc + SC_STATUS, 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (h[1] & ST_DESC_OVERFLOW) {
+    if ((rc = pipe_scan(ctx, p, k, m, 0, NP1, 1))) return rc;  // rescans every tile with room to spare
+  } else {
+    p.n_desc = h[0];
+    p.desc_cap = desc_cap;
+    ctx->cap_desc = std::max(ctx->cap_desc, desc_cap);
+  }
+  uint64_t n_out = 0;
+  if ((rc = pipe_partition(ctx, p))) return rc;
+  if ((rc = pipe_count(ctx, p, k, cfg->threshold, mode, false, &n_out, false))) return rc;
+  p.n_desc_total += p.n_desc;
+  if ((rc = pipe_finish(ctx, p, mode, k, m, cfg->threshold, n_out))) return rc;
+  if (n_records) *n_records = n_out;
+  return MCZI_OK;
+}
+
 GraphSig make_sig(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint32_t passes) {
   GraphSig g;
   g.text_len = ctx->text_len;
@@ -733,6 +887,8 @@ int32_t mczi_open(int32_t device, mczi_ctx** out) {
   for (auto& ev : ctx->ev) cudaEventCreate(&ev);
   for (auto& ev : ctx->ev_pre) cudaEventCreate(&ev);
   for (auto& ev : ctx->ev_graph) cudaEventCreate(&ev);
+  cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+  cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming);
   *out = ctx;
   return MCZI_OK;
 }
@@ -752,6 +908,8 @@ int32_t mczi_close(mczi_ctx* ctx) {
   for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
   for (auto& ev : ctx->ev_pre) if (ev) cudaEventDestroy(ev);
   for (auto& ev : ctx->ev_graph) if (ev) cudaEventDestroy(ev);
+  if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   drop_graph(ctx);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
@@ -788,9 +946,10 @@ int32_t mczi_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int32_t mode, 
   cudaSetDevice(ctx->device);
   int32_t rc = validate(ctx, cfg, mode);
   if (rc) return rc;
+  if (!ctx->graph_mode) return run_count_streamed(ctx, cfg, mode, inputs, n_inputs, n_records);
   rc = stage_inputs(ctx, inputs, n_inputs);
   if (rc) return rc;
-  return ctx->graph_mode ? run_count_graph(ctx, cfg, mode, n_records) : run_count(ctx, cfg, mode, n_records);
+  return run_count_graph(ctx, cfg, mode, n_records);
 }
 
 int32_t mczi_result_copy(mczi_ctx* ctx, uint64_t* key_lo, uint64_t* key_hi, uint64_t* counts, uint64_t cap,
@@ -936,6 +1095,14 @@ int32_t mczi_set_count_filter(mczi_ctx* ctx, int32_t mode) {
   if (!ctx) return MCZI_ERR_STATE;
   if (mode < -1 || mode > 1) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "filter mode must be -1, 0 or 1");
   ctx->count_filter = mode;
+  return MCZI_OK;
+}
+
+int32_t mczi_set_streamed_staging(mczi_ctx* ctx, int32_t enable, uint64_t segment_bytes) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (segment_bytes % PACK_TILE) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "segment size must be a multiple of 8192");
+  ctx->streamed = enable ? 1 : 0;
+  ctx->stream_seg_tiles = segment_bytes / PACK_TILE;
   return MCZI_OK;
 }
 

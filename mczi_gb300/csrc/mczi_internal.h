@@ -37,6 +37,10 @@ struct PackArgs {
   uint64_t* input_base;  // first base of each input
 };
 void launch_pack(const PackArgs& a, cudaStream_t s);
+// tiles [t0, t1) only, after tiles [0, t0): the prefix scans continue from the
+// running totals (carry_* are one-element device scratch each)
+void launch_pack_segment(const PackArgs& a, uint64_t t0, uint64_t t1, LineSum* carry_line, BaseSum* carry_base,
+                         cudaStream_t s);
 
 // partition digits of the superkmer key (mix32 of the minimizer value)
 constexpr int P1_BITS = 12;
@@ -61,8 +65,16 @@ struct ScanArgs {
   uint64_t desc_cap;
   uint32_t* status;
   uint32_t p1_lo, p1_hi;     // emit superkmers with key >> (32 - P1_BITS) in [p1_lo, p1_hi)
+  const uint64_t* tile_range;  // null: every tile; else device [first, end) of the tiles to scan
 };
 void launch_scan(const ScanArgs& a, cudaStream_t s);
+// Streamed scan: `range` (device, two words, start zeroed) advances to the
+// tiles whose packed words are complete given `avail` packed bases (all tiles
+// when `final`), at most `max_tiles` of them; a final window with more sets
+// ST_DESC_OVERFLOW.  launch_scan_range then scans the range.
+void launch_scan_window(const uint64_t* avail, uint64_t* range, bool final, uint64_t max_tiles, uint32_t* status,
+                        cudaStream_t s);
+void launch_scan_range(const ScanArgs& a, uint64_t max_tiles, cudaStream_t s);
 
 // ---------------------------------------------------------------- K3 partition
 constexpr int PART_CTAS = 304;   // 2 per SM on a 152-SM GB300

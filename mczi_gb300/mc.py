@@ -221,6 +221,11 @@ class Context:
         """0 = automatic; n forces n passes over disjoint minimizer-key ranges."""
         self._ck(self._lib.mczi_set_key_range_passes(self._h, passes))
 
+    def set_streamed_staging(self, enable: bool = True, segment_bytes: int = 0) -> None:
+        """count() copies its inputs in segments overlapped with pack + scan
+        (default on; segment_bytes a multiple of 8192, 0 = automatic)."""
+        self._ck(self._lib.mczi_set_streamed_staging(self._h, 1 if enable else 0, segment_bytes))
+
     def set_minimizer_precount(self, enable: bool) -> None:
         self._ck(self._lib.mczi_set_minimizer_precount(self._h, 1 if enable else 0))
 
