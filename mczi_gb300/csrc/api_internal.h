@@ -60,7 +60,7 @@ struct DevBuf {
 
 // device scalars, in u64 slots
 enum { SC_NDESC = 0, SC_NOUT = 1, SC_STATS = 2, SC_STATUS = 10, SC_WORK = 11, SC_NKEPT = 12, SC_NRUNS = 13,
-       SC_SCANST = 14, SC_COUNT = 16 };
+       SC_SCANST = 14, SC_NABSW = 15, SC_COUNT = 16 };
 
 constexpr int N_PHASES = 5;
 constexpr int MPHF_MAX_LEVELS = 40;
@@ -74,6 +74,7 @@ struct ZiIndex {
   uint64_t n_bases = 0;
   DevBuf sk;             // superkmer descriptors grouped by bucket
   DevBuf bucket_off;     // n_keys + 1 offsets into sk (u32)
+  DevBuf bucket_key;     // the superkmer key (minimizer) of each bucket (u32)
   DevBuf bits, rank;     // MPHF bit vector (u64 words) and per-word rank (u32)
   uint64_t n_keys = 0, n_sk = 0, n_words = 0;
   int levels = 0;
@@ -124,7 +125,7 @@ struct mczi_ctx {
   uint64_t stream_seg_tiles = 0;       // segment size in pack tiles (0 = automatic)
   mczi::DevBuf scalars;
   mczi::DevBuf mintab, pairtab;
-  mczi::DevBuf zi_tmp0, zi_tmp1, zi_tmp2;
+  mczi::DevBuf zi_tmp0, zi_tmp1, zi_tmp2, zi_tmp3, zi_tmp4;
 
   // staged inputs
   bool staged = false;

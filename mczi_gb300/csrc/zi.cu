@@ -20,16 +20,19 @@
 // The minimizer value is a function of the canonical k-mer (both strands hold
 // the same canonical m-mers), so a present k-mer always finds its index
 // superkmer in that bucket; a key outside the MPHF's set lands in an
-// arbitrary bucket or none, and the comparison rejects it.  sshash-lib's own
-// layout is not reproduced; only its answers are.
+// arbitrary bucket (whose stored key differs: all its windows are absent) or
+// none.  sshash-lib's own layout is not reproduced; only its answers are.
 //
 // Streaming: one lookup per query superkmer (consecutive windows share the
 // minimizer), like sshash's streaming query.  Absent windows are emitted as
-// run descriptors carrying the superkmer's partition key, so the MC partition
-// and counting kernels (threshold 0) deduplicate them exactly.
+// run descriptors, expanded once into (k-mer, input) records bucketed by
+// k-mer hash, and deduplicated per bucket in shared memory (zi_dedup).
 #include "api_internal.h"
 #include "mczi_common.cuh"
 #include "scan.cuh"
+
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
 
 #include <algorithm>
 #include <cstring>
@@ -143,11 +146,13 @@ __global__ void k_zi_bucket_count(const uint32_t* __restrict__ key, uint64_t n, 
 }
 
 __global__ void k_zi_bucket_fill(const uint64_t* __restrict__ desc, const uint32_t* __restrict__ key, uint64_t n,
-                                 MphfView v, uint64_t n_keys, uint32_t* cursor, uint64_t* sk) {
+                                 MphfView v, uint64_t n_keys, uint32_t* cursor, uint64_t* sk,
+                                 uint32_t* __restrict__ bucket_key) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t b = mphf_lookup(v, key[i]);
     if (b >= n_keys) continue;
     sk[atomicAdd(&cursor[b], 1u)] = desc[i];
+    bucket_key[b] = key[i];  // every superkmer of a bucket carries the same key
   }
 }
 
@@ -165,11 +170,24 @@ struct ProbeArgs {
   uint64_t* out_desc;
   uint32_t* out_key;
   unsigned long long* n_runs;
+  unsigned long long* n_absent_windows;
   uint64_t cap;
+  const uint32_t* bucket_key;
 };
 
+// one pair of atomics per group of lanes emitting together (the run counter
+// and the absent-window total are single addresses every thread hits)
 __device__ __forceinline__ void emit_run(const ProbeArgs& a, uint64_t start, uint32_t len, uint32_t key) {
-  const unsigned long long idx = atomicAdd(a.n_runs, 1ull);
+  namespace cg = cooperative_groups;
+  cg::coalesced_group g = cg::coalesced_threads();
+  const unsigned long long w = cg::reduce(g, (unsigned long long)len, cg::plus<unsigned long long>());
+  unsigned long long base = 0;
+  if (g.thread_rank() == 0) {
+    base = atomicAdd(a.n_runs, (unsigned long long)g.size());
+    atomicAdd(a.n_absent_windows, w);
+  }
+  base = g.shfl(base, 0);
+  const unsigned long long idx = base + g.thread_rank();
   if (idx < a.cap) {
     a.out_desc[idx] = (start << 24) | (uint64_t)(len - 1);
     a.out_key[idx] = key;
@@ -198,7 +216,9 @@ __global__ void __launch_bounds__(ZI_THREADS) k_zi_probe(ProbeArgs a) {
     const uint32_t key = a.qkey[i];
     const uint64_t b = mphf_lookup(a.v, key);
     uint32_t blo = 0, bhi = 0;
-    if (b < a.n_keys) { blo = a.bucket_off[b]; bhi = a.bucket_off[b + 1]; }
+    // a minimizer the index does not hold maps to an arbitrary bucket: its
+    // k-mers are all absent (equal canonical k-mers have equal minimizers)
+    if (b < a.n_keys && a.bucket_key[b] == key) { blo = a.bucket_off[b]; bhi = a.bucket_off[b + 1]; }
     int64_t run = -1;
     for (uint32_t c0 = 0; c0 < nw; c0 += Q_CHUNK) {
       const uint32_t cn = min((uint32_t)Q_CHUNK, nw - c0);
@@ -247,6 +267,311 @@ __global__ void __launch_bounds__(ZI_THREADS) k_zi_probe(ProbeArgs a) {
   }
 }
 
+
+// ---- dedup of the absent windows
+// Absent k-mers are mostly distinct (sequencing errors, foreign reads), and
+// their runs are short and scattered, so regenerating them per counting round
+// would pay a scattered packed-stream gather per run and per round.  Instead:
+//   1. expand: each absent run is rolled once, in emission order (close to
+//      stream order), into flat (k-mer, input) records scattered into 2^b1
+//      buckets (b1 <= 8) by the top bits of the k-mer hash (histogram, scan
+//      and per-CTA shared-memory cursors).  At most 256 x 304 destinations
+//      are open at a time, so L2 combines the scattered writes;
+//   2. split: when more buckets are needed, one CTA per bucket splits it by
+//      the next b2 <= 8 bits the same way;
+//   3. dedup: a persistent CTA takes one final bucket at a time (sized to
+//      about half its shared-memory table) and deduplicates it there, in
+//      sub-rounds over the next 20 hash bits when the bucket is larger; a
+//      sub-round that overflows is redone as two (no estimate can change the
+//      result).
+constexpr int DD_MAX_BITS1 = 8;
+constexpr int DD_NB1 = 1 << DD_MAX_BITS1;
+constexpr int DD_CTAS = 304;
+constexpr int DD_THREADS = 512;
+constexpr int DDK_THREADS = 1024;
+constexpr uint32_t DD_PROBE_LIMIT = 256;
+
+struct ExpandArgs {
+  const uint64_t* runs;        // start << 24 | (windows - 1)
+  uint64_t n_runs;
+  const uint32_t* packed;
+  const uint64_t* input_base;  // n_inputs + 1 first bases
+  int n_inputs;
+  int with_ids;                // per-input results: record each window's input
+  int k;
+  int bits1;                   // level-1 bucket bits (0 .. 8)
+  uint32_t* hist;              // [2^bits1][DD_CTAS]
+  const uint32_t* pre;         // exclusive scan of hist (scatter pass)
+  void* keys_out;
+  uint16_t* ids_out;
+};
+
+// hash bits [64 - hi - n, 64 - hi): a digit below the top `hi` bits
+__device__ __forceinline__ uint32_t dd_digit(uint64_t h, int hi, int n) {
+  return n == 0 ? 0u : (uint32_t)(h >> (64 - hi - n)) & ((1u << n) - 1u);
+}
+
+template <class K, class R, bool SCATTER>
+__global__ void __launch_bounds__(DD_THREADS) k_zi_expand(ExpandArgs a) {
+  __shared__ uint32_t c[DD_NB1];
+  const int nb = 1 << a.bits1;
+  for (int i = threadIdx.x; i < nb; i += DD_THREADS) c[i] = SCATTER ? a.pre[(uint64_t)i * DD_CTAS + blockIdx.x] : 0u;
+  __syncthreads();
+  const uint64_t per = (a.n_runs + DD_CTAS - 1) / DD_CTAS;
+  uint64_t lo = per * blockIdx.x, hi = lo + per;
+  if (hi > a.n_runs) hi = a.n_runs;
+  const int k = a.k;
+  // the input of the previous run, kept: consecutive runs of a slice mostly
+  // come from the same input
+  int cur = -1;
+  uint64_t cur_lo = 0, cur_hi = 0;
+  for (uint64_t i = lo + threadIdx.x; i < hi; i += DD_THREADS) {
+    const uint64_t d = a.runs[i];
+    const uint64_t s0 = d >> 24;
+    const uint32_t nw = (uint32_t)(d & 0xffffffu) + 1u;
+    uint16_t ds = 0;
+    if (SCATTER && a.with_ids) {  // input of the run: largest j with input_base[j] <= s0
+      if (cur < 0 || s0 < cur_lo || s0 >= cur_hi) {
+        int l2 = 0, h2 = a.n_inputs;
+        while (h2 - l2 > 1) { const int mid = (l2 + h2) >> 1; if (a.input_base[mid] <= s0) l2 = mid; else h2 = mid; }
+        cur = l2;
+        cur_lo = a.input_base[l2];
+        cur_hi = a.input_base[l2 + 1];
+      }
+      ds = (uint16_t)cur;
+    }
+    R r;
+    roll_set<K, R>(r, a.packed, s0, k);
+    uint64_t p = s0 + (uint64_t)k;
+    for (uint32_t u = 0; u < nw; u++) {
+      if (u > 0) { r.push(base_at(a.packed, p)); p++; }
+      const K key = r.canon();
+      const uint32_t b = dd_digit(key_hash(key), 0, a.bits1);
+      if (!SCATTER) {
+        atomicAdd(&c[b], 1u);
+      } else {
+        const uint32_t pos = atomicAdd(&c[b], 1u);
+        reinterpret_cast<K*>(a.keys_out)[pos] = key;
+        if (a.with_ids) a.ids_out[pos] = ds;
+      }
+    }
+  }
+  if (!SCATTER) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += DD_THREADS) a.hist[(uint64_t)i * DD_CTAS + blockIdx.x] = c[i];
+  }
+}
+
+// bucket offsets of level 1: off[b] = pre[b * DD_CTAS] (b <= 2^bits1)
+__global__ void k_zi_off1(const uint32_t* __restrict__ pre, int nb, uint32_t* __restrict__ off) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= nb; i += gridDim.x * blockDim.x) off[i] = pre[(uint64_t)i * DD_CTAS];
+}
+
+struct SplitArgs {
+  const void* keys_in;
+  const uint16_t* ids_in;
+  const uint32_t* off1;        // level-1 bucket b = [off1[b], off1[b + 1])
+  int bits1, bits2;
+  void* keys_out;
+  uint16_t* ids_out;
+  uint32_t* off2;              // final bucket b1 << bits2 | j, plus the total at the end
+};
+
+// one CTA per level-1 bucket: histogram by the next bits2 bits, scan, scatter
+template <class K>
+__global__ void __launch_bounds__(DDK_THREADS) k_zi_split(SplitArgs a) {
+  __shared__ uint32_t c[DD_NB1];
+  __shared__ uint32_t ws[32];
+  const int nb2 = 1 << a.bits2;
+  const uint32_t b1 = blockIdx.x;
+  const uint32_t lo = a.off1[b1], hi = a.off1[b1 + 1];
+  const K* kin = reinterpret_cast<const K*>(a.keys_in);
+  for (int i = threadIdx.x; i < nb2; i += blockDim.x) c[i] = 0;
+  __syncthreads();
+  for (uint32_t j = lo + threadIdx.x; j < hi; j += blockDim.x)
+    atomicAdd(&c[dd_digit(key_hash(kin[j]), a.bits1, a.bits2)], 1u);
+  __syncthreads();
+  if (threadIdx.x < 32) {  // exclusive scan of <= 256 bins by one warp
+    const int lane = threadIdx.x;
+    const int per = (nb2 + 31) / 32;
+    uint32_t sum = 0;
+    for (int q = 0; q < per; q++) { const int i = lane * per + q; if (i < nb2) sum += c[i]; }
+    uint32_t x = sum;
+    for (int o = 1; o < 32; o <<= 1) { const uint32_t y = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += y; }
+    uint32_t run = lo + x - sum;
+    for (int q = 0; q < per; q++) {
+      const int i = lane * per + q;
+      if (i < nb2) { const uint32_t v = c[i]; c[i] = run; a.off2[(uint64_t)b1 * nb2 + i] = run; run += v; }
+    }
+    ws[lane] = 0;
+  }
+  if (b1 == gridDim.x - 1 && threadIdx.x == 0) a.off2[(uint64_t)gridDim.x * nb2] = hi;
+  __syncthreads();
+  K* kout = reinterpret_cast<K*>(a.keys_out);
+  for (uint32_t j = lo + threadIdx.x; j < hi; j += blockDim.x) {
+    const K key = kin[j];
+    const uint32_t pos = atomicAdd(&c[dd_digit(key_hash(key), a.bits1, a.bits2)], 1u);
+    kout[pos] = key;
+    if (a.ids_in) a.ids_out[pos] = a.ids_in[j];
+  }
+}
+
+struct BucketDedupArgs {
+  const void* keys;
+  const uint16_t* ids;
+  const uint32_t* off;         // bucket b = records [off[b], off[b + 1])
+  uint32_t n_buckets;
+  int bits;                    // hash bits the buckets consumed
+  int W;                       // mask words per slot (0: union, no masks)
+  uint32_t slots;
+  unsigned int* work;
+  uint64_t* out_lo;
+  uint64_t* out_hi;
+  uint32_t* out_count;
+  unsigned long long* out_mask;
+  unsigned long long* n_out;
+  uint64_t cap;
+  uint32_t* status;
+};
+
+__device__ __forceinline__ bool dd_maybe_empty(K64 c) { return c.v == ~0ull; }
+__device__ __forceinline__ bool dd_maybe_empty(K128 c) { return c.lo == ~0ull || c.hi == ~0ull; }
+__device__ __forceinline__ K64 dd_cas(K64* p, K64 cmp, K64 val) {
+  return K64{(uint64_t)atomicCAS(reinterpret_cast<unsigned long long*>(p), (unsigned long long)cmp.v,
+                                 (unsigned long long)val.v)};
+}
+__device__ __forceinline__ K128 dd_cas(K128* p, K128 cmp, K128 val) { return atomicCAS(p, cmp, val); }
+
+// exclusive block scan of one u32 per thread; ws holds 32 words
+__device__ __forceinline__ uint32_t dd_block_scan(uint32_t v, uint32_t* total, uint32_t* ws) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t t = lane < nw ? ws[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    ws[lane] = t;
+  }
+  __syncthreads();
+  const uint32_t r = x - v + (wid ? ws[wid - 1] : 0u);
+  *total = ws[nw - 1];
+  __syncthreads();
+  return r;
+}
+
+template <class K>
+__global__ void __launch_bounds__(DDK_THREADS) k_zi_bucket_dedup(BucketDedupArgs a) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const uint32_t S = a.slots;
+  const int W = a.W;
+  K* tk = reinterpret_cast<K*>(smem);
+  unsigned long long* tm = reinterpret_cast<unsigned long long*>(smem + (((size_t)S * sizeof(K) + 15) & ~(size_t)15));
+  __shared__ uint32_t s_b, s_over;
+  __shared__ uint32_t ws[32];
+  __shared__ unsigned long long s_base;
+  const K EMPTY = key_empty<K>();
+  const K* keys = reinterpret_cast<const K*>(a.keys);
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) s_b = atomicAdd(a.work, 1u);
+    __syncthreads();
+    const uint32_t b = s_b;
+    if (b >= a.n_buckets) break;
+    const uint32_t lo = a.off[b], hi = a.off[b + 1];
+    if (hi <= lo) continue;
+    // sub-rounds: at most half a table of records each (distinct <= records)
+    uint32_t r = (hi - lo + S / 2 - 1) / (S / 2);
+    uint32_t i = 0;
+    while (i < r) {
+      const uint32_t sub_lo = (uint32_t)(((uint64_t)i << 20) / r), sub_hi = (uint32_t)(((uint64_t)(i + 1) << 20) / r);
+      for (uint32_t s = tid; s < S; s += nth) {
+        tk[s] = EMPTY;
+        for (int q = 0; q < W; q++) tm[(size_t)s * W + q] = 0ull;
+      }
+      if (tid == 0) s_over = 0;
+      __syncthreads();
+      for (uint32_t j = lo + tid; j < hi; j += nth) {
+        if (*(volatile uint32_t*)&s_over) break;
+        const K key = keys[j];
+        const uint64_t h = key_hash(key);
+        const uint32_t sub = dd_digit(h, a.bits, 20);
+        if (sub < sub_lo || sub >= sub_hi) continue;
+        uint32_t slot = (uint32_t)(((h & 0xffffffffull) * (uint64_t)S) >> 32);
+        bool done = false;
+        for (uint32_t probe = 0; probe < DD_PROBE_LIMIT; probe++) {
+          K cur = tk[slot];
+          if (dd_maybe_empty(cur)) {
+            const K prev = dd_cas(&tk[slot], EMPTY, key);
+            if (key_eq(prev, EMPTY)) { done = true; break; }
+            cur = prev;
+          }
+          if (key_eq(cur, key)) { done = true; break; }
+          slot = (slot + 1 == S) ? 0u : slot + 1;
+        }
+        if (!done) { s_over = 1; break; }
+        if (W) {
+          const uint32_t ds = a.ids[j];
+          atomicOr(&tm[(size_t)slot * W + (ds >> 6)], 1ull << (ds & 63));
+        }
+      }
+      __syncthreads();
+      if (s_over) {
+        // this sub-range becomes two: sub-round i of r is sub-rounds 2i, 2i+1 of 2r
+        if (r >= (1u << 20)) {
+          if (tid == 0) set_status(a.status, ST_TABLE_STUCK);
+          i = r;
+        } else {
+          r *= 2;
+          i *= 2;
+        }
+        continue;
+      }
+      // emit: one global atomic per sub-round
+      uint32_t mine = 0;
+      for (uint32_t s = tid; s < S; s += nth) mine += key_eq(tk[s], EMPTY) ? 0u : 1u;
+      uint32_t tot;
+      const uint32_t off = dd_block_scan(mine, &tot, ws);
+      if (tid == 0) s_base = atomicAdd(a.n_out, (unsigned long long)tot);
+      __syncthreads();
+      unsigned long long o = s_base + off;
+      for (uint32_t s = tid; s < S; s += nth) {
+        const K key = tk[s];
+        if (key_eq(key, EMPTY)) continue;
+        if (o < a.cap) {
+          uint32_t c = 1;
+          if (W) {
+            c = 0;
+            for (int q = 0; q < W; q++) {
+              const unsigned long long m = tm[(size_t)s * W + q];
+              a.out_mask[o * (uint64_t)W + q] = m;
+              c += __popcll(m);
+            }
+          }
+          if constexpr (sizeof(K) == 8) {
+            a.out_lo[o] = reinterpret_cast<const K64&>(key).v;
+          } else {
+            a.out_lo[o] = reinterpret_cast<const K128&>(key).lo;
+            a.out_hi[o] = reinterpret_cast<const K128&>(key).hi;
+          }
+          a.out_count[o] = c;
+        } else {
+          set_status(a.status, ST_OUT_OVERFLOW);
+        }
+        o++;
+      }
+      i++;
+    }
+  }
+}
 
 // ---- per-input split of a batch result (records x masks -> per-input lists)
 constexpr int SPLIT_CHUNK = 4096;
@@ -429,6 +754,7 @@ int32_t zi_build(mczi_ctx* ctx, const uint8_t* fasta, uint64_t len, uint32_t k, 
   // buckets: CSR from MPHF index to superkmers
   const MphfView v = view_of(z);
   CKA(z.bucket_off, (n_keys + 2) * 4);
+  CKA(z.bucket_key, std::max<uint64_t>(n_keys, 1) * 4);
   CKA(z.sk, std::max<uint64_t>(n_desc, 1) * 8);
   uint32_t* cnt = ctx->zi_tmp1.as<uint32_t>();  // reuse: n_keys + 1 <= 2 * n_desc words
   CKA(ctx->zi_tmp1, std::max<uint64_t>((n_keys + 2) * 4 * 2 + (n_keys / SCAN_CHUNK + 2) * 4, 16));
@@ -442,7 +768,8 @@ int32_t zi_build(mczi_ctx* ctx, const uint8_t* fasta, uint64_t len, uint32_t k, 
     exclusive_scan<uint32_t, SumU32>(cnt, z.bucket_off.as<uint32_t>(), n_keys, cursor + n_keys + 1, s);
     CK(cudaMemcpyAsync(cursor, z.bucket_off.p, (n_keys + 1) * 4, cudaMemcpyDeviceToDevice, s));
     k_zi_bucket_fill<<<grid_for(ctx, n_desc), ZI_THREADS, 0, s>>>(ctx->desc.as<uint64_t>(), d_key, n_desc, v, n_keys,
-                                                                  cursor, z.sk.as<uint64_t>());
+                                                                  cursor, z.sk.as<uint64_t>(),
+                                                                  z.bucket_key.as<uint32_t>());
   } else {
     CK(cudaMemsetAsync(z.bucket_off.p, 0, 8, s));
   }
@@ -460,6 +787,132 @@ int32_t zi_build(mczi_ctx* ctx, const uint8_t* fasta, uint64_t len, uint32_t k, 
 }
 
 // absent k-mers of the staged queries; per_input: records carry input masks
+// Absent runs (ctx->desc) -> deduplicated records (+ per-input masks).
+// Records come out in bucket order; ZI's results are sets.
+int32_t zi_dedup(mczi_ctx* ctx, Pipe& p, bool per_input, uint64_t absent_w, uint64_t* n_out) {
+  ZiIndex& z = ctx->zi;
+  cudaStream_t s = ctx->stream;
+  uint64_t* sc = ctx->scalars.as<uint64_t>();
+  const bool wide = z.k > 32;
+  const int W = per_input ? (ctx->n_inputs + 63) / 64 : 0;
+  if (absent_w >= 0xffffffffull) return fail(ctx, MCZI_ERR_TOO_LARGE, "more than 2^32 absent k-mers in one query");
+  if (per_input && ctx->n_inputs > 65535) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "more than 65535 inputs in one batch");
+  CK(cudaEventRecord(ctx->ev[2], s));
+  const size_t keyb = wide ? 16 : 8;
+  // dedup table: one CTA of 1024 threads per SM with the largest table that fits
+  const size_t slotb = keyb + 8 * (size_t)W;
+  cudaFuncAttributes fa{};
+  if (wide) cudaFuncGetAttributes(&fa, k_zi_bucket_dedup<K128>);
+  else cudaFuncGetAttributes(&fa, k_zi_bucket_dedup<K64>);
+  const size_t budget = std::min((size_t)ctx->smem_optin, (size_t)(227 * 1024)) - fa.sharedSizeBytes - 64;
+  const uint32_t slots = (uint32_t)std::min<size_t>((budget - 16) / slotb, 1u << 20);
+  if (slots < 2048) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "too many inputs for the ZI dedup table");
+  const size_t smem = (((size_t)slots * keyb + 15) & ~(size_t)15) + (size_t)slots * 8 * W;
+  // final buckets of about half a table each, in one or two levels of <= 8 bits
+  int bits = 0;
+  while (bits < 16 && ((uint64_t)slots / 2) << bits < absent_w) bits++;
+  const int bits1 = std::min(bits, DD_MAX_BITS1), bits2 = bits - bits1;
+  const uint32_t nb1 = 1u << bits1, nbf = 1u << bits;
+  const uint64_t nh = (uint64_t)nb1 * DD_CTAS;
+  const uint64_t ntmp = nh / SCAN_CHUNK + 2;
+  const uint64_t cap = std::max<uint64_t>(absent_w, 1);
+  CKA(ctx->zi_tmp0, (2 * nh + 2 + ntmp + (nb1 + 1) + (nbf + 1)) * 4);
+  CKA(ctx->zi_tmp1, cap * keyb);
+  if (W) CKA(ctx->zi_tmp2, cap * 2);
+  if (bits2) {
+    CKA(ctx->zi_tmp3, cap * keyb);
+    if (W) CKA(ctx->zi_tmp4, cap * 2);
+  }
+  uint32_t* hist = ctx->zi_tmp0.as<uint32_t>();
+  uint32_t* pre = hist + nh + 1;
+  uint32_t* tmp = pre + nh + 1;
+  uint32_t* off1 = tmp + ntmp;
+  uint32_t* offf = off1 + nb1 + 1;
+  CKA(ctx->out_lo, cap * 8);
+  if (wide) CKA(ctx->out_hi, cap * 8);
+  CKA(ctx->out_cnt, cap * 4);
+  if (W) CKA(ctx->out_mask, cap * 8 * (uint64_t)W);
+  CK(cudaMemsetAsync(sc + SC_NOUT, 0, 8, s));
+  CK(cudaMemsetAsync(sc + SC_STATUS, 0, 8, s));
+  CK(cudaMemsetAsync(sc + SC_WORK, 0, 8, s));
+  ExpandArgs ea;
+  ea.runs = ctx->desc.as<uint64_t>();
+  ea.n_runs = p.n_desc;
+  ea.packed = ctx->packed.as<uint32_t>();
+  ea.input_base = ctx->input_base.as<uint64_t>();
+  ea.n_inputs = ctx->n_inputs;
+  ea.with_ids = W ? 1 : 0;
+  ea.k = z.k;
+  ea.bits1 = bits1;
+  ea.hist = hist;
+  ea.pre = pre;
+  ea.keys_out = ctx->zi_tmp1.p;
+  ea.ids_out = W ? ctx->zi_tmp2.as<uint16_t>() : nullptr;
+  if (wide) k_zi_expand<K128, Roll128, false><<<DD_CTAS, DD_THREADS, 0, s>>>(ea);
+  else k_zi_expand<K64, Roll64, false><<<DD_CTAS, DD_THREADS, 0, s>>>(ea);
+  exclusive_scan<uint32_t, SumU32>(hist, pre, nh, tmp, s);
+  if (wide) k_zi_expand<K128, Roll128, true><<<DD_CTAS, DD_THREADS, 0, s>>>(ea);
+  else k_zi_expand<K64, Roll64, true><<<DD_CTAS, DD_THREADS, 0, s>>>(ea);
+  k_zi_off1<<<1, 256, 0, s>>>(pre, (int)nb1, bits2 ? off1 : offf);
+  const void* dkeys = ctx->zi_tmp1.p;
+  const uint16_t* dids = W ? ctx->zi_tmp2.as<uint16_t>() : nullptr;
+  p.launches += 6;
+  if (bits2) {
+    SplitArgs sa;
+    sa.keys_in = ctx->zi_tmp1.p;
+    sa.ids_in = dids;
+    sa.off1 = off1;
+    sa.bits1 = bits1;
+    sa.bits2 = bits2;
+    sa.keys_out = ctx->zi_tmp3.p;
+    sa.ids_out = W ? ctx->zi_tmp4.as<uint16_t>() : nullptr;
+    sa.off2 = offf;
+    if (wide) k_zi_split<K128><<<nb1, DDK_THREADS, 0, s>>>(sa);
+    else k_zi_split<K64><<<nb1, DDK_THREADS, 0, s>>>(sa);
+    dkeys = ctx->zi_tmp3.p;
+    dids = W ? ctx->zi_tmp4.as<uint16_t>() : nullptr;
+    p.launches += 1;
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->ev[3], s));
+  BucketDedupArgs da;
+  da.keys = dkeys;
+  da.ids = dids;
+  da.off = offf;
+  da.n_buckets = nbf;
+  da.bits = bits;
+  da.W = W;
+  da.slots = slots;
+  da.work = reinterpret_cast<unsigned int*>(sc + SC_WORK);
+  da.out_lo = ctx->out_lo.as<uint64_t>();
+  da.out_hi = wide ? ctx->out_hi.as<uint64_t>() : nullptr;
+  da.out_count = ctx->out_cnt.as<uint32_t>();
+  da.out_mask = W ? ctx->out_mask.as<unsigned long long>() : nullptr;
+  da.n_out = reinterpret_cast<unsigned long long*>(sc + SC_NOUT);
+  da.cap = cap;
+  da.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
+  const unsigned grid = (unsigned)std::min<uint32_t>(nbf, (uint32_t)ctx->sm_count);
+  if (wide) {
+    cudaFuncSetAttribute(k_zi_bucket_dedup<K128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_zi_bucket_dedup<K128><<<grid, DDK_THREADS, smem, s>>>(da);
+  } else {
+    cudaFuncSetAttribute(k_zi_bucket_dedup<K64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_zi_bucket_dedup<K64><<<grid, DDK_THREADS, smem, s>>>(da);
+  }
+  p.launches += 1;
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->ev[4], s));
+  uint64_t h[2];
+  CK(cudaMemcpyAsync(h, sc + SC_NOUT, 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(h + 1, sc + SC_STATUS, 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (h[1] & (ST_TABLE_STUCK | ST_OUT_OVERFLOW)) return fail(ctx, MCZI_ERR_DEVICE, "ZI dedup could not place every k-mer");
+  ctx->mask_words = W;
+  ctx->cap_out = std::max(ctx->cap_out, cap);
+  *n_out = h[0];
+  return MCZI_OK;
+}
+
 int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, uint64_t* n_out) {
   ZiIndex& z = ctx->zi;
   if (!z.built) return fail(ctx, MCZI_ERR_STATE, "no ZI index: call mczi_zi_build first");
@@ -477,7 +930,7 @@ int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, u
   uint64_t* sc = ctx->scalars.as<uint64_t>();
   // probe: absent-window runs into (desc2, key2)
   uint64_t cap = 2 * p.n_desc + 1024;
-  uint64_t n_runs = 0;
+  uint64_t n_runs = 0, absent_w = 0;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -489,6 +942,7 @@ int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, u
     CKA(ctx->desc2, cap * 8);
     CKA(ctx->key2, cap * 4);
     CK(cudaMemsetAsync(sc + SC_NRUNS, 0, 8, s));
+    CK(cudaMemsetAsync(sc + SC_NABSW, 0, 8, s));
     ProbeArgs pa;
     pa.qdesc = ctx->desc.as<uint64_t>();
     pa.qkey = ctx->key.as<uint32_t>();
@@ -497,6 +951,8 @@ int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, u
     pa.ipacked = z.packed.as<uint32_t>();
     pa.sk = z.sk.as<uint64_t>();
     pa.bucket_off = z.bucket_off.as<uint32_t>();
+    pa.bucket_key = z.bucket_key.as<uint32_t>();
+    pa.n_absent_windows = reinterpret_cast<unsigned long long*>(sc + SC_NABSW);
     pa.n_keys = z.n_keys;
     pa.v = view_of(z);
     pa.k = z.k;
@@ -510,6 +966,7 @@ int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, u
     p.launches += 1;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&n_runs, sc + SC_NRUNS, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&absent_w, sc + SC_NABSW, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (n_runs <= cap) break;
     cap = n_runs + 1024;
@@ -525,15 +982,15 @@ int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, u
   CK(cudaEventElapsedTime(&probe_ms, e0, e1));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if ((rc = pipe_partition(ctx, p))) return rc;
   const int mode = per_input ? MCZI_MODE_PRESENCE : MCZI_MODE_ABUNDANCE;
   uint64_t out = 0;
-  if ((rc = pipe_count(ctx, p, z.k, 0, mode, per_input, &out))) return rc;
+  if ((rc = zi_dedup(ctx, p, per_input, absent_w, &out))) return rc;
   if ((rc = pipe_finish(ctx, p, mode, z.k, z.m, 0, out))) return rc;
-  // phases for ZI: [0] pack, [1] scan, [2] partition, [3] dedup count, [4] probe
+  // phases for ZI: [0] pack, [1] scan, [2] expand into buckets, [3] bucket dedup, [4] probe
   ctx->phase_ms[1] -= probe_ms;
   ctx->phase_ms[4] = probe_ms;
   ctx->stats[1] = n_runs;
+  ctx->stats[6] = absent_w;
   if (n_out) *n_out = out;
   (void)p.n_desc_total;
   return MCZI_OK;
