@@ -132,8 +132,13 @@ __global__ void k_count(CountArgs a) {
   off = (off + 15) & ~(size_t)15;
   const uint32_t fwords = a.filter_words;  // 0: single-pass rounds
   const bool filtered = fwords > 0;
-  const uint64_t fbits = (uint64_t)fwords * 32;
+  // filtered rounds: the seen-once bitmap (7/8 of the words) and a coarser
+  // claimed-key bitmap (1/8) that lets pass 2 skip the table for keys pass 1
+  // never stored (both indexed by the same 32 hash bits)
+  const uint32_t cwords = filtered ? ((fwords / 8) & ~31u) : 0u;
+  const uint64_t fbits = (uint64_t)(fwords - cwords) * 32, cbits = (uint64_t)cwords * 32;
   uint32_t* bmap = reinterpret_cast<uint32_t*>(smem + off);
+  uint32_t* cmap = bmap + (fwords - cwords);
   off += (size_t)fwords * 4;
   off = (off + 15) & ~(size_t)15;
   uint32_t* occ = reinterpret_cast<uint32_t*>(smem + off);   // NP2 + 1, becomes occupancy prefix
@@ -397,7 +402,13 @@ __global__ void k_count(CountArgs a) {
                   if (hk < rr.hlo || hk > rr.hhi) continue;
                 }
                 uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
+                // bitmap positions from hash bits 20..51 (the slot uses the low
+                // 32 bits, range splits bits 32..63)
+                const uint64_t hb = (hv >> 20) & 0xffffffffull;
                 if (ph == 2) {
+                  // a key pass 1 never stored has its claimed bit clear
+                  const uint32_t cp = (uint32_t)((hb * cbits) >> 32);
+                  if (!((cmap[cp >> 5] >> (cp & 31)) & 1u)) continue;
                   // keys are final during pass 2: plain loads, stop at EMPTY
                   for (uint32_t probe = 0; probe < PROBE_LIMIT; probe++) {
                     const K cur = keys[s];
@@ -412,11 +423,11 @@ __global__ void k_count(CountArgs a) {
                   continue;
                 }
                 if (ph == 1) {
-                  // bitmap position from hash bits 20..51 (the slot uses the low
-                  // 32 bits, range splits bits 32..63)
-                  const uint32_t bp = (uint32_t)((((hv >> 20) & 0xffffffffull) * (uint64_t)fbits) >> 32);
+                  const uint32_t bp = (uint32_t)((hb * fbits) >> 32);
                   const uint32_t bit = 1u << (bp & 31);
                   if (!(atomicOr(&bmap[bp >> 5], bit) & bit)) continue;  // first sight: not stored
+                  const uint32_t cp = (uint32_t)((hb * cbits) >> 32);
+                  atomicOr(&cmap[cp >> 5], 1u << (cp & 31));  // stored (below) or already stored
                 }
                 bool done = false;
                 // Probe with plain loads; CAS only on a slot that looks empty.
