@@ -198,11 +198,26 @@ def run_ours(args):
             phase_sum[i] += t
     e1.record(stream)
     barrier()
-    clk = clocks.stop()
-    dev_ms = e0.elapsed_time(e1) / args.steps
-    dev_ms = max_over_ranks(dev_ms)
+    dev_ms_plain = max_over_ranks(e0.elapsed_time(e1) / args.steps)
     stats = ctx.run_stats()
     nb = stats[0]
+    # the same steps replayed from one captured CUDA graph (the first replay
+    # request captures; results are identical, see tests)
+    graph_ms = None
+    if not args.no_graph:
+        ctx.set_graph_replay(True)
+        for _ in range(args.warmup):
+            ctx.count_staged(cfg)
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            ctx.count_staged(cfg)
+        e1.record(stream)
+        barrier()
+        graph_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+        ctx.set_graph_replay(False)
+    clk = clocks.stop()
+    dev_ms = graph_ms if graph_ms else dev_ms_plain
     value = nb * ws / (dev_ms * 1e-3) / 1e9
 
     # ---- end to end through the C ABI: H2D from pinned + count + D2H of every
@@ -259,6 +274,8 @@ def run_ours(args):
                 "staging_ms": round(stage_ms, 3), "staging_gbs": round(nbytes / (stage_ms * 1e-3) / 1e9, 1)},
         "gpu_launches": int(stats[8]) * args.steps,
         "tuning": tuning_report,
+        "device_ms": {"launched": round(dev_ms_plain, 3),
+                      "graph_replay": round(graph_ms, 3) if graph_ms else None},
         "phases_ms": {nm: round(v, 3) for nm, v in avg.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
@@ -315,6 +332,81 @@ def run_reference(args):
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cb["cores"], "kind": "port",
                              "sample": cb["sample"] + "; the Rust reference cannot be built here (no cargo/rustc)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_mc_fof(args):
+    """MC fof dataset presence: 64 datasets drawn from one seeded 20 Mbp genome
+    (0.1 % private SNPs each, 150 bp reads at coverage uniform in [5x, 30x],
+    0.5 % errors), k=31 m=21 x=5 (kept if present in > 5 datasets); all
+    datasets in one set of launches, in key-range passes when the superkmers
+    exceed one pass's buffers.  Inputs sit in one pinned host buffer."""
+    import torch
+    from mczi_gb300 import build, gen
+    from mczi_gb300.mc import Context, CounterConfig
+    build.build_all()
+    t0 = time.perf_counter()
+    ds = gen.c3_datasets(64, genome_len=int(20_000_000 * args.scale))
+    gen_s = time.perf_counter() - t0
+    nbytes = int(sum(d.size for d in ds))
+    # the datasets in one pinned host buffer (as a loader would deliver them)
+    pinned = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    view, o, inputs = pinned.numpy(), 0, []
+    for d in ds:
+        view[o:o + d.size] = d
+        inputs.append((pinned.data_ptr() + o, int(d.size)))
+        o += d.size
+    del ds
+    cfg = CounterConfig(31, 21, 5)
+    stream = torch.cuda.current_stream()
+    ctx = Context(0)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.stage(inputs)
+    for _ in range(args.warmup):
+        n = ctx.count_staged(cfg, 1)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    phase_sum = [0.0] * 5
+    e0.record(stream)
+    for _ in range(args.steps):
+        n = ctx.count_staged(cfg, 1)
+        phase_sum = [a + b for a, b in zip(phase_sum, ctx.phase_times())]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dev_ms = e0.elapsed_time(e1) / args.steps
+    stats = ctx.run_stats()
+    nb = stats[0]
+    # end to end: staging from pinned host memory + count + records into
+    # pinned buffers
+    import numpy as np
+    outs = [torch.empty(max(1, n), dtype=torch.int64, pin_memory=True).numpy().view(np.uint64) for _ in range(2)]
+    ctx.count(inputs, cfg, 1)
+    ctx.records(n, sorted=False, out=(outs[0], None, outs[1]))
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        n2 = ctx.count(inputs, cfg, 1)
+        rec = ctx.records(n2, sorted=False, out=(outs[0], None, outs[1]))
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    assert n2 == n
+    line = {"metric": "MC Gbases/s", "value": round(nb / (dev_ms * 1e-3) / 1e9, 3), "unit": "Gbases/s",
+            "impl": "ours", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dev_ms, 3), "higher_is_better": True, "scaling": "weak",
+            "dtype": "u8/u64 (2-bit bases, 64-bit k-mers, 64-bit dataset masks)",
+            "data": "synthetic (seeded generator, no dataset)",
+            "config": {"workload": "mc_fof_64_datasets_k31", "k": 31, "m": 21, "x": 5, "mode": "presence",
+                       "datasets": 64, "genome_bp": int(20_000_000 * args.scale), "bases": nb,
+                       "text_bytes": nbytes, "superkmers": stats[1], "kept_records": n,
+                       "launches": stats[8], "generate_s": round(gen_s, 1)},
+            "phases_ms": {nm: round(v / args.steps, 3) for nm, v in
+                          zip(["pack", "scan", "partition", "count", "precount"], phase_sum)},
+            "e2e": {"value": round(nb / (e2e_ms * 1e-3) / 1e9, 3), "unit": "Gbases/s", "ms_per_step": round(e2e_ms, 3),
+                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": int(n) * 16,
+                    "host_memory": "pinned"},
+            "clocks": clk}
+    ctx.close()
     print(json.dumps(line), flush=True)
 
 
@@ -493,7 +585,8 @@ def main():
     ap.add_argument("--ref-sample-scale", type=float, default=0.004)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the untimed autotuning on a sample")
-    ap.add_argument("--workload", default="mc", choices=["mc", "zi", "zi-serve"])
+    ap.add_argument("--no-graph", action="store_true", help="skip the graph-replay timing")
+    ap.add_argument("--workload", default="mc", choices=["mc", "mc-fof", "zi", "zi-serve"])
     ap.add_argument("--zi-files", type=int, default=200)
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-workers", type=int, default=2)
@@ -504,6 +597,8 @@ def main():
         return run_zi(args)
     if args.workload == "zi-serve" and args.impl == "ours":
         return run_zi_serve(args)
+    if args.workload == "mc-fof" and args.impl == "ours":
+        return run_mc_fof(args)
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":

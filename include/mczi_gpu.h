@@ -168,8 +168,10 @@ int32_t mczi_set_minimizer_precount(mczi_ctx* ctx, int32_t enable);
  * while earlier segments are packed and scanned.  enable 0 stages everything
  * first; segment_bytes (a multiple of 8192) sets the segment size, 0 =
  * automatic (>= 32 MiB, about 16 segments).  Results are identical either way.
- * Default on.  Batches that need several key-range passes or the pre-count,
- * and graph replay, always stage first. */
+ * Default on.  Batches estimated (from their text length) to need more than
+ * two key-range passes, counts with the pre-count, and graph replay always
+ * stage first; a streamed batch that overflows one pass is recounted through
+ * the staged path. */
 int32_t mczi_set_streamed_staging(mczi_ctx* ctx, int32_t enable, uint64_t segment_bytes);
 
 /* Packer parity hook: after mczi_count/mczi_count_staged, copies the 2-bit

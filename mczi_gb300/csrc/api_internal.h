@@ -198,6 +198,7 @@ struct Pipe {
   uint64_t n_desc_total = 0;
   uint64_t pwords = 0;
   const uint64_t* d_nbases = nullptr;
+  uint64_t n_bases_host = 0;  // after the pack, when the host read it
   float pre_ms = 0.f;
   float ms[mczi::N_PHASES] = {0, 0, 0, 0, 0};  // accumulated over key-range passes
   // graph capture: enqueue only (no host synchronisation, no event records),
@@ -231,7 +232,7 @@ int32_t pipe_partition(mczi_ctx* ctx, Pipe& p);
 int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emit_masks, uint64_t* n_out,
                    bool append = false);
 // number of key-range passes a staged batch needs (descriptor memory, 32-bit counters)
-uint32_t key_range_passes(mczi_ctx* ctx, int k, int m);
+uint32_t key_range_passes(mczi_ctx* ctx, int k, int m, uint64_t bases);
 int32_t pipe_finish(mczi_ctx* ctx, Pipe& p, int mode, int k, int m, uint64_t x, uint64_t n_out);
 
 }  // namespace mczi

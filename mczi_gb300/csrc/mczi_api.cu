@@ -221,15 +221,21 @@ int32_t pipe_pack(mczi_ctx* ctx, Pipe& p) {
   return MCZI_OK;
 }
 
-uint32_t key_range_passes(mczi_ctx* ctx, int k, int m) {
+// Superkmers one pass may hold: the partition addresses them with 32-bit
+// positions.
+constexpr uint64_t PASS_MAX_DESC = 4000000000ull;
+
+uint32_t key_range_passes(mczi_ctx* ctx, int k, int m, uint64_t bases) {
   if (ctx->key_passes > 0) return (uint32_t)ctx->key_passes;
   const int w = k - m + 1;
-  const double est = (double)ctx->text_len * 2.0 / (double)(w + 1);  // expected superkmers
+  // expected superkmers: 2 / (w + 1) per base of a random sequence; before the
+  // pack only the text length is known (headers and line breaks included)
+  const double est = (double)(bases ? bases : ctx->text_len) * 2.0 / (double)(w + 1);
   size_t free_b = 0, total_b = 0;
   if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) { cudaGetLastError(); free_b = 8ull << 30; }
   // descriptors (12 B) + their pass-1 copy (8 B) + precount/partition slack
-  const double per_pass = std::min((double)(1u << 30) * 1.5, (double)free_b * 0.45 / 24.0);
-  uint32_t r = (uint32_t)std::ceil(est * 1.3 / per_pass);
+  const double per_pass = std::min((double)PASS_MAX_DESC, (double)free_b * 0.45 / 24.0);
+  uint32_t r = (uint32_t)std::ceil(est * (bases ? 1.1 : 1.3) / per_pass);
   return std::max(1u, std::min(r, 64u));
 }
 
@@ -237,12 +243,14 @@ int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m, uint32_t p1_lo, uint32_t
   cudaStream_t s = ctx->stream;
   uint64_t* sc = ctx->scalars.as<uint64_t>();
   const uint64_t text_len = ctx->text_len;
+  const uint64_t bases = p.n_bases_host ? p.n_bases_host : text_len;
   const int w = k - m + 1;
-  uint64_t desc_cap = text_len * 3 / (uint64_t)(w + 1) / passes + (1u << 20);
-  if (desc_cap > text_len + 1024) desc_cap = text_len + 1024;
+  uint64_t desc_cap = bases * 3 / (uint64_t)(w + 1) / passes + (1u << 20);
+  if (desc_cap > bases + 1024) desc_cap = bases + 1024;
+  if (desc_cap > PASS_MAX_DESC) desc_cap = PASS_MAX_DESC;
   if (p.capture) desc_cap = ctx->cap_desc;
   for (int attempt = 0; attempt < 3; attempt++) {
-    if (desc_cap >= 0xffffffffull) return fail(ctx, MCZI_ERR_OOM, "input batch too large: more than 2^32 superkmers");
+    if (desc_cap > PASS_MAX_DESC) return fail(ctx, MCZI_ERR_TOO_LARGE, "more superkmers than one key-range pass holds");
     CKA(ctx->desc, desc_cap * 8);
     CKA(ctx->key, desc_cap * 4);
     CK(cudaMemsetAsync(sc + SC_NDESC, 0, 8, s));
@@ -537,11 +545,14 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
   }
   Pipe p;
   std::memset(ctx->stats, 0, sizeof ctx->stats);
-  // inputs with more superkmers than one pass can hold are counted in passes
-  // over disjoint ranges of the partition key (disjoint sets of k-mers);
-  // decided before any launch (it queries free memory)
-  const uint32_t passes = key_range_passes(ctx, k, m);
   if ((rc = pipe_pack(ctx, p))) return rc;
+  // inputs with more superkmers than one pass can hold are counted in passes
+  // over disjoint ranges of the partition key (disjoint sets of k-mers),
+  // decided from the packed base count; a pass that still overflows doubles
+  // the number of passes
+  CK(cudaMemcpyAsync(&p.n_bases_host, p.d_nbases, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  uint32_t passes = key_range_passes(ctx, k, m, p.n_bases_host);
   uint64_t n_out = 0;
   for (uint32_t r = 0; r < passes; r++) {
     const uint32_t lo = (uint32_t)((uint64_t)NP1 * r / passes), hi = (uint32_t)((uint64_t)NP1 * (r + 1) / passes);
@@ -560,7 +571,18 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
       CK(cudaEventRecord(ctx->ev[0], ctx->stream));
       CK(cudaEventRecord(ctx->ev[1], ctx->stream));
     }
-    if ((rc = pipe_scan(ctx, p, k, m, lo, hi, passes))) return rc;
+    if ((rc = pipe_scan(ctx, p, k, m, lo, hi, passes))) {
+      if (rc != MCZI_ERR_TOO_LARGE || passes >= 64 || ctx->key_passes > 0) return rc;
+      passes = std::min(64u, passes * 2);  // start over with narrower key ranges
+      r = (uint32_t)-1;
+      n_out = 0;
+      p.n_desc_total = 0;
+      p.pre_ms = 0.f;
+      for (int i = 0; i < N_PHASES; i++) p.ms[i] = 0.f;
+      CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+      CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+      continue;
+    }
     if (ctx->precount && (rc = pipe_precount(ctx, p, mode, cfg->threshold))) return rc;
     if ((rc = pipe_partition(ctx, p))) return rc;
     if ((rc = pipe_count(ctx, p, k, cfg->threshold, mode, false, &n_out, r > 0))) return rc;
@@ -587,10 +609,12 @@ int32_t run_count_streamed(mczi_ctx* ctx, const mczi_counter_config* cfg, int mo
   if ((rc = stage_layout(ctx, pl, n))) return rc;
   ctx->mask_words = 0;
   const int k = (int)cfg->k, m = (int)cfg->minimizer;
-  const uint32_t passes = key_range_passes(ctx, k, m);
+  const uint32_t passes = key_range_passes(ctx, k, m, 0);
   // segments of >= 32 MiB of text, about 16 per batch
   const uint64_t seg_min = ctx->stream_seg_tiles > 0 ? ctx->stream_seg_tiles : 4096;
-  const bool plain = passes > 1 || ctx->precount || !ctx->streamed || pl.n_tiles < 2 * seg_min ||
+  // the text-length estimate over-counts bases (headers, line breaks): up to
+  // two estimated passes are tried as one, with the plain path as fallback
+  const bool plain = passes > 2 || ctx->precount || !ctx->streamed || pl.n_tiles < 2 * seg_min ||
                      (mode == MCZI_MODE_PRESENCE && cfg->threshold >= (uint64_t)n);
   if (plain) {
     if ((rc = copy_text_range(ctx, inputs, n, pl, 0, pl.text_len, ctx->stream))) return rc;
@@ -609,6 +633,7 @@ int32_t run_count_streamed(mczi_ctx* ctx, const mczi_counter_config* cfg, int mo
   const int w = k - m + 1;
   uint64_t desc_cap = pl.text_len * 3 / (uint64_t)(w + 1) + (1u << 20);
   if (desc_cap > pl.text_len + 1024) desc_cap = pl.text_len + 1024;
+  if (desc_cap > PASS_MAX_DESC) desc_cap = PASS_MAX_DESC;
   CKA(ctx->desc, desc_cap * 8);
   CKA(ctx->key, desc_cap * 4);
   CK(cudaMemsetAsync(sc + SC_NDESC, 0, 8, s));
@@ -667,7 +692,9 @@ int32_t run_count_streamed(mczi_ctx* ctx, const mczi_counter_config* cfg, int mo
   CK(cudaMemcpyAsync(h + 1, sc + SC_STATUS, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (h[1] & ST_DESC_OVERFLOW) {
-    if ((rc = pipe_scan(ctx, p, k, m, 0, NP1, 1))) return rc;  // rescans every tile with room to spare
+    // more superkmers than the streamed pass holds: the inputs are staged,
+    // so the plain path (which sizes its passes from the packed bases) redoes it
+    return run_count(ctx, cfg, mode, n_records);
   } else {
     p.n_desc = h[0];
     p.desc_cap = desc_cap;
@@ -769,7 +796,7 @@ int32_t run_count_graph(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode,
   if (!ctx->staged) return fail(ctx, MCZI_ERR_STATE, "no staged inputs");
   if (ctx->precount || (mode == MCZI_MODE_PRESENCE && cfg->threshold >= (uint64_t)ctx->n_inputs))
     return run_count(ctx, cfg, mode, n_records);
-  const uint32_t passes = key_range_passes(ctx, (int)cfg->k, (int)cfg->minimizer);
+  const uint32_t passes = key_range_passes(ctx, (int)cfg->k, (int)cfg->minimizer, 0);
   if (ctx->graph_exec && make_sig(ctx, cfg, mode, passes) == ctx->graph_sig) {
     cudaStream_t s = ctx->stream;
     CK(cudaEventRecord(ctx->ev_graph[0], s));
