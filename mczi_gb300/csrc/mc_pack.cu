@@ -87,22 +87,22 @@ __device__ __forceinline__ uint32_t thread_state(const uint8_t* sb, bool fastq, 
                                                  uint32_t tile_line4, int first) {
   __shared__ NlSum sh[SCAN_THREADS + 1];
   NlSum mine{-1, 0};
-  {
-    // newlines of this thread's 32 bytes, four at a time
-    const uint4 v0 = *reinterpret_cast<const uint4*>(sb + first);
-    const uint4 v1 = *reinterpret_cast<const uint4*>(sb + first + 16);
-    const uint32_t w[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
+  for (int q = 0; q < PACK_PER_THREAD / 16; q++) {
+    // newlines of this thread's bytes, four at a time
+    const uint4 v = *reinterpret_cast<const uint4*>(sb + first + 16 * q);
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
       const uint32_t z = zero_bytes(w[j] ^ 0x0a0a0a0au);
       if (z) {
         mine.nl += __popc(z);
-        mine.last = first + 4 * j + (31 - __clz(z)) / 8;
+        mine.last = first + 16 * q + 4 * j + (31 - __clz(z)) / 8;
       }
     }
   }
   NlSum tot;
-  NlSum pre = block_exclusive_scan<NlSum, NlOp>(mine, &tot, sh);
+  NlSum pre = block_exclusive_scan<NlSum, NlOp, PACK_THREADS>(mine, &tot, sh);
   if (fastq) return (tile_line4 + pre.nl) & 3u;
   if (pre.last >= 0) {
     const int ls = pre.last + 1;
@@ -258,21 +258,29 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_count(const uint8_t* __re
   const int first = threadIdx.x * PACK_PER_THREAD;
   uint32_t st = thread_state(sb, fastq, tst, tl4, first);
   BaseSum s{0, 0, 0, 0};
-  uint64_t codes;
-  const bool seq_line = fastq ? ((st & 3u) == 1u) : (st != HDR);
-  if (seq_line && acgt32(sb + first, &codes)) {
-    s.nb = PACK_PER_THREAD;  // 32 bases, no break
-  } else {
-    for (int i = 0; i < PACK_PER_THREAD; i++) {
-      uint32_t c = sb[first + i];
-      uint32_t r = fastq ? step_fastq(c, st) : step_fasta(c, st);
-      if (r < 4) { s.nb++; s.lb = 0; }
-      else if (r == 4) { if (s.nb == 0) s.fb = 1; s.lb = 1; }
+  // 32-byte chunks in order; an all-ACGT chunk on a sequence line leaves the
+  // line state as it is
+#pragma unroll
+  for (int h = 0; h < PACK_PER_THREAD / 32; h++) {
+    const int f = first + 32 * h;
+    BaseSum c{0, 0, 0, 0};
+    uint64_t codes;
+    const bool seq_line = fastq ? ((st & 3u) == 1u) : (st != HDR);
+    if (seq_line && acgt32(sb + f, &codes)) {
+      c.nb = 32;  // 32 bases, no break; a FASTA line that started here is now mid-sequence
+      if (!fastq) st = SEQ;
+    } else {
+      for (int i = 0; i < 32; i++) {
+        const uint32_t r = fastq ? step_fastq(sb[f + i], st) : step_fasta(sb[f + i], st);
+        if (r < 4) { c.nb++; c.lb = 0; }
+        else if (r == 4) { if (c.nb == 0) c.fb = 1; c.lb = 1; }
+      }
     }
+    s = BaseOp::combine(s, c);
   }
   // for nb == 0 lb means "any break"; for nb > 0 fb is a break before the first base
   BaseSum tot;
-  block_exclusive_scan<BaseSum, BaseOp>(s, &tot, shs);
+  block_exclusive_scan<BaseSum, BaseOp, PACK_THREADS>(s, &tot, shs);
   if (threadIdx.x == 0) out[tile] = tot;
 }
 
@@ -298,25 +306,37 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __re
   tile_line_state(text, tile_info, input_tile0, line_pre, tile, fastq, tst, tl4);
   __syncthreads();
   const int first = threadIdx.x * PACK_PER_THREAD;
+  constexpr int NCH = PACK_PER_THREAD / 32;
   const uint32_t st0 = thread_state(sb, fastq, tst, tl4, first);
-  // pass A: this thread's summary (all-ACGT chunks take the fast path)
+  // pass A: this thread's summary, 32-byte chunks in order (all-ACGT chunks
+  // on a sequence line take the fast path and leave the line state as it is)
   uint32_t st = st0;
   BaseSum s{0, 0, 0, 0};
-  uint64_t codes = 0;
-  const bool seq_line = fastq ? ((st & 3u) == 1u) : (st != HDR);
-  const bool fast = seq_line && acgt32(sb + first, &codes);
-  if (fast) {
-    s.nb = PACK_PER_THREAD;
-  } else {
-    for (int i = 0; i < PACK_PER_THREAD; i++) {
-      uint32_t r = fastq ? step_fastq(sb[first + i], st) : step_fasta(sb[first + i], st);
-      if (r < 4) { s.nb++; s.lb = 0; }
-      else if (r == 4) { if (s.nb == 0) s.fb = 1; s.lb = 1; }
+  uint64_t codes[NCH];
+  bool fast[NCH];
+#pragma unroll
+  for (int h = 0; h < NCH; h++) {
+    const int f = first + 32 * h;
+    BaseSum c{0, 0, 0, 0};
+    codes[h] = 0;
+    const bool seq_line = fastq ? ((st & 3u) == 1u) : (st != HDR);
+    fast[h] = seq_line && acgt32(sb + f, &codes[h]);
+    if (fast[h]) {
+      c.nb = 32;
+      if (!fastq) st = SEQ;  // 32 letters: a FASTA line that started here is now mid-sequence
+    } else {
+      for (int i = 0; i < 32; i++) {
+        const uint32_t r = fastq ? step_fastq(sb[f + i], st) : step_fasta(sb[f + i], st);
+        if (r < 4) { c.nb++; c.lb = 0; }
+        else if (r == 4) { if (c.nb == 0) c.fb = 1; c.lb = 1; }
+      }
     }
+    s = BaseOp::combine(s, c);
   }
   BaseSum tot;
   const BaseSum tile_pre = base_pre[tile];
-  BaseSum excl = BaseOp::combine(tile_pre, block_exclusive_scan<BaseSum, BaseOp>(s, &tot, shs));
+  BaseSum excl =
+      BaseOp::combine(tile_pre, block_exclusive_scan<BaseSum, BaseOp, PACK_THREADS>(s, &tot, shs));
   if (threadIdx.x == 0 && (tile_info[tile] & 1u)) input_base[tile_info[tile] >> 2] = tile_pre.nb;
   // pass B: write codes and start bits into the staging buffers
   const uint64_t tb = tile_pre.nb;        // first base of this tile
@@ -324,24 +344,31 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __re
   uint64_t p = excl.nb;
   uint32_t pending = (excl.nb == 0) ? 1u : excl.lb;
   st = st0;
-  if (fast) {
-    // 32 bases at p: spread the 64 code bits over (up to) three staging words
-    const uint64_t q = (p >> 4) - w0;
-    const uint32_t r2 = 2 * (uint32_t)(p & 15);
-    atomicOr(&spk[q], (uint32_t)(codes >> (32 + r2)));
-    atomicOr(&spk[q + 1], (uint32_t)(codes >> r2));
-    if (r2) atomicOr(&spk[q + 2], (uint32_t)(codes << (32 - r2)));
-    if (pending) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
-  } else {
-    for (int i = 0; i < PACK_PER_THREAD; i++) {
-      uint32_t r = fastq ? step_fastq(sb[first + i], st) : step_fasta(sb[first + i], st);
-      if (r < 4) {
-        atomicOr(&spk[(p >> 4) - w0], r << (30 - 2 * (uint32_t)(p & 15)));
-        if (pending) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
-        pending = 0;
-        p++;
-      } else if (r == 4) {
-        pending = 1;
+#pragma unroll
+  for (int h = 0; h < NCH; h++) {
+    const int f = first + 32 * h;
+    if (fast[h]) {
+      // 32 bases at p: spread the 64 code bits over (up to) three staging words
+      const uint64_t q = (p >> 4) - w0;
+      const uint32_t r2 = 2 * (uint32_t)(p & 15);
+      atomicOr(&spk[q], (uint32_t)(codes[h] >> (32 + r2)));
+      atomicOr(&spk[q + 1], (uint32_t)(codes[h] >> r2));
+      if (r2) atomicOr(&spk[q + 2], (uint32_t)(codes[h] << (32 - r2)));
+      if (pending) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
+      pending = 0;
+      p += 32;
+      if (!fastq) st = SEQ;
+    } else {
+      for (int i = 0; i < 32; i++) {
+        const uint32_t r = fastq ? step_fastq(sb[f + i], st) : step_fasta(sb[f + i], st);
+        if (r < 4) {
+          atomicOr(&spk[(p >> 4) - w0], r << (30 - 2 * (uint32_t)(p & 15)));
+          if (pending) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
+          pending = 0;
+          p++;
+        } else if (r == 4) {
+          pending = 1;
+        }
       }
     }
   }

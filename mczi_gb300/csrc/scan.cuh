@@ -30,12 +30,13 @@ __device__ __forceinline__ T shfl_up_T(const T& v, int d) {
 }
 
 // Exclusive block scan of one value per thread (warp shuffles, then the warp
-// totals); returns this thread's exclusive prefix and writes the block total
-// to *total (all threads).  sh needs SCAN_THREADS / 32 + 1 entries.
-template <class T, class Op>
+// totals) over a block of NT threads; returns this thread's exclusive prefix
+// and writes the block total to *total (all threads).  sh needs NT / 32 + 1
+// entries.
+template <class T, class Op, int NT = SCAN_THREADS>
 __device__ T block_exclusive_scan(T v, T* total, T* sh) {
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  constexpr int NW = SCAN_THREADS / 32;
+  constexpr int NW = NT / 32;
   T incl = v;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {

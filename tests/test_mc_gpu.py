@@ -378,3 +378,35 @@ def test_streamed_staging_identical(gpu_ctx, oracle, seg):
         assert plain == oracle_dict(oracle, shared, 21, 1, 1)
     finally:
         gpu_ctx.set_streamed_staging(True, 0)
+
+
+def test_packer_markers_inside_lines(gpu_ctx, oracle):
+    """'>' / '@' inside a sequence line are breaks, not record starts -- also
+    when they follow an all-ACGT 32-byte chunk that began at a line start (the
+    packer's fast path), at every 32-byte phase of the tile."""
+    from mczi_gb300.mc import CounterConfig
+    rng = np.random.default_rng(5)
+    bufs = []
+    for off in (0, 1, 31, 32, 33, 63, 64, 65, 96, 127, 128):
+        head = b">" + b"h" * max(0, off - 2) + b"\n" if off >= 2 else b""
+        lines = []
+        for j in range(6):
+            s = rng.choice(np.frombuffer(b"ACGT", dtype=np.uint8), size=200).tobytes()
+            cut = 32 * (j % 3 + 1)
+            lines.append(s[:cut] + (b">" if j % 2 else b"@") + s[cut:])
+        bufs.append((head if off >= 2 else b">r\n") + b"\n".join(lines) + b"\n")
+    fq = b"@q\n" + b"A" * 32 + b">" + b"C" * 40 + b"\n+\n" + b"I" * 73 + b"\n"
+    bufs.append(fq)
+    gpu_ctx.count(bufs, CounterConfig(1, 1, 0))
+    codes, starts = gpu_ctx.debug_packed()
+    exp_codes, exp_starts = [], []
+    for buf in bufs:
+        cc, offs, _ = oracle.fragments(buf, 1)
+        exp_codes.append(cc)
+        st = np.zeros(cc.size, dtype=np.uint8)
+        st[offs[:-1].astype(np.int64)] = 1
+        exp_starts.append(st)
+    assert np.array_equal(codes, np.concatenate(exp_codes))
+    assert np.array_equal(starts, np.concatenate(exp_starts))
+    for k in (5, 31):
+        assert gpu_dict(gpu_ctx, bufs, k, min(k, 3), 0) == oracle_dict(oracle, bufs, k, 0)
