@@ -311,31 +311,39 @@ __global__ void k_count(CountArgs a) {
         //   keys with plain-load lookups.  A k-mer seen once is never stored,
         //   and a k-mer seen twice or more always is, so for x >= 1 the
         //   emitted set and counts are the same as the single pass.
+        // a round of one batch keeps that batch's descriptors and chunk
+        // prefixes in shared memory from pass 1 to pass 2
+        const bool one_batch = dhi - dlo <= (uint64_t)nth;
+        uint32_t total = 0;
         for (int ph = filtered ? 1 : 0; ph <= (filtered ? 2 : 0); ph++) {
-          if (ph == 2) __syncthreads();
-          for (uint64_t bb = dlo; bb < dhi; bb += (uint64_t)nth) {
-            const bool has = bb + (uint64_t)tid < dhi;
-            uint64_t dsc = 0;
-            uint32_t nch = 0;
-            if (has) {
-              dsc = a.desc[lo + bb + (uint64_t)tid];
-              const uint32_t len = bd_windows(dsc);
-              nch = (len + chunk - 1) / chunk;
-              if (MODE == 1) {
-                const uint64_t s0 = bd_start(dsc);
-                int l2 = 0, h2 = a.n_datasets;  // largest i with dsbase[i] <= s0
-                while (h2 - l2 > 1) { const int mid = (l2 + h2) >> 1; if (dsbase[mid] <= s0) l2 = mid; else h2 = mid; }
-                sh_dset[tid] = (uint16_t)l2;
-              }
-            }
-            sh_desc[tid] = dsc;
-            if (tid == 0) s_step = 0;  // the previous batch's steps all ended before its closing barrier
-            uint32_t total;
-            const uint32_t cp = block_excl_scan_u32(nch, &total, warp_tmp);
-            sh_cpre[tid] = cp;
-            if (lane == 0) sh_cpre32[tid >> 5] = cp;
-            if (tid == 0) sh_cpre[nth] = total;
+          if (ph == 2) {
+            if (one_batch && tid == 0) s_step = 0;
             __syncthreads();
+          }
+          for (uint64_t bb = dlo; bb < dhi; bb += (uint64_t)nth) {
+            if (!(ph == 2 && one_batch)) {
+              const bool has = bb + (uint64_t)tid < dhi;
+              uint64_t dsc = 0;
+              uint32_t nch = 0;
+              if (has) {
+                dsc = a.desc[lo + bb + (uint64_t)tid];
+                const uint32_t len = bd_windows(dsc);
+                nch = (len + chunk - 1) / chunk;
+                if (MODE == 1) {
+                  const uint64_t s0 = bd_start(dsc);
+                  int l2 = 0, h2 = a.n_datasets;  // largest i with dsbase[i] <= s0
+                  while (h2 - l2 > 1) { const int mid = (l2 + h2) >> 1; if (dsbase[mid] <= s0) l2 = mid; else h2 = mid; }
+                  sh_dset[tid] = (uint16_t)l2;
+                }
+              }
+              sh_desc[tid] = dsc;
+              if (tid == 0) s_step = 0;  // the previous batch's steps all ended before its closing barrier
+              const uint32_t cp = block_excl_scan_u32(nch, &total, warp_tmp);
+              sh_cpre[tid] = cp;
+              if (lane == 0) sh_cpre32[tid >> 5] = cp;
+              if (tid == 0) sh_cpre[nth] = total;
+              __syncthreads();
+            }
             const int nd = (int)min((uint64_t)nth, dhi - bb);
             // Warps take steps of 32 chunks (one per lane) from a shared
             // counter, so a batch ends with at most one step of imbalance.  The
