@@ -122,8 +122,32 @@ def make_workload(scale: float, pinned: bool):
     return buf, n
 
 
+def figure_of_record_bytes(stats, k: int, text_bytes: int):
+    """Algorithmic bytes per kernel by the hot path's figure of record for the
+    minimizer-filtered MC path: FASTA read once (B_fasta), the 2-bit stream
+    written and read (0.5 N_b), the pass-1 re-read and minimizer table
+    (0.25 N_b + 24 B per superkmer), superkmer records written and read
+    (2 S_skm; payload ceil((windows + k - 1) / 4) + an 8 B header each), for
+    k > 32 the k-mer key round trip (2 x 16 B per window: the keys of one
+    partition do not fit on chip in a CPU-style design), and the output.
+    Assigned to the kernel that stands for each step: pack (FASTA, stream
+    write), scan (stream read, pass-1 terms, record write), count (record read,
+    key round trip, output); partition has no term of its own."""
+    nb, ns, win, nout = stats[0], stats[1], stats[6], stats[5]
+    rec = 24 if k > 32 else 12
+    s_skm = (win + ns * (k - 1)) / 4 + 8 * ns
+    keys = 2 * 16 * win if k > 32 else 0
+    return {
+        "pack": text_bytes + nb / 4,
+        "scan": nb / 4 + nb / 4 + 24 * ns + s_skm,
+        "partition": 0.0,
+        "count": s_skm + keys + rec * nout,
+    }
+
+
 def algorithmic_bytes(stats, k: int, text_bytes: int):
-    """Bytes each kernel must move (its inputs read once, outputs written once).
+    """Bytes this design's kernels must move (inputs read once, outputs
+    written once), with no credit for data the design avoids moving.
 
     pack     : FASTA bytes + 2-bit stream (N_b/4) + fragment bits (N_b/8)
     scan     : 2-bit stream + fragment bits + descriptors (12 B each)
@@ -252,9 +276,11 @@ def run_ours(args):
     names = ["pack", "scan", "partition", "count"]
     avg = {nm: phase_sum[i] / args.steps for i, nm in enumerate(names)}
     dom = max(avg, key=avg.get)
-    alg = algorithmic_bytes(stats, k, nbytes)
+    alg = figure_of_record_bytes(stats, k, nbytes)
+    own = algorithmic_bytes(stats, k, nbytes)
     peak, peak_kind = load_peaks()
     achieved = alg[dom] / (avg[dom] * 1e-3) / 1e9
+    achieved_own = own[dom] / (avg[dom] * 1e-3) / 1e9
     traffic = None
     tf = ROOT / "profiles" / "ncu_traffic.json"
     if tf.exists():
@@ -279,10 +305,15 @@ def run_ours(args):
         "phases_ms": {nm: round(v, 3) for nm, v in avg.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
-                     "algorithmic_bytes": int(alg[dom]), "traffic": int(traffic) if traffic else None},
+                     "algorithmic_bytes": int(alg[dom]), "bytes_basis": "figure of record (key round trip credited)",
+                     "traffic": int(traffic) if traffic else None},
+        "roofline_onchip": {"kernel": dom, "achieved": round(achieved_own, 1), "frac": round(achieved_own / peak, 4),
+                            "algorithmic_bytes": int(own[dom]),
+                            "bytes_basis": "this design's own movement (k-mers never leave the chip)"},
         "pipeline_roofline": {"algorithmic_bytes": int(sum(alg.values())),
                               "achieved_gbs": round(sum(alg.values()) / (dev_ms * 1e-3) / 1e9, 1),
-                              "frac": round(sum(alg.values()) / (dev_ms * 1e-3) / 1e9 / peak, 4)},
+                              "frac": round(sum(alg.values()) / (dev_ms * 1e-3) / 1e9 / peak, 4),
+                              "onchip_frac": round(sum(own.values()) / (dev_ms * 1e-3) / 1e9 / peak, 4)},
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:
