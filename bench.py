@@ -486,11 +486,16 @@ def run_zi(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     phases = [0.0] * 5
+    qsk = qbases_packed = 0
     for _ in range(args.steps):
         n_rec = 0
+        qsk = qbases_packed = 0
         for g in groups:
             n_rec += zi.query_per_input(ctx, g)
             phases = [a + b for a, b in zip(phases, ctx.phase_times())]
+            st = ctx.run_stats()
+            qbases_packed += st[0]
+            qsk += st[2]
     torch.cuda.synchronize()
     batched_s = (time.perf_counter() - t0) / args.steps
     phases = [x / args.steps for x in phases]
@@ -532,6 +537,14 @@ def run_zi(args):
                       "file_p50_ms": round(percentile(lat, 50) * 1e3, 3),
                       "file_p99_ms": round(percentile(lat, 99) * 1e3, 3)},
             "batched_over_plain": round(plain_s / batched_s, 2),
+            # for information (figure of record: FASTA once, 2-bit stream written and
+            # read, 96 B per query superkmer for MPHF / offsets / strings, records out)
+            "roofline": {"bound": "hbm", "kernel": "whole batched query", "unit": "GB/s",
+                         "algorithmic_bytes": int(query.size + qbases_packed / 2 + 96 * qsk + 16 * n_rec),
+                         "achieved": round((query.size + qbases_packed / 2 + 96 * qsk + 16 * n_rec) / batched_s / 1e9, 1),
+                         "peak": load_peaks()[0],
+                         "frac": round((query.size + qbases_packed / 2 + 96 * qsk + 16 * n_rec) / batched_s / 1e9
+                                       / load_peaks()[0], 4)},
             "union": {"s": round(union_s, 4), "lookups_per_s": round(windows / union_s, 1), "absent_kmers": n_absent},
             "data": "synthetic (seeded generator, no dataset)"}
     ctx.close()

@@ -124,7 +124,8 @@ int32_t mczi_phase_times(mczi_ctx* ctx, float* ms, int32_t cap);
 /* Statistics of the last run: [0] bases, [1] superkmers, [2] counting rounds,
  * [3] round splits, [4] distinct k-mers inserted, [5] kept records,
  * [6] k-mer windows, [7] skipped inputs, [8] kernel launches of the last
- * count, [9] host-to-device input bytes of the last staging. */
+ * count, [9] host-to-device input bytes of the last staging.  After a ZI
+ * query: [1] absent runs, [2] query superkmers, [6] absent windows. */
 int32_t mczi_run_stats(mczi_ctx* ctx, uint64_t* out, int32_t cap);
 
 /* Tuning knobs (results never depend on them): threads per counting CTA,

@@ -927,6 +927,7 @@ int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, u
   Pipe p;
   if ((rc = pipe_pack(ctx, p))) return rc;
   if ((rc = pipe_scan(ctx, p, z.k, z.m))) return rc;
+  const uint64_t n_query_sk = p.n_desc;
   uint64_t* sc = ctx->scalars.as<uint64_t>();
   // probe: absent-window runs into (desc2, key2)
   uint64_t cap = 2 * p.n_desc + 1024;
@@ -990,6 +991,7 @@ int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, u
   ctx->phase_ms[1] -= probe_ms;
   ctx->phase_ms[4] = probe_ms;
   ctx->stats[1] = n_runs;
+  ctx->stats[2] = n_query_sk;
   ctx->stats[6] = absent_w;
   if (n_out) *n_out = out;
   (void)p.n_desc_total;
