@@ -118,6 +118,7 @@ struct mczi_ctx {
   mczi::DevBuf desc, key, desc2, key2, part_hist, part_tmp, bucket_off;
   mczi::DevBuf out_lo, out_hi, out_cnt, out_mask;
   mczi::DevBuf cnt64;  // counts widened to u64 for direct copies to the caller
+  mczi::DevBuf sx_keys, sx_tab, sx_rank, sx_ext;  // simplitig writer: sorted keys, key->rank table, extensions
   mczi::DevBuf stream_scratch;     // streamed staging: pack carries, scan tile range
   cudaStream_t copy_stream = nullptr;  // host-to-device copies of the streamed staging
   cudaEvent_t ev_copy = nullptr;       // last copied segment
@@ -220,6 +221,10 @@ int32_t stage_layout(mczi_ctx* ctx, const InputPlan& pl, size_t n);
 int32_t copy_text_range(mczi_ctx* ctx, const mczi_input* inputs, size_t n, const InputPlan& pl, uint64_t b0,
                         uint64_t b1, cudaStream_t s);
 int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n);
+// simplitig.cu: extension table of n sorted distinct keys (lo, hi host arrays)
+// into ext_host (n x SIMPLITIG_STRIDE words; see host_io.h)
+int32_t simplitig_extensions(mczi_ctx* ctx, const uint64_t* lo, const uint64_t* hi, uint64_t n, int k,
+                             uint32_t* ext_host);
 int32_t pack_prepare(mczi_ctx* ctx, Pipe& p, mczi::PackArgs& pa);
 int32_t pipe_pack(mczi_ctx* ctx, Pipe& p);
 int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m, uint32_t p1_lo = 0, uint32_t p1_hi = 1u << 12,

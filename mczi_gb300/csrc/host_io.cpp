@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <thread>
 
 namespace mczi {
 
@@ -217,6 +218,98 @@ bool write_simplitig_file(const std::string& path, const HostRecords& r, int k, 
     extend_forward(seq, k, rem);
     revcomp(seq);
     extend_forward(seq, k, rem);
+    revcomp(seq);
+    idx++;
+    const int l = std::snprintf(line, sizeof line, ">MC_simplitig_%llu kmers=%llu\n", (unsigned long long)idx,
+                                (unsigned long long)(seq.size() - (size_t)k + 1));
+    o.put(line, (size_t)l);
+    for (size_t p = 0; p < seq.size(); p += 80) {
+      const size_t len = std::min<size_t>(80, seq.size() - p);
+      o.put(seq.data() + p, len);
+      o.put_u8('\n');
+    }
+  }
+  if (!o.close()) {
+    *err = "failed to write " + path;
+    return false;
+  }
+  return true;
+}
+
+void sorted_keys(const HostRecords& r, std::vector<uint64_t>* lo, std::vector<uint64_t>* hi, int threads) {
+  const size_t n = r.lo.size();
+  std::vector<u128> a(n), b(n);
+  for (size_t i = 0; i < n; i++) a[i] = key_at(r, i);
+  // chunks sorted in parallel, then merged pairwise (also in parallel)
+  size_t parts = 1;
+  while ((int)parts * 2 <= std::max(1, threads) && n / (parts * 2) >= (1u << 16)) parts *= 2;
+  std::vector<size_t> cut(parts + 1);
+  for (size_t p = 0; p <= parts; p++) cut[p] = n * p / parts;
+  {
+    std::vector<std::thread> th;
+    for (size_t p = 0; p < parts; p++) th.emplace_back([&, p] { std::sort(a.begin() + cut[p], a.begin() + cut[p + 1]); });
+    for (auto& t : th) t.join();
+  }
+  for (size_t w = 1; w < parts; w *= 2) {
+    std::vector<std::thread> th;
+    for (size_t p = 0; p < parts; p += 2 * w) {
+      const size_t l = cut[p], m = cut[std::min(p + w, parts)], h = cut[std::min(p + 2 * w, parts)];
+      th.emplace_back([&, l, m, h] { std::merge(a.begin() + l, a.begin() + m, a.begin() + m, a.begin() + h, b.begin() + l); });
+    }
+    for (auto& t : th) t.join();
+    a.swap(b);
+  }
+  a.erase(std::unique(a.begin(), a.end()), a.end());
+  lo->resize(a.size());
+  hi->resize(a.size());
+  for (size_t i = 0; i < a.size(); i++) {
+    (*lo)[i] = (uint64_t)a[i];
+    (*hi)[i] = (uint64_t)(a[i] >> 64);
+  }
+}
+
+bool write_simplitig_walk(const std::string& path, const uint64_t* lo, const uint64_t* hi, uint64_t n, int k,
+                          const uint32_t* ext, std::string* err) {
+  File o(path);
+  if (!o.f) {
+    *err = "failed to create " + path;
+    return false;
+  }
+  static const char B[4] = {'A', 'C', 'G', 'T'};
+  std::vector<uint8_t> used_flags(n, 0);
+  auto used = [&](uint64_t j) -> uint8_t& { return used_flags[j]; };
+  std::string seq;
+  char line[64];
+  uint64_t idx = 0;
+  // follows the extension table from (i, o), appending bases, marking k-mers used
+  auto extend = [&](uint32_t i, uint32_t o) {
+    for (;;) {
+      const uint32_t* e = ext + (uint64_t)i * SIMPLITIG_STRIDE + o * 4;
+      bool moved = false;
+      for (int b = 0; b < 4; b++) {
+        const uint32_t v = e[b];
+        if (v == SIMPLITIG_NO_EXT) continue;
+        const uint32_t j = v >> 1;
+        if (used(j)) continue;
+        used(j) = 1;
+        seq.push_back(B[b]);
+        i = j;
+        o = v & 1u;
+        moved = true;
+        break;
+      }
+      if (!moved) return;
+    }
+  };
+  for (uint64_t s = 0; s < n; s++) {
+    if (used(s)) continue;
+    used(s) = 1;
+    const u128 seed = ((u128)hi[s] << 64) | lo[s];
+    seq.clear();
+    for (int j = 0; j < k; j++) seq.push_back(B[(int)((seed >> (2 * (k - 1 - j))) & 3)]);
+    extend((uint32_t)s, 0);  // the path ends in the seed's canonical string
+    revcomp(seq);
+    extend((uint32_t)s, 1);  // reverse-complemented, it ends in the seed's reverse complement
     revcomp(seq);
     idx++;
     const int l = std::snprintf(line, sizeof line, ">MC_simplitig_%llu kmers=%llu\n", (unsigned long long)idx,

@@ -18,6 +18,21 @@ bool write_kff_file(const std::string& path, const HostRecords& r, int k, int m,
 // Greedy simplitig FASTA (src/lib.rs:1469-1533).  Returns false on I/O error.
 bool write_simplitig_file(const std::string& path, const HostRecords& r, int k, std::string* err);
 
+// The same FASTA from the keys in ascending order (lo, hi; hi all 0 for k <= 32)
+// and their extension table, SIMPLITIG_STRIDE words per key: ext[i *
+// SIMPLITIG_STRIDE + o * 4 + b] = j << 1 | o' when k-mer i in orientation o
+// (0: canonical string, 1: its reverse complement) followed by base b (A0 C1
+// G2 T3) is k-mer j in orientation o', else SIMPLITIG_NO_EXT.  Byte-identical
+// to write_simplitig_file.
+constexpr uint32_t SIMPLITIG_NO_EXT = 0xffffffffu;
+constexpr int SIMPLITIG_STRIDE = 8;
+bool write_simplitig_walk(const std::string& path, const uint64_t* lo, const uint64_t* hi, uint64_t n, int k,
+                          const uint32_t* ext, std::string* err);
+
+// The distinct keys of r in ascending (hi, lo) order, sorted on up to
+// `threads` host threads.
+void sorted_keys(const HostRecords& r, std::vector<uint64_t>* lo, std::vector<uint64_t>* hi, int threads);
+
 bool read_file(const std::string& path, std::vector<uint8_t>* out, std::string* err);
 
 }  // namespace mczi

@@ -16,6 +16,7 @@
 #include "scan.cuh"
 
 #include <algorithm>
+#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1049,7 +1050,19 @@ int32_t mczi_result_write_fasta(mczi_ctx* ctx, const char* path) {
   int32_t rc = fetch_records(ctx, &r);
   if (rc) return rc;
   std::string e;
-  if (!write_simplitig_file(path, r, ctx->k, &e)) return fail(ctx, MCZI_ERR_IO, e);
+  if (r.lo.size() >= (1ull << 31)) {  // ranks must fit 31 bits: the plain writer
+    if (!write_simplitig_file(path, r, ctx->k, &e)) return fail(ctx, MCZI_ERR_IO, e);
+    return MCZI_OK;
+  }
+  // seeds in ascending order (host, parallel), their extensions on the device,
+  // then the greedy walk over the table (host)
+  std::vector<uint64_t> lo, hi;
+  const unsigned hw = std::thread::hardware_concurrency();
+  sorted_keys(r, &lo, &hi, (int)std::max(1u, std::min(hw, 64u)));
+  r = HostRecords();
+  std::vector<uint32_t> ext(lo.size() * SIMPLITIG_STRIDE);
+  if ((rc = simplitig_extensions(ctx, lo.data(), hi.data(), lo.size(), ctx->k, ext.data()))) return rc;
+  if (!write_simplitig_walk(path, lo.data(), hi.data(), lo.size(), ctx->k, ext.data(), &e)) return fail(ctx, MCZI_ERR_IO, e);
   return MCZI_OK;
 }
 
