@@ -1,11 +1,11 @@
 """Command lines of MC and ZI over the GPU library.
 
-``python -m mczi_gb300.cli mc ...`` and ``python -m mczi_gb300.cli zi ...``
-take the flags of the reference's binaries (MC: src/main.rs:10-101, ZI:
-src/zi.rs:13-101) with the same defaults and validation messages, and run the
-same library entry points (count_inputs_to_{kff,fasta}_path,
+``python -m mczi_gb300.cli mc|zi|mczi ...`` take the flags of the reference's
+binaries (MC: src/main.rs:10-101, ZI: src/zi.rs:13-101, MCZI:
+src/mczi.rs:140-230) with the same defaults and validation messages, and run
+the same library entry points (count_inputs_to_{kff,fasta}_path,
 count_datasets_to_{kff,fasta}_path; build_dictionary,
-collect_query_kmers_absent_from_index, write_novel_simplitigs).  Errors print
+collect_query_kmers_absent_from_index, write_novel_simplitigs; mczi.run).  Errors print
 as ``Error: <message>`` with exit status 1.  ``--threads`` is accepted and
 validated; the device work does not use host threads, and ZI's
 ``--ram-limit-gib`` only bounded the reference's external-memory build.
@@ -58,6 +58,44 @@ def _zi_parser() -> argparse.ArgumentParser:
     return ap
 
 
+def _mczi_parser() -> argparse.ArgumentParser:
+    ap = argparse.ArgumentParser(prog="MCZI", description="Run MC indexing and ZI subtraction in one process (GB300)")
+    ap.add_argument("--index-input", nargs="+", required=True, type=Path,
+                    help="MC index-set input FASTA/FASTQ file(s), or FOFN path(s) with --index-fofn")
+    ap.add_argument("--index-fofn", action="store_true", help="Treat --index-input path(s) as MC file-of-filenames")
+    ap.add_argument("--query-input", nargs="+", required=True, type=Path,
+                    help="Query FASTA/FASTQ file(s), or FOFN path(s) with --query-fofn")
+    ap.add_argument("--query-fofn", action="store_true", help="Treat --query-input path(s) as file-of-filenames")
+    ap.add_argument("-k", "--kmer-size", type=int, required=True, help="K-mer size; must be odd and in [3, 63]")
+    ap.add_argument("-m", "--minimizer-size", type=int, required=True, help="MC minimizer size; also used for the index")
+    ap.add_argument("-x", "--threshold", type=int, default=1, help="MC threshold for the index set")
+    ap.add_argument("-o", "--output", type=Path, default=None,
+                    help="Output FASTA path (a folder in --query-fofn mode)")
+    ap.add_argument("--output-suffix", default="filtered", help="Suffix of each output name in --query-fofn mode")
+    ap.add_argument("--output-mode", default="simplitig", help="simplitig or no-output")
+    ap.add_argument("--reform-output", action="store_true", help="R-style reforming (not available here)")
+    ap.add_argument("-t", "--threads", type=int, default=None, help="Host worker threads (validated only)")
+    ap.add_argument("--partition-count", type=int, default=mc.DEFAULT_PARTITION_COUNT)
+    ap.add_argument("--ram-limit-gib", type=int, default=8, help="Build RAM limit of the reference (unused)")
+    return ap
+
+
+def mczi_main(argv: list[str]) -> None:
+    from . import mczi
+    a = _mczi_parser().parse_args(argv)
+    if a.reform_output:
+        raise N.MCZIError(N.MCZI_ERR_INVALID_CONFIG, "--reform-output (the R reformer) is not available in this build")
+    if a.threads is not None and a.threads <= 0:
+        raise N.MCZIError(N.MCZI_ERR_INVALID_CONFIG, "--threads must be greater than 0")
+    index_inputs = mc.expand_fofns(a.index_input) if a.index_fofn else list(a.index_input)
+    query_inputs = mc.expand_fofns(a.query_input) if a.query_fofn else list(a.query_input)
+    started = time.perf_counter()
+    stats = mczi.run(index_inputs, query_inputs, a.kmer_size, a.minimizer_size, a.threshold, a.output,
+                     a.query_fofn, a.output_suffix, a.output_mode, a.partition_count)
+    print(f"MCZI_STAT\tindex_kmers\t{stats['index_kmers']}\tabsent_kmers\t{sum(stats['absent'])}", file=sys.stderr)
+    _phase("total", started)
+
+
 def _phase(name: str, t0: float) -> None:
     print(f"ZI_PHASE\t{name}\t{time.perf_counter() - t0:.6f}s", file=sys.stderr)
 
@@ -100,11 +138,12 @@ def zi_main(argv: list[str]) -> None:
 
 def main(argv: list[str] | None = None) -> int:
     argv = list(sys.argv[1:] if argv is None else argv)
-    if not argv or argv[0] not in ("mc", "zi"):
-        print("usage: python -m mczi_gb300.cli {mc,zi} [flags of the MC / ZI binaries]", file=sys.stderr)
+    mains = {"mc": mc_main, "zi": zi_main, "mczi": mczi_main}
+    if not argv or argv[0] not in mains:
+        print("usage: python -m mczi_gb300.cli {mc,zi,mczi} [flags of the MC / ZI / MCZI binaries]", file=sys.stderr)
         return 2
     try:
-        (mc_main if argv[0] == "mc" else zi_main)(argv[1:])
+        mains[argv[0]](argv[1:])
     except N.MCZIError as e:
         print(f"Error: {e}", file=sys.stderr)
         return 1

@@ -90,3 +90,53 @@ def test_zi_cli_absent_set(oracle, tmp_path):
 def oracle_absent_set(oracle, index, queries, k):
     lo, hi = oracle.zi_absent(index, queries, k)
     return to_int(lo, hi)
+
+
+def test_mczi_output_names_and_validation(tmp_path, capsys):
+    from mczi_gb300 import mczi
+    assert mczi.suffixed_query_file_name("reads.fq.gz", "filtered") == "reads.filtered.fq.gz"
+    assert mczi.suffixed_query_file_name("a.FASTA", "x") == "a.x.FASTA"
+    assert mczi.suffixed_query_file_name("noext", "f") == "noext.f"
+    assert mczi.normalized_output_suffix(" .keep ") == "keep"
+    fa = tmp_path / "i.fa"
+    fa.write_bytes(b">r\nACGTACGTAC\n")
+    assert run_cli(["mczi", "--index-input", str(fa), "--query-input", str(fa), "-k", "5", "-m", "3"]) == 1
+    assert "--output is required unless --query-fofn or --output-mode no-output is set" in capsys.readouterr().err
+    assert run_cli(["mczi", "--index-input", str(fa), "--query-input", str(fa), "-k", "5", "-m", "3",
+                    "--output-mode", "no-output", "-o", str(tmp_path / "o.fa")]) == 1
+    assert "--output is not used with --output-mode no-output" in capsys.readouterr().err
+    assert run_cli(["mczi", "--index-input", str(fa), "--query-input", str(fa), "-k", "6", "-m", "3",
+                    "-o", str(tmp_path / "o.fa")]) == 1
+    assert "k must be odd for sshash-rs" in capsys.readouterr().err
+
+
+@pytest.mark.gpu
+def test_mczi_cli_absent_sets(oracle, tmp_path):
+    rng = np.random.default_rng(9)
+    g = rng.choice(np.frombuffer(b"ACGT", dtype=np.uint8), size=5000).tobytes()
+    other = rng.choice(np.frombuffer(b"ACGT", dtype=np.uint8), size=2000).tobytes()
+    # the index set: k-mers seen more than once (x = 1) in reads of g
+    reads = b"".join(b">r%d\n%s\n" % (i, g[s:s + 300]) for i, s in enumerate(range(0, 4700, 150)))
+    ip = tmp_path / "index.fa"
+    ip.write_bytes(reads)
+    q1 = tmp_path / "q1.fa"
+    q1.write_bytes(b">a\n" + g[1000:1400] + b"\n>b\n" + other[:600] + b"\n")
+    q2 = tmp_path / "q2.fasta"
+    q2.write_bytes(b">c\n" + other[500:1500] + b"\n")
+    lo, hi, _ = oracle.count([reads], 31, 1)
+    idx_fa = tmp_path / "kept.fa"
+    oracle.write_simplitigs(idx_fa, lo, hi, 31)
+    fofn = tmp_path / "queries.fofn"
+    fofn.write_text("q1.fa\nq2.fasta\n")
+    outdir = tmp_path / "out"
+    assert run_cli(["mczi", "--index-input", str(ip), "--query-input", str(fofn), "--query-fofn",
+                    "-k", "31", "-m", "19", "-x", "1", "-o", str(outdir)]) == 0
+    for q, name in ((q1, "q1.filtered.fa"), (q2, "q2.filtered.fasta")):
+        got = {_canon(v, 31) for v in _fasta_kmers(outdir / name, 31)}
+        assert got == set(oracle_absent_set(oracle, idx_fa.read_bytes(), [q.read_bytes()], 31))
+    # one output for all queries
+    single = tmp_path / "all.fa"
+    assert run_cli(["mczi", "--index-input", str(ip), "--query-input", str(q1), str(q2),
+                    "-k", "31", "-m", "19", "-o", str(single)]) == 0
+    got = {_canon(v, 31) for v in _fasta_kmers(single, 31)}
+    assert got == set(oracle_absent_set(oracle, idx_fa.read_bytes(), [q1.read_bytes(), q2.read_bytes()], 31))
