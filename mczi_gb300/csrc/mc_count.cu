@@ -390,21 +390,15 @@ __global__ void k_count(CountArgs a) {
               const uint32_t* wp = a.packed + (p >> 4);
               uint32_t q = (uint32_t)(p & 15);
               uint32_t word = *wp << (2 * q);
-              // software pipeline: the key and hash of window j + 1 are made
-              // before window j probes the table (independent work for the
-              // scheduler while the probe's shared-memory loads are in flight)
-              K key_n = roll.canon();
-              uint64_t hv_n = key_hash(key_n);
               for (uint32_t j = w0; j < w1; j++) {
-                const K key = key_n;
-                const uint64_t hv = hv_n;
-                if (j + 1 < w1) {
+                if (j > w0) {
                   roll.push(word >> 30);
                   word <<= 2;
                   if (++q == 16) { q = 0; word = *++wp; }
-                  key_n = roll.canon();
-                  hv_n = key_hash(key_n);
                 }
+                // slot, bitmap position and range come from the strand-symmetric
+                // hash; the canonical key is formed only where the table is touched
+                const uint64_t hv = sym_hash(roll);
                 if (!full_range) {
                   const uint32_t hk = (uint32_t)(hv >> 32);
                   if (hk < rr.hlo || hk > rr.hhi) continue;
@@ -417,6 +411,7 @@ __global__ void k_count(CountArgs a) {
                   // a key pass 1 never stored has its claimed bit clear
                   const uint32_t cp = (uint32_t)((hb * cbits) >> 32);
                   if (!((cmap[cp >> 5] >> (cp & 31)) & 1u)) continue;
+                  const K key = roll.canon();
                   // keys are final during pass 2: plain loads, stop at EMPTY
                   for (uint32_t probe = 0; probe < PROBE_LIMIT; probe++) {
                     const K cur = keys[s];
@@ -437,6 +432,7 @@ __global__ void k_count(CountArgs a) {
                   const uint32_t cp = (uint32_t)((hb * cbits) >> 32);
                   atomicOr(&cmap[cp >> 5], 1u << (cp & 31));  // stored (below) or already stored
                 }
+                const K key = roll.canon();
                 bool done = false;
                 // Probe with plain loads; CAS only on a slot that looks empty.
                 // A slot goes from EMPTY to a key exactly once, so a load that

@@ -141,6 +141,15 @@ struct Roll128 {
   }
 };
 
+// Strand-symmetric hash of a rolling k-mer: forward XOR reverse complement is
+// the same for both strands, so the hash is a function of the canonical k-mer
+// without forming it (the 128-bit compare and select of canon()).
+__device__ __forceinline__ uint64_t sym_hash(const Roll64& r) { return mix64(r.fwd ^ r.rev); }
+__device__ __forceinline__ uint64_t sym_hash(const Roll128& r) {
+  const uint64_t a = r.flo ^ r.rlo ^ 0x2d358dccaa6c78a5ull, b = r.fhi ^ r.rhi ^ 0x8bb84b93962eacc9ull;
+  return (a * b) ^ __umul64hi(a, b);
+}
+
 // ------------------------------------------------------------- packed stream
 __device__ __forceinline__ uint32_t base_at(const uint32_t* __restrict__ packed, uint64_t p) {
   return (packed[p >> 4] >> (30 - 2 * (uint32_t)(p & 15))) & 3u;
