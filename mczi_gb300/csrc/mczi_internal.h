@@ -77,8 +77,8 @@ void launch_scan_window(const uint64_t* avail, uint64_t* range, bool final, uint
 void launch_scan_range(const ScanArgs& a, uint64_t max_tiles, cudaStream_t s);
 
 // ---------------------------------------------------------------- K3 partition
-constexpr int PART_CTAS = 304;   // 2 per SM on a 152-SM GB300
-constexpr int PART_THREADS = 512;
+constexpr int PART_CTAS = 152;   // 1 per SM on a 152-SM GB300
+constexpr int PART_THREADS = 1024;
 
 struct PartArgs {
   const uint64_t* desc_in;
