@@ -123,6 +123,7 @@ struct mczi_ctx {
   cudaStream_t copy_stream = nullptr;  // host-to-device copies of the streamed staging
   cudaEvent_t ev_copy = nullptr;       // last copied segment
   int streamed = 1;                    // one-shot counts overlap staging with pack + scan
+  int fuse_part2 = 1;                  // partition pass 2 runs inside the counting kernel
   uint64_t stream_seg_tiles = 0;       // segment size in pack tiles (0 = automatic)
   mczi::DevBuf scalars;
   mczi::DevBuf mintab, pairtab;

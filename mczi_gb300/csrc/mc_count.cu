@@ -186,10 +186,11 @@ __global__ void k_count(CountArgs a) {
     if (hi <= lo) continue;
 
     // ---- per-bin occupancy and descriptor counts
+    const uint64_t* src = a.desc_unsorted ? a.desc_unsorted : a.desc;
     for (int i = tid; i <= NP2; i += nth) { occ[i] = 0; dst[i] = 0; }
     __syncthreads();
     for (uint64_t i = lo + tid; i < hi; i += nth) {
-      const uint64_t bd = a.desc[i];
+      const uint64_t bd = src[i];
       const uint32_t bin = bd_p2(bd);
       const uint32_t len = bd_windows(bd);
       atomicAdd(&occ[bin], len);
@@ -242,6 +243,25 @@ __global__ void k_count(CountArgs a) {
       __syncthreads();
       if (tid == nth - 1) { occ[NP2] = ro; dst[NP2] = rd; }
       __syncthreads();
+    }
+    if (a.desc_unsorted) {
+      // partition pass 2 of this bucket: p2 order into `desc`, the bin starts
+      // as cursors (afterwards dst[b] holds the start of bin b + 1)
+      uint64_t* out = const_cast<uint64_t*>(a.desc);
+      for (uint64_t i = lo + tid; i < hi; i += nth) {
+        const uint64_t bd = src[i];
+        out[lo + atomicAdd(&dst[bd_p2(bd)], 1u)] = bd;
+      }
+      __syncthreads();
+      // shift back by one bin, top chunk first: a chunk reads only entries
+      // below itself, which later (lower) chunks have not rewritten yet
+      for (int top = NP2; top >= 0; top -= nth) {
+        const int i = top - tid;
+        const uint32_t v = (i > 0) ? dst[i - 1] : 0u;
+        __syncthreads();
+        if (i >= 0) dst[i] = v;
+        __syncthreads();
+      }
     }
 
     // ---- cut bins into rounds: round id of a bin = floor(occ_prefix / budget)

@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(PART_THREADS) k_part2(PartArgs a) {
   }
 }
 
-void launch_partition(const PartArgs& a, cudaStream_t s) {
+void launch_partition(const PartArgs& a, cudaStream_t s, bool with_pass2) {
   k_part1_hist<<<PART_CTAS, PART_THREADS, 0, s>>>(a);
   const uint64_t nh = (uint64_t)NP1 * PART_CTAS;
   // scanned hist goes to hist + nh + 1 .. (exclusive; entry nh is the total)
@@ -185,7 +185,7 @@ void launch_partition(const PartArgs& a, cudaStream_t s) {
   exclusive_scan<uint32_t, SumU32>(a.hist, pre, nh, a.hist_tmp, s);
   k_part1_offsets<<<16, 256, 0, s>>>(pre, a.bucket_off);
   k_part1_scatter<<<PART_CTAS, PART_THREADS, 0, s>>>(a, pre);
-  k_part2<<<NP1, PART_THREADS, 0, s>>>(a);
+  if (with_pass2) k_part2<<<NP1, PART_THREADS, 0, s>>>(a);
 }
 
 }  // namespace mczi

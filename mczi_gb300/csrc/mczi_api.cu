@@ -366,7 +366,7 @@ int32_t pipe_partition(mczi_ctx* ctx, Pipe& p) {
   qa.bucket_off = ctx->bucket_off.as<uint64_t>();
   qa.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
   if (p.n_desc > 0) {
-    launch_partition(qa, s);
+    launch_partition(qa, s, !ctx->fuse_part2);
     p.launches += 7;
   }
   CK(cudaGetLastError());
@@ -443,6 +443,7 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       CountArgs ca;
       ca.packed = ctx->packed.as<uint32_t>();
       ca.desc = ctx->desc.as<uint64_t>();
+      ca.desc_unsorted = ctx->fuse_part2 ? ctx->desc2.as<uint64_t>() : nullptr;
       ca.key = ctx->key.as<uint32_t>();
       ca.bucket_off = ctx->bucket_off.as<uint64_t>();
       ca.k = k;

@@ -92,7 +92,7 @@ struct PartArgs {
   uint64_t* bucket_off; // NP1 + 1 bucket offsets (p1 buckets)
   uint32_t* status;
 };
-void launch_partition(const PartArgs& a, cudaStream_t s);
+void launch_partition(const PartArgs& a, cudaStream_t s, bool with_pass2 = true);
 
 // ---------------------------------------------------------------- K4 pre-count
 struct PrecountArgs {
@@ -118,6 +118,9 @@ void launch_precount(const PrecountArgs& a, int sm_count, cudaStream_t s);
 struct CountArgs {
   const uint32_t* packed;
   const uint64_t* desc;       // sorted by (p1, p2)
+  // when set: the pass-1 output (grouped by p1 only); each CTA sorts its
+  // bucket by p2 into `desc` itself (partition pass 2 fused into counting)
+  const uint64_t* desc_unsorted;
   const uint32_t* key;
   const uint64_t* bucket_off; // NP1 + 1
   int k;
