@@ -423,7 +423,6 @@ __global__ void k_count(CountArgs a) {
                   const uint32_t hk = (uint32_t)(hv >> 32);
                   if (hk < rr.hlo || hk > rr.hhi) continue;
                 }
-                uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
                 // bitmap positions from hash bits 20..51 (the slot uses the low
                 // 32 bits, range splits bits 32..63)
                 const uint64_t hb = (hv >> 20) & 0xffffffffull;
@@ -432,6 +431,7 @@ __global__ void k_count(CountArgs a) {
                   const uint32_t cp = (uint32_t)((hb * cbits) >> 32);
                   if (!((cmap[cp >> 5] >> (cp & 31)) & 1u)) continue;
                   const K key = roll.canon();
+                  uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
                   // keys are final during pass 2: plain loads, stop at EMPTY
                   for (uint32_t probe = 0; probe < PROBE_LIMIT; probe++) {
                     const K cur = keys[s];
@@ -453,6 +453,7 @@ __global__ void k_count(CountArgs a) {
                   atomicOr(&cmap[cp >> 5], 1u << (cp & 31));  // stored (below) or already stored
                 }
                 const K key = roll.canon();
+                uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
                 bool done = false;
                 // Probe with plain loads; CAS only on a slot that looks empty.
                 // A slot goes from EMPTY to a key exactly once, so a load that

@@ -295,12 +295,10 @@ __global__ void k_scan_window(const uint64_t* __restrict__ avail, uint64_t* __re
   range[1] = hi;
 }
 
+// the attribute is per device: set before every launch (a host-side call of
+// microseconds, allowed during stream capture)
 static void scan_attr() {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scan_smem_bytes());
-    attr_set = true;
-  }
+  cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scan_smem_bytes());
 }
 
 void launch_scan(const ScanArgs& a, cudaStream_t s) {
