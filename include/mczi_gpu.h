@@ -221,6 +221,13 @@ int32_t mczi_zi_batch_split(mczi_ctx* ctx, uint64_t* key_lo, uint64_t* key_hi, u
  * [5] distinct minimizers (MPHF keys), [6] MPHF levels, [7] build time (us). */
 int32_t mczi_zi_info(mczi_ctx* ctx, uint64_t* out, int32_t cap);
 
+/* Records per final bucket of the ZI deduplication (no reference counterpart:
+ * a sizing knob of this library).  The absent windows are partitioned by
+ * k-mer hash into 2^b <= 131072 buckets of about `records` each, in one level
+ * of <= 256 buckets or two; 0 = automatic (half the shared-memory table).
+ * Smaller values only add partition work; results are identical. */
+int32_t mczi_set_zi_bucket_records(mczi_ctx* ctx, uint32_t records);
+
 /* ------------------------------------------------ packing without allocation */
 
 /* The 2-bit packer of mczi_count's first phase, for callers that cannot

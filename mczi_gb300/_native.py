@@ -81,6 +81,7 @@ SIGNATURES = [
     ("mczi_set_graph_replay", C.c_int32, [C.c_void_p, C.c_int32]),
     ("mczi_set_minimizer_precount", C.c_int32, [C.c_void_p, C.c_int32]),
     ("mczi_set_streamed_staging", C.c_int32, [C.c_void_p, C.c_int32, C.c_uint64]),
+    ("mczi_set_zi_bucket_records", C.c_int32, [C.c_void_p, C.c_uint32]),
     ("mczi_debug_packed", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     ("mczi_zi_build", C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32]),
     ("mczi_zi_query", C.c_int32, [C.c_void_p, C.POINTER(InputC), C.c_size_t, C.POINTER(C.c_uint64)]),

@@ -109,6 +109,8 @@ struct mczi_ctx {
   int device = 0;
   int sm_count = 0;
   size_t smem_optin = 0;
+  size_t smem_per_sm = 0;
+  size_t smem_reserved = 0;            // reserved shared memory per block
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   std::string err;
@@ -125,6 +127,7 @@ struct mczi_ctx {
   int streamed = 1;                    // one-shot counts overlap staging with pack + scan
   int fuse_part2 = 1;                  // partition pass 2 runs inside the counting kernel
   uint64_t stream_seg_tiles = 0;       // segment size in pack tiles (0 = automatic)
+  uint32_t zi_bucket_records = 0;      // records per final ZI dedup bucket (0 = half a table)
   mczi::DevBuf scalars;
   mczi::DevBuf mintab, pairtab;
   mczi::DevBuf zi_tmp0, zi_tmp1, zi_tmp2, zi_tmp3, zi_tmp4;

@@ -908,6 +908,8 @@ int32_t mczi_open(int32_t device, mczi_ctx** out) {
   }
   ctx->sm_count = prop.multiProcessorCount;
   ctx->smem_optin = prop.sharedMemPerBlockOptin;
+  ctx->smem_per_sm = prop.sharedMemPerMultiprocessor;
+  ctx->smem_reserved = prop.reservedSharedMemPerBlock;
   if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete ctx;
     return MCZI_ERR_DEVICE;
@@ -1144,6 +1146,12 @@ int32_t mczi_set_streamed_staging(mczi_ctx* ctx, int32_t enable, uint64_t segmen
   if (segment_bytes % PACK_TILE) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "segment size must be a multiple of 8192");
   ctx->streamed = enable ? 1 : 0;
   ctx->stream_seg_tiles = segment_bytes / PACK_TILE;
+  return MCZI_OK;
+}
+
+int32_t mczi_set_zi_bucket_records(mczi_ctx* ctx, uint32_t records) {
+  if (!ctx) return MCZI_ERR_STATE;
+  ctx->zi_bucket_records = records;
   return MCZI_OK;
 }
 

@@ -273,12 +273,14 @@ __global__ void __launch_bounds__(ZI_THREADS) k_zi_probe(ProbeArgs a) {
 // their runs are short and scattered, so regenerating them per counting round
 // would pay a scattered packed-stream gather per run and per round.  Instead:
 //   1. expand: each absent run is rolled once, in emission order (close to
-//      stream order), into flat (k-mer, input) records scattered into 2^b1
-//      buckets (b1 <= 8) by the top bits of the k-mer hash (histogram, scan
-//      and per-CTA shared-memory cursors).  At most 256 x 304 destinations
-//      are open at a time, so L2 combines the scattered writes;
+//      stream order), into flat (k-mer, input) records partitioned into 2^b1
+//      buckets (b1 <= 8) by the top bits of the k-mer hash: a histogram pass
+//      gives every CTA its own range of each bucket, then the CTA takes about
+//      a thousand runs at a time, counting-sorts their records by bucket in
+//      shared memory and writes each bucket's share as one contiguous piece
+//      (a run of more than DD_LONG windows is written record by record);
 //   2. split: when more buckets are needed, one CTA per bucket splits it by
-//      the next b2 <= 8 bits the same way;
+//      the next b2 <= 9 bits, with the same tile-sorted writes;
 //   3. dedup: a persistent CTA takes one final bucket at a time (sized to
 //      about half its shared-memory table) and deduplicates it there, in
 //      sub-rounds over the next 20 hash bits when the bucket is larger; a
@@ -286,10 +288,48 @@ __global__ void __launch_bounds__(ZI_THREADS) k_zi_probe(ProbeArgs a) {
 //      result).
 constexpr int DD_MAX_BITS1 = 8;
 constexpr int DD_NB1 = 1 << DD_MAX_BITS1;
+constexpr int DD_MAX_BITS = 17;  // final buckets: level 1 (<= 8 bits) + level 2 (<= 9 bits)
+constexpr int DD_NB2 = 1 << (DD_MAX_BITS - DD_MAX_BITS1);
 constexpr int DD_CTAS = 304;
 constexpr int DD_THREADS = 512;
 constexpr int DDK_THREADS = 1024;
 constexpr uint32_t DD_PROBE_LIMIT = 256;
+constexpr uint32_t DD_LONG = 64;  // longer runs bypass the shared-memory tile
+constexpr int DD_RPT = 2;         // runs per thread in one expand tile
+
+// records in one shared-memory tile of the sorted scatters (key, input id and
+// bucket per record: about 90 KB for 64-bit keys, 76 KB for 128-bit keys)
+template <class K> struct DdTile;
+template <> struct DdTile<K64> { static constexpr uint32_t CAP = 8192; };
+template <> struct DdTile<K128> { static constexpr uint32_t CAP = 4096; };
+template <class K> constexpr size_t dd_tile_bytes() { return (size_t)DdTile<K>::CAP * (sizeof(K) + 3); }
+// the split's tile: a 16-bit bucket per record (up to 9 bits)
+template <class K> constexpr size_t dd_split_tile_bytes() { return (size_t)DdTile<K>::CAP * (sizeof(K) + 4); }
+
+// exclusive block scan of one u32 per thread; ws holds 32 words
+__device__ __forceinline__ uint32_t dd_block_scan(uint32_t v, uint32_t* total, uint32_t* ws) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t t = lane < nw ? ws[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    ws[lane] = t;
+  }
+  __syncthreads();
+  const uint32_t r = x - v + (wid ? ws[wid - 1] : 0u);
+  *total = ws[nw - 1];
+  __syncthreads();
+  return r;
+}
 
 struct ExpandArgs {
   const uint64_t* runs;        // start << 24 | (windows - 1)
@@ -311,54 +351,169 @@ __device__ __forceinline__ uint32_t dd_digit(uint64_t h, int hi, int n) {
   return n == 0 ? 0u : (uint32_t)(h >> (64 - hi - n)) & ((1u << n) - 1u);
 }
 
-template <class K, class R, bool SCATTER>
-__global__ void __launch_bounds__(DD_THREADS) k_zi_expand(ExpandArgs a) {
+// the input of a run: largest j with input_base[j] <= start; the last answer
+// is kept, as consecutive runs of a slice mostly come from the same input
+struct InputCursor {
+  int cur = -1;
+  uint64_t lo = 0, hi = 0;
+  __device__ __forceinline__ uint16_t of(const ExpandArgs& a, uint64_t s0) {
+    if (cur < 0 || s0 < lo || s0 >= hi) {
+      int l2 = 0, h2 = a.n_inputs;
+      while (h2 - l2 > 1) { const int mid = (l2 + h2) >> 1; if (a.input_base[mid] <= s0) l2 = mid; else h2 = mid; }
+      cur = l2;
+      lo = a.input_base[l2];
+      hi = a.input_base[l2 + 1];
+    }
+    return (uint16_t)cur;
+  }
+};
+
+__device__ __forceinline__ void dd_slice(uint64_t n, uint64_t* lo, uint64_t* hi) {
+  const uint64_t per = (n + DD_CTAS - 1) / DD_CTAS;
+  *lo = min(per * blockIdx.x, n);
+  *hi = min(*lo + per, n);
+}
+
+// histogram pass: records per (level-1 bucket, CTA)
+template <class K, class R>
+__global__ void __launch_bounds__(DD_THREADS) k_zi_expand_count(ExpandArgs a) {
   __shared__ uint32_t c[DD_NB1];
   const int nb = 1 << a.bits1;
-  for (int i = threadIdx.x; i < nb; i += DD_THREADS) c[i] = SCATTER ? a.pre[(uint64_t)i * DD_CTAS + blockIdx.x] : 0u;
+  for (int i = threadIdx.x; i < nb; i += DD_THREADS) c[i] = 0u;
   __syncthreads();
-  const uint64_t per = (a.n_runs + DD_CTAS - 1) / DD_CTAS;
-  uint64_t lo = per * blockIdx.x, hi = lo + per;
-  if (hi > a.n_runs) hi = a.n_runs;
+  uint64_t lo, hi;
+  dd_slice(a.n_runs, &lo, &hi);
   const int k = a.k;
-  // the input of the previous run, kept: consecutive runs of a slice mostly
-  // come from the same input
-  int cur = -1;
-  uint64_t cur_lo = 0, cur_hi = 0;
   for (uint64_t i = lo + threadIdx.x; i < hi; i += DD_THREADS) {
     const uint64_t d = a.runs[i];
     const uint64_t s0 = d >> 24;
     const uint32_t nw = (uint32_t)(d & 0xffffffu) + 1u;
-    uint16_t ds = 0;
-    if (SCATTER && a.with_ids) {  // input of the run: largest j with input_base[j] <= s0
-      if (cur < 0 || s0 < cur_lo || s0 >= cur_hi) {
-        int l2 = 0, h2 = a.n_inputs;
-        while (h2 - l2 > 1) { const int mid = (l2 + h2) >> 1; if (a.input_base[mid] <= s0) l2 = mid; else h2 = mid; }
-        cur = l2;
-        cur_lo = a.input_base[l2];
-        cur_hi = a.input_base[l2 + 1];
-      }
-      ds = (uint16_t)cur;
-    }
     R r;
     roll_set<K, R>(r, a.packed, s0, k);
     uint64_t p = s0 + (uint64_t)k;
     for (uint32_t u = 0; u < nw; u++) {
       if (u > 0) { r.push(base_at(a.packed, p)); p++; }
-      const K key = r.canon();
-      const uint32_t b = dd_digit(key_hash(key), 0, a.bits1);
-      if (!SCATTER) {
-        atomicAdd(&c[b], 1u);
-      } else {
-        const uint32_t pos = atomicAdd(&c[b], 1u);
-        reinterpret_cast<K*>(a.keys_out)[pos] = key;
-        if (a.with_ids) a.ids_out[pos] = ds;
-      }
+      atomicAdd(&c[dd_digit(key_hash(r.canon()), 0, a.bits1)], 1u);
     }
   }
-  if (!SCATTER) {
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += DD_THREADS) a.hist[(uint64_t)i * DD_CTAS + blockIdx.x] = c[i];
+}
+
+// scatter pass over the same slices.  Per tile: the threads' runs are laid
+// out by a block scan of their window counts (the threads whose runs fit in
+// the tile are a prefix); the records are rolled once to count them per
+// bucket, once more to place them in bucket order in shared memory, and the
+// tile is written out bucket by bucket at the CTA's cursors.
+template <class K, class R>
+__global__ void __launch_bounds__(DD_THREADS) k_zi_expand_scatter(ExpandArgs a) {
+  constexpr uint32_t CAP = DdTile<K>::CAP;
+  extern __shared__ __align__(16) uint8_t smem[];
+  K* skey = reinterpret_cast<K*>(smem);
+  uint16_t* sid = reinterpret_cast<uint16_t*>(smem + (size_t)CAP * sizeof(K));
+  uint8_t* sb = reinterpret_cast<uint8_t*>(sid + CAP);
+  __shared__ uint32_t gcur[DD_NB1], gdst[DD_NB1], tcnt[DD_NB1], tstart[DD_NB1];
+  __shared__ uint32_t ws[32];
+  const int nb = 1 << a.bits1;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < nb; i += DD_THREADS) {
+    gcur[i] = a.pre[(uint64_t)i * DD_CTAS + blockIdx.x];
+    tcnt[i] = 0u;
+  }
+  uint64_t lo, hi;
+  dd_slice(a.n_runs, &lo, &hi);
+  const int k = a.k;
+  K* kout = reinterpret_cast<K*>(a.keys_out);
+  uint16_t* iout = a.with_ids ? a.ids_out : nullptr;
+  InputCursor ic;
+  __syncthreads();
+  for (uint64_t base = lo; base < hi;) {
+    const uint64_t r0 = base + (uint64_t)tid * DD_RPT;
+    uint64_t d[DD_RPT];
+    uint32_t nwt = 0;
+#pragma unroll
+    for (int q = 0; q < DD_RPT; q++) {
+      d[q] = r0 + q < hi ? a.runs[r0 + q] : ~0ull;
+      const uint32_t nw = d[q] == ~0ull ? 0u : (uint32_t)(d[q] & 0xffffffu) + 1u;
+      nwt += nw <= DD_LONG ? nw : 0u;
+    }
+    uint32_t total;
+    const uint32_t o = dd_block_scan(nwt, &total, ws);
+    const bool fit = o + nwt <= CAP;
+    const int n_fit = __syncthreads_count(fit);
+    // pass A: count the tile's records per bucket; long runs go straight out
+    if (fit) {
+#pragma unroll
+      for (int q = 0; q < DD_RPT; q++) {
+        if (d[q] == ~0ull) continue;
+        const uint64_t s0 = d[q] >> 24;
+        const uint32_t nw = (uint32_t)(d[q] & 0xffffffu) + 1u;
+        const bool lng = nw > DD_LONG;
+        const uint16_t ds = (a.with_ids && lng) ? ic.of(a, s0) : 0;
+        R r;
+        roll_set<K, R>(r, a.packed, s0, k);
+        uint64_t p = s0 + (uint64_t)k;
+        for (uint32_t u = 0; u < nw; u++) {
+          if (u > 0) { r.push(base_at(a.packed, p)); p++; }
+          const K key = r.canon();
+          const uint32_t b = dd_digit(key_hash(key), 0, a.bits1);
+          if (!lng) {
+            atomicAdd(&tcnt[b], 1u);
+          } else {
+            const uint32_t pos = atomicAdd(&gcur[b], 1u);
+            kout[pos] = key;
+            if (iout) iout[pos] = ds;
+          }
+        }
+      }
+    }
     __syncthreads();
-    for (int i = threadIdx.x; i < nb; i += DD_THREADS) a.hist[(uint64_t)i * DD_CTAS + blockIdx.x] = c[i];
+    {
+      const uint32_t v = tid < nb ? tcnt[tid] : 0u;
+      uint32_t tt;
+      const uint32_t pre = dd_block_scan(v, &tt, ws);
+      if (tid < nb) {
+        tstart[tid] = pre;
+        tcnt[tid] = pre;  // the tile cursor of pass B
+        gdst[tid] = gcur[tid];
+        gcur[tid] += v;
+      }
+      total = tt;
+    }
+    __syncthreads();
+    // pass B: place the records in bucket order
+    if (fit) {
+#pragma unroll
+      for (int q = 0; q < DD_RPT; q++) {
+        if (d[q] == ~0ull) continue;
+        const uint64_t s0 = d[q] >> 24;
+        const uint32_t nw = (uint32_t)(d[q] & 0xffffffu) + 1u;
+        if (nw > DD_LONG) continue;
+        const uint16_t ds = a.with_ids ? ic.of(a, s0) : 0;
+        R r;
+        roll_set<K, R>(r, a.packed, s0, k);
+        uint64_t p = s0 + (uint64_t)k;
+        for (uint32_t u = 0; u < nw; u++) {
+          if (u > 0) { r.push(base_at(a.packed, p)); p++; }
+          const K key = r.canon();
+          const uint32_t b = dd_digit(key_hash(key), 0, a.bits1);
+          const uint32_t pos = atomicAdd(&tcnt[b], 1u);
+          skey[pos] = key;
+          sid[pos] = ds;
+          sb[pos] = (uint8_t)b;
+        }
+      }
+    }
+    __syncthreads();
+    for (uint32_t j = tid; j < total; j += DD_THREADS) {
+      const uint32_t b = sb[j];
+      const uint32_t g = gdst[b] + (j - tstart[b]);
+      kout[g] = skey[j];
+      if (iout) iout[g] = sid[j];
+    }
+    __syncthreads();
+    for (int i = tid; i < nb; i += DD_THREADS) tcnt[i] = 0u;
+    base += (uint64_t)n_fit * DD_RPT;
   }
 }
 
@@ -377,42 +532,85 @@ struct SplitArgs {
   uint32_t* off2;              // final bucket b1 << bits2 | j, plus the total at the end
 };
 
-// one CTA per level-1 bucket: histogram by the next bits2 bits, scan, scatter
-template <class K>
+// one CTA per level-1 bucket: histogram by the next bits2 bits, scan, then
+// tiles of DDK_THREADS x E records counting-sorted in shared memory and
+// written out bucket by bucket
+template <class K, int E>
 __global__ void __launch_bounds__(DDK_THREADS) k_zi_split(SplitArgs a) {
-  __shared__ uint32_t c[DD_NB1];
+  constexpr uint32_t T = (uint32_t)DDK_THREADS * E;
+  static_assert(T <= DdTile<K>::CAP, "split tile larger than the shared-memory tile");
+  extern __shared__ __align__(16) uint8_t smem[];
+  K* skey = reinterpret_cast<K*>(smem);
+  uint16_t* sid = reinterpret_cast<uint16_t*>(smem + (size_t)T * sizeof(K));
+  uint16_t* sb = sid + T;
+  __shared__ uint32_t gcur[DD_NB2], gdst[DD_NB2], tcnt[DD_NB2], tstart[DD_NB2];
   __shared__ uint32_t ws[32];
   const int nb2 = 1 << a.bits2;
+  const int tid = threadIdx.x;
   const uint32_t b1 = blockIdx.x;
   const uint32_t lo = a.off1[b1], hi = a.off1[b1 + 1];
   const K* kin = reinterpret_cast<const K*>(a.keys_in);
-  for (int i = threadIdx.x; i < nb2; i += blockDim.x) c[i] = 0;
-  __syncthreads();
-  for (uint32_t j = lo + threadIdx.x; j < hi; j += blockDim.x)
-    atomicAdd(&c[dd_digit(key_hash(kin[j]), a.bits1, a.bits2)], 1u);
-  __syncthreads();
-  if (threadIdx.x < 32) {  // exclusive scan of <= 256 bins by one warp
-    const int lane = threadIdx.x;
-    const int per = (nb2 + 31) / 32;
-    uint32_t sum = 0;
-    for (int q = 0; q < per; q++) { const int i = lane * per + q; if (i < nb2) sum += c[i]; }
-    uint32_t x = sum;
-    for (int o = 1; o < 32; o <<= 1) { const uint32_t y = __shfl_up_sync(0xffffffffu, x, o); if (lane >= o) x += y; }
-    uint32_t run = lo + x - sum;
-    for (int q = 0; q < per; q++) {
-      const int i = lane * per + q;
-      if (i < nb2) { const uint32_t v = c[i]; c[i] = run; a.off2[(uint64_t)b1 * nb2 + i] = run; run += v; }
-    }
-    ws[lane] = 0;
-  }
-  if (b1 == gridDim.x - 1 && threadIdx.x == 0) a.off2[(uint64_t)gridDim.x * nb2] = hi;
-  __syncthreads();
   K* kout = reinterpret_cast<K*>(a.keys_out);
-  for (uint32_t j = lo + threadIdx.x; j < hi; j += blockDim.x) {
-    const K key = kin[j];
-    const uint32_t pos = atomicAdd(&c[dd_digit(key_hash(key), a.bits1, a.bits2)], 1u);
-    kout[pos] = key;
-    if (a.ids_in) a.ids_out[pos] = a.ids_in[j];
+  for (int i = tid; i < nb2; i += DDK_THREADS) { gcur[i] = 0u; tcnt[i] = 0u; }
+  __syncthreads();
+  for (uint32_t j = lo + tid; j < hi; j += DDK_THREADS)
+    atomicAdd(&gcur[dd_digit(key_hash(kin[j]), a.bits1, a.bits2)], 1u);
+  __syncthreads();
+  {
+    const uint32_t v = tid < nb2 ? gcur[tid] : 0u;
+    uint32_t tot;
+    const uint32_t pre = dd_block_scan(v, &tot, ws);
+    if (tid < nb2) {
+      gcur[tid] = lo + pre;
+      a.off2[(uint64_t)b1 * nb2 + tid] = lo + pre;
+    }
+  }
+  if (b1 == gridDim.x - 1 && tid == 0) a.off2[(uint64_t)gridDim.x * nb2] = hi;
+  __syncthreads();
+  for (uint32_t t0 = lo; t0 < hi; t0 += T) {
+    K key[E];
+    uint16_t id[E];
+    uint32_t bb[E], rk[E];
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const uint32_t j = t0 + (uint32_t)e * DDK_THREADS + tid;
+      bb[e] = 0xffffffffu;
+      if (j < hi) {
+        key[e] = kin[j];
+        id[e] = a.ids_in ? a.ids_in[j] : (uint16_t)0;
+        bb[e] = dd_digit(key_hash(key[e]), a.bits1, a.bits2);
+        rk[e] = atomicAdd(&tcnt[bb[e]], 1u);
+      }
+    }
+    __syncthreads();
+    uint32_t total;
+    {
+      const uint32_t v = tid < nb2 ? tcnt[tid] : 0u;
+      const uint32_t pre = dd_block_scan(v, &total, ws);
+      if (tid < nb2) {
+        tstart[tid] = pre;
+        gdst[tid] = gcur[tid];
+        gcur[tid] += v;
+        tcnt[tid] = 0u;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      if (bb[e] == 0xffffffffu) continue;
+      const uint32_t pos = tstart[bb[e]] + rk[e];
+      skey[pos] = key[e];
+      sid[pos] = id[e];
+      sb[pos] = (uint16_t)bb[e];
+    }
+    __syncthreads();
+    for (uint32_t j = tid; j < total; j += DDK_THREADS) {
+      const uint32_t b = sb[j];
+      const uint32_t g = gdst[b] + (j - tstart[b]);
+      kout[g] = skey[j];
+      if (a.ids_out) a.ids_out[g] = sid[j];
+    }
+    __syncthreads();
   }
 }
 
@@ -442,89 +640,124 @@ __device__ __forceinline__ K64 dd_cas(K64* p, K64 cmp, K64 val) {
 }
 __device__ __forceinline__ K128 dd_cas(K128* p, K128 cmp, K128 val) { return atomicCAS(p, cmp, val); }
 
-// exclusive block scan of one u32 per thread; ws holds 32 words
-__device__ __forceinline__ uint32_t dd_block_scan(uint32_t v, uint32_t* total, uint32_t* ws) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  uint32_t x = v;
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) ws[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    uint32_t t = lane < nw ? ws[lane] : 0u;
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
-      if (lane >= o) t += y;
-    }
-    ws[lane] = t;
-  }
-  __syncthreads();
-  const uint32_t r = x - v + (wid ? ws[wid - 1] : 0u);
-  *total = ws[nw - 1];
-  __syncthreads();
-  return r;
+// Two CTAs per SM, so one CTA's barriers overlap the other's work.  CTA c
+// takes buckets c, c + G, c + 2G, ...; a bucket's records (at most
+// dd_e<K>() per thread, the bucket size the host plans for) stay in registers
+// through its sub-rounds, and the next bucket's records are loaded while the
+// last sub-round is emitted.  Larger buckets (more than 2^17 buckets would be
+// needed) are read from global memory per sub-round.  The table starts empty
+// and every emit (or overflow) leaves it empty.
+constexpr int DDD_THREADS = 512;
+template <class K> __host__ __device__ constexpr int dd_e() { return sizeof(K) == 8 ? 8 : 4; }
+template <class K> __host__ __device__ constexpr size_t dd_keys_bytes(uint32_t slots) {
+  return ((size_t)slots * sizeof(K) + 15) & ~(size_t)15;
 }
 
 template <class K>
-__global__ void __launch_bounds__(DDK_THREADS) k_zi_bucket_dedup(BucketDedupArgs a) {
+__global__ void __launch_bounds__(DDD_THREADS, 2) k_zi_bucket_dedup(BucketDedupArgs a) {
+  constexpr int E = dd_e<K>();
   extern __shared__ __align__(16) uint8_t smem[];
   const uint32_t S = a.slots;
   const int W = a.W;
+  // table keys, W mask words per slot, and the list of occupied slots in
+  // insertion order (the emit walks only these, and writes them densely)
   K* tk = reinterpret_cast<K*>(smem);
-  unsigned long long* tm = reinterpret_cast<unsigned long long*>(smem + (((size_t)S * sizeof(K) + 15) & ~(size_t)15));
-  __shared__ uint32_t s_b, s_over;
-  __shared__ uint32_t ws[32];
+  unsigned long long* tm = reinterpret_cast<unsigned long long*>(smem + dd_keys_bytes<K>(S));
+  uint16_t* list = reinterpret_cast<uint16_t*>(smem + dd_keys_bytes<K>(S) + (size_t)S * 8 * W);
+  __shared__ uint32_t s_over, s_n;
   __shared__ unsigned long long s_base;
   const K EMPTY = key_empty<K>();
   const K* keys = reinterpret_cast<const K*>(a.keys);
   const int tid = threadIdx.x, nth = blockDim.x;
-  for (;;) {
-    __syncthreads();
-    if (tid == 0) s_b = atomicAdd(a.work, 1u);
-    __syncthreads();
-    const uint32_t b = s_b;
-    if (b >= a.n_buckets) break;
-    const uint32_t lo = a.off[b], hi = a.off[b + 1];
-    if (hi <= lo) continue;
+  const uint32_t in_regs = (uint32_t)E * (uint32_t)nth;
+  K rk[E];
+  uint16_t rd[E];
+  auto load_regs = [&](uint32_t l, uint32_t h) {
+#pragma unroll
+    for (int e = 0; e < E; e++) {
+      const uint32_t j = l + (uint32_t)e * nth + tid;
+      if (j < h) {
+        rk[e] = keys[j];
+        rd[e] = W ? a.ids[j] : (uint16_t)0;
+      }
+    }
+  };
+  // insert one record; false when its probe sequence found no room
+  auto insert = [&](const K& key, uint16_t ds, uint32_t sub_lo, uint32_t sub_hi) -> bool {
+    const uint64_t h = key_hash(key);
+    const uint32_t sub = dd_digit(h, a.bits, 20);
+    if (sub < sub_lo || sub >= sub_hi) return true;
+    uint32_t slot = (uint32_t)(((h & 0xffffffffull) * (uint64_t)S) >> 32);
+    for (uint32_t probe = 0; probe < DD_PROBE_LIMIT; probe++) {
+      K cur = tk[slot];
+      if (dd_maybe_empty(cur)) {
+        const K prev = dd_cas(&tk[slot], EMPTY, key);
+        if (key_eq(prev, EMPTY)) {
+          namespace cg = cooperative_groups;
+          cg::coalesced_group g = cg::coalesced_threads();
+          uint32_t at = 0;
+          if (g.thread_rank() == 0) at = atomicAdd(&s_n, g.size());
+          list[g.shfl(at, 0) + g.thread_rank()] = (uint16_t)slot;
+          cur = key;
+        } else {
+          cur = prev;
+        }
+      }
+      if (key_eq(cur, key)) {
+        if (W) atomicOr(&tm[(size_t)slot * W + (ds >> 6)], 1ull << (ds & 63));
+        return true;
+      }
+      slot = (slot + 1 == S) ? 0u : slot + 1;
+    }
+    return false;
+  };
+  for (uint32_t s = tid; s < S; s += nth) {
+    tk[s] = EMPTY;
+    for (int q = 0; q < W; q++) tm[(size_t)s * W + q] = 0ull;
+  }
+  if (tid == 0) s_n = 0;
+  const uint32_t G = gridDim.x, NB = a.n_buckets;
+  uint32_t b = blockIdx.x;
+  uint32_t lo = 0, hi = 0;
+  if (b < NB) {
+    lo = a.off[b];
+    hi = a.off[b + 1];
+    if (hi - lo <= in_regs) load_regs(lo, hi);
+  }
+  __syncthreads();
+  for (; b < NB; b += G) {
+    uint32_t nlo = 0, nhi = 0;
+    if (b + G < NB) {
+      nlo = a.off[b + G];
+      nhi = a.off[b + G + 1];
+    }
+    bool regs = hi - lo <= in_regs;
     // sub-rounds: at most half a table of records each (distinct <= records)
-    uint32_t r = (hi - lo + S / 2 - 1) / (S / 2);
+    uint32_t r = hi > lo ? (hi - lo + S / 2 - 1) / (S / 2) : 0u;
     uint32_t i = 0;
     while (i < r) {
       const uint32_t sub_lo = (uint32_t)(((uint64_t)i << 20) / r), sub_hi = (uint32_t)(((uint64_t)(i + 1) << 20) / r);
-      for (uint32_t s = tid; s < S; s += nth) {
-        tk[s] = EMPTY;
-        for (int q = 0; q < W; q++) tm[(size_t)s * W + q] = 0ull;
-      }
       if (tid == 0) s_over = 0;
       __syncthreads();
-      for (uint32_t j = lo + tid; j < hi; j += nth) {
-        if (*(volatile uint32_t*)&s_over) break;
-        const K key = keys[j];
-        const uint64_t h = key_hash(key);
-        const uint32_t sub = dd_digit(h, a.bits, 20);
-        if (sub < sub_lo || sub >= sub_hi) continue;
-        uint32_t slot = (uint32_t)(((h & 0xffffffffull) * (uint64_t)S) >> 32);
-        bool done = false;
-        for (uint32_t probe = 0; probe < DD_PROBE_LIMIT; probe++) {
-          K cur = tk[slot];
-          if (dd_maybe_empty(cur)) {
-            const K prev = dd_cas(&tk[slot], EMPTY, key);
-            if (key_eq(prev, EMPTY)) { done = true; break; }
-            cur = prev;
-          }
-          if (key_eq(cur, key)) { done = true; break; }
-          slot = (slot + 1 == S) ? 0u : slot + 1;
+      if (regs) {
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+          const uint32_t j = lo + (uint32_t)e * nth + tid;
+          if (j < hi && !insert(rk[e], rd[e], sub_lo, sub_hi)) s_over = 1;
         }
-        if (!done) { s_over = 1; break; }
-        if (W) {
-          const uint32_t ds = a.ids[j];
-          atomicOr(&tm[(size_t)slot * W + (ds >> 6)], 1ull << (ds & 63));
+      } else {
+        for (uint32_t j = lo + tid; j < hi; j += nth) {
+          if (*(volatile uint32_t*)&s_over) break;
+          if (!insert(keys[j], W ? a.ids[j] : (uint16_t)0, sub_lo, sub_hi)) { s_over = 1; break; }
         }
       }
       __syncthreads();
+      const uint32_t n = s_n;
       if (s_over) {
+        for (uint32_t s = tid; s < S; s += nth) {
+          tk[s] = EMPTY;
+          for (int q = 0; q < W; q++) tm[(size_t)s * W + q] = 0ull;
+        }
         // this sub-range becomes two: sub-round i of r is sub-rounds 2i, 2i+1 of 2r
         if (r >= (1u << 20)) {
           if (tid == 0) set_status(a.status, ST_TABLE_STUCK);
@@ -533,29 +766,34 @@ __global__ void __launch_bounds__(DDK_THREADS) k_zi_bucket_dedup(BucketDedupArgs
           r *= 2;
           i *= 2;
         }
+        __syncthreads();
+        if (tid == 0) s_n = 0;
         continue;
       }
-      // emit: one global atomic per sub-round
-      uint32_t mine = 0;
-      for (uint32_t s = tid; s < S; s += nth) mine += key_eq(tk[s], EMPTY) ? 0u : 1u;
-      uint32_t tot;
-      const uint32_t off = dd_block_scan(mine, &tot, ws);
-      if (tid == 0) s_base = atomicAdd(a.n_out, (unsigned long long)tot);
+      if (i + 1 == r) {  // this bucket's records are done with: load the next bucket's
+        regs = false;
+        if (nhi - nlo <= in_regs) load_regs(nlo, nhi);
+      }
+      // emit the listed slots densely (one global atomic per sub-round) and reset them
+      if (tid == 0) s_base = atomicAdd(a.n_out, (unsigned long long)n);
       __syncthreads();
-      unsigned long long o = s_base + off;
-      for (uint32_t s = tid; s < S; s += nth) {
-        const K key = tk[s];
-        if (key_eq(key, EMPTY)) continue;
-        if (o < a.cap) {
-          uint32_t c = 1;
-          if (W) {
-            c = 0;
-            for (int q = 0; q < W; q++) {
-              const unsigned long long m = tm[(size_t)s * W + q];
-              a.out_mask[o * (uint64_t)W + q] = m;
-              c += __popcll(m);
-            }
+      const unsigned long long base = s_base;
+      for (uint32_t t = tid; t < n; t += nth) {
+        const uint32_t slot = list[t];
+        const K key = tk[slot];
+        tk[slot] = EMPTY;
+        const unsigned long long o = base + t;
+        uint32_t c = 1;
+        if (W) {
+          c = 0;
+          for (int q = 0; q < W; q++) {
+            const unsigned long long m = tm[(size_t)slot * W + q];
+            tm[(size_t)slot * W + q] = 0ull;
+            if (o < a.cap) a.out_mask[o * (uint64_t)W + q] = m;
+            c += __popcll(m);
           }
+        }
+        if (o < a.cap) {
           if constexpr (sizeof(K) == 8) {
             a.out_lo[o] = reinterpret_cast<const K64&>(key).v;
           } else {
@@ -566,10 +804,14 @@ __global__ void __launch_bounds__(DDK_THREADS) k_zi_bucket_dedup(BucketDedupArgs
         } else {
           set_status(a.status, ST_OUT_OVERFLOW);
         }
-        o++;
       }
+      if (tid == 0) s_n = 0;  // every thread read n before the barrier above
+      __syncthreads();
       i++;
     }
+    if (r == 0 && nhi - nlo <= in_regs) load_regs(nlo, nhi);
+    lo = nlo;
+    hi = nhi;
   }
 }
 
@@ -800,17 +1042,22 @@ int32_t zi_dedup(mczi_ctx* ctx, Pipe& p, bool per_input, uint64_t absent_w, uint
   CK(cudaEventRecord(ctx->ev[2], s));
   const size_t keyb = wide ? 16 : 8;
   // dedup table: one CTA of 1024 threads per SM with the largest table that fits
-  const size_t slotb = keyb + 8 * (size_t)W;
+  const size_t slotb = keyb + 8 * (size_t)W + 2;  // key, masks, list entry
   cudaFuncAttributes fa{};
   if (wide) cudaFuncGetAttributes(&fa, k_zi_bucket_dedup<K128>);
   else cudaFuncGetAttributes(&fa, k_zi_bucket_dedup<K64>);
-  const size_t budget = std::min((size_t)ctx->smem_optin, (size_t)(227 * 1024)) - fa.sharedSizeBytes - 64;
-  const uint32_t slots = (uint32_t)std::min<size_t>((budget - 16) / slotb, 1u << 20);
+  // two CTAs per SM
+  const size_t per_cta = std::min((size_t)ctx->smem_optin, ctx->smem_per_sm / 2 - ctx->smem_reserved);
+  const size_t budget = per_cta - fa.sharedSizeBytes - 64;
+  // at most twice the records a CTA keeps in registers (the planned bucket size is half a table)
+  const size_t reg_records = (size_t)DDD_THREADS * (wide ? dd_e<K128>() : dd_e<K64>());
+  const uint32_t slots = (uint32_t)std::min<size_t>(std::min<size_t>((budget - 16) / slotb, 2 * reg_records), 1u << 20);
   if (slots < 2048) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "too many inputs for the ZI dedup table");
-  const size_t smem = (((size_t)slots * keyb + 15) & ~(size_t)15) + (size_t)slots * 8 * W;
-  // final buckets of about half a table each, in one or two levels of <= 8 bits
+  const size_t smem = (((size_t)slots * keyb + 15) & ~(size_t)15) + (size_t)slots * 8 * W + (size_t)slots * 2;
+  // final buckets of about half a table each, in one level (<= 8 bits) or two (<= 8 + 9)
+  const uint64_t per_bucket = ctx->zi_bucket_records ? std::min<uint64_t>(ctx->zi_bucket_records, slots / 2) : slots / 2;
   int bits = 0;
-  while (bits < 16 && ((uint64_t)slots / 2) << bits < absent_w) bits++;
+  while (bits < DD_MAX_BITS && per_bucket << bits < absent_w) bits++;
   const int bits1 = std::min(bits, DD_MAX_BITS1), bits2 = bits - bits1;
   const uint32_t nb1 = 1u << bits1, nbf = 1u << bits;
   const uint64_t nh = (uint64_t)nb1 * DD_CTAS;
@@ -848,11 +1095,18 @@ int32_t zi_dedup(mczi_ctx* ctx, Pipe& p, bool per_input, uint64_t absent_w, uint
   ea.pre = pre;
   ea.keys_out = ctx->zi_tmp1.p;
   ea.ids_out = W ? ctx->zi_tmp2.as<uint16_t>() : nullptr;
-  if (wide) k_zi_expand<K128, Roll128, false><<<DD_CTAS, DD_THREADS, 0, s>>>(ea);
-  else k_zi_expand<K64, Roll64, false><<<DD_CTAS, DD_THREADS, 0, s>>>(ea);
+  if (wide) k_zi_expand_count<K128, Roll128><<<DD_CTAS, DD_THREADS, 0, s>>>(ea);
+  else k_zi_expand_count<K64, Roll64><<<DD_CTAS, DD_THREADS, 0, s>>>(ea);
   exclusive_scan<uint32_t, SumU32>(hist, pre, nh, tmp, s);
-  if (wide) k_zi_expand<K128, Roll128, true><<<DD_CTAS, DD_THREADS, 0, s>>>(ea);
-  else k_zi_expand<K64, Roll64, true><<<DD_CTAS, DD_THREADS, 0, s>>>(ea);
+  if (wide) {
+    CK(cudaFuncSetAttribute(k_zi_expand_scatter<K128, Roll128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)dd_tile_bytes<K128>()));
+    k_zi_expand_scatter<K128, Roll128><<<DD_CTAS, DD_THREADS, dd_tile_bytes<K128>(), s>>>(ea);
+  } else {
+    CK(cudaFuncSetAttribute(k_zi_expand_scatter<K64, Roll64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)dd_tile_bytes<K64>()));
+    k_zi_expand_scatter<K64, Roll64><<<DD_CTAS, DD_THREADS, dd_tile_bytes<K64>(), s>>>(ea);
+  }
   k_zi_off1<<<1, 256, 0, s>>>(pre, (int)nb1, bits2 ? off1 : offf);
   const void* dkeys = ctx->zi_tmp1.p;
   const uint16_t* dids = W ? ctx->zi_tmp2.as<uint16_t>() : nullptr;
@@ -867,8 +1121,15 @@ int32_t zi_dedup(mczi_ctx* ctx, Pipe& p, bool per_input, uint64_t absent_w, uint
     sa.keys_out = ctx->zi_tmp3.p;
     sa.ids_out = W ? ctx->zi_tmp4.as<uint16_t>() : nullptr;
     sa.off2 = offf;
-    if (wide) k_zi_split<K128><<<nb1, DDK_THREADS, 0, s>>>(sa);
-    else k_zi_split<K64><<<nb1, DDK_THREADS, 0, s>>>(sa);
+    if (wide) {
+      CK(cudaFuncSetAttribute(k_zi_split<K128, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)dd_split_tile_bytes<K128>()));
+      k_zi_split<K128, 4><<<nb1, DDK_THREADS, dd_split_tile_bytes<K128>(), s>>>(sa);
+    } else {
+      CK(cudaFuncSetAttribute(k_zi_split<K64, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)dd_split_tile_bytes<K64>()));
+      k_zi_split<K64, 8><<<nb1, DDK_THREADS, dd_split_tile_bytes<K64>(), s>>>(sa);
+    }
     dkeys = ctx->zi_tmp3.p;
     dids = W ? ctx->zi_tmp4.as<uint16_t>() : nullptr;
     p.launches += 1;
@@ -891,13 +1152,13 @@ int32_t zi_dedup(mczi_ctx* ctx, Pipe& p, bool per_input, uint64_t absent_w, uint
   da.n_out = reinterpret_cast<unsigned long long*>(sc + SC_NOUT);
   da.cap = cap;
   da.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
-  const unsigned grid = (unsigned)std::min<uint32_t>(nbf, (uint32_t)ctx->sm_count);
+  const unsigned grid = (unsigned)std::min<uint32_t>(nbf, (uint32_t)ctx->sm_count * 2);
   if (wide) {
     cudaFuncSetAttribute(k_zi_bucket_dedup<K128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_zi_bucket_dedup<K128><<<grid, DDK_THREADS, smem, s>>>(da);
+    k_zi_bucket_dedup<K128><<<grid, DDD_THREADS, smem, s>>>(da);
   } else {
     cudaFuncSetAttribute(k_zi_bucket_dedup<K64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    k_zi_bucket_dedup<K64><<<grid, DDK_THREADS, smem, s>>>(da);
+    k_zi_bucket_dedup<K64><<<grid, DDD_THREADS, smem, s>>>(da);
   }
   p.launches += 1;
   CK(cudaGetLastError());

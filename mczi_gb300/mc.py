@@ -226,6 +226,11 @@ class Context:
         (default on; segment_bytes a multiple of 8192, 0 = automatic)."""
         self._ck(self._lib.mczi_set_streamed_staging(self._h, 1 if enable else 0, segment_bytes))
 
+    def set_zi_bucket_records(self, records: int = 0) -> None:
+        """Records per final bucket of the ZI deduplication (0 = automatic,
+        half a shared-memory table); smaller values only add partition work."""
+        self._ck(self._lib.mczi_set_zi_bucket_records(self._h, records))
+
     def set_minimizer_precount(self, enable: bool) -> None:
         self._ck(self._lib.mczi_set_minimizer_precount(self._h, 1 if enable else 0))
 

@@ -91,6 +91,49 @@ def test_zi_per_input_equals_alone(gpu_ctx, oracle):
         assert alone[i] == oracle_absent(oracle, b">g\n" + g + b"\n", [r], 31)
 
 
+@pytest.mark.parametrize("bucket", [0, 16, 1])
+@pytest.mark.parametrize("k,m", [(31, 19), (31, 7), (33, 19), (63, 11)])
+def test_zi_partition_paths(gpu_ctx, oracle, k, m, bucket):
+    """Absent runs longer than a tile's per-run limit (low-complexity reads,
+    where one minimizer value spans a whole scan tile), expand tiles that
+    overflow (long superkmers: small m), and the two-level bucket split (small
+    final buckets) all give the oracle's sets, for the union and per input."""
+    from mczi_gb300 import zi
+    rng = np.random.default_rng(k * 7 + m + bucket)
+    g = rand_seq(rng, 30000)
+    index = b">g\n" + g + b"\n"
+    low = b">a\n" + b"A" * 3000 + b"\n>c\n" + b"AC" * 1500 + b"\n>t\n" + b"ACGTTGCA" * 300 + b"\n"
+    qs = [reads(rng, g, 200, 150, 0.01), reads(rng, rand_seq(rng, 6000), 150, 150, 0.0), low,
+          low + reads(rng, g, 50, 150, 0.02)]
+    gpu_ctx.set_zi_bucket_records(bucket)
+    try:
+        zi.build_dictionary(index, k, m, ctx=gpu_ctx)
+        assert zi.collect_query_kmers_absent_from_index(gpu_ctx, qs).encoded() == oracle_absent(oracle, index, qs, k)
+        zi.query_per_input(gpu_ctx, qs)
+        for i, q in enumerate(qs):
+            assert zi.input_result(gpu_ctx, i) == oracle_absent(oracle, index, [q], k), i
+    finally:
+        gpu_ctx.set_zi_bucket_records(0)
+
+
+def test_zi_widest_split(gpu_ctx, oracle):
+    """2^17 final buckets (8 + 9 bits) from about 3 M absent windows."""
+    from mczi_gb300 import zi
+    rng = np.random.default_rng(77)
+    g = rand_seq(rng, 50000)
+    index = b">g\n" + g + b"\n"
+    qs = [reads(rng, rand_seq(rng, 400000), 5000, 150, 0.01) for _ in range(4)] + [reads(rng, g, 500, 150, 0.01)]
+    gpu_ctx.set_zi_bucket_records(16)
+    try:
+        zi.build_dictionary(index, 31, 19, ctx=gpu_ctx)
+        assert zi.collect_query_kmers_absent_from_index(gpu_ctx, qs).encoded() == oracle_absent(oracle, index, qs, 31)
+        zi.query_per_input(gpu_ctx, qs)
+        for i, q in enumerate(qs):
+            assert zi.input_result(gpu_ctx, i) == oracle_absent(oracle, index, [q], 31), i
+    finally:
+        gpu_ctx.set_zi_bucket_records(0)
+
+
 def test_zi_fasta_output(gpu_ctx, oracle, tmp_path):
     from mczi_gb300 import zi
     rng = np.random.default_rng(9)
