@@ -118,8 +118,10 @@ int32_t mczi_count_datasets_to_fasta_path(mczi_ctx* ctx, const char* const* inpu
  * the context's stream: [0] pack, [1] minimizer scan, [2] partition,
  * [3] k-mer counting, [4] minimizer pre-count (0 when not run).  After a
  * streamed mczi_count, [0] spans the overlapped staging + pack + scan and
- * [1] only a rescan, if one was needed.  Returns the number of phases
- * written. */
+ * [1] only a rescan, if one was needed.  After a ZI query: [0] pack, [1] scan,
+ * [2] partition of the absent windows, [3] their deduplication, [4] probe; a
+ * query of at least 64 MiB of text is streamed like mczi_count ([0] then
+ * spans staging + pack + scan).  Returns the number of phases written. */
 int32_t mczi_phase_times(mczi_ctx* ctx, float* ms, int32_t cap);
 /* Statistics of the last run: [0] bases, [1] superkmers, [2] counting rounds,
  * [3] round splits, [4] distinct k-mers inserted, [5] kept records,

@@ -225,6 +225,14 @@ int32_t stage_layout(mczi_ctx* ctx, const InputPlan& pl, size_t n);
 int32_t copy_text_range(mczi_ctx* ctx, const mczi_input* inputs, size_t n, const InputPlan& pl, uint64_t b0,
                         uint64_t b1, cudaStream_t s);
 int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n);
+// Streamed staging: the text (laid out by stage_layout) is copied in segments
+// on the copy stream while earlier segments are packed and scanned (one
+// key-range pass) on the context stream.  Returns with the inputs staged and
+// packed and the superkmers in (desc, key), or with *overflow set when they
+// did not fit (then pipe_scan redoes the scan).
+bool streamed_worthwhile(const mczi_ctx* ctx, const InputPlan& pl);
+int32_t stream_pack_scan(mczi_ctx* ctx, const mczi_input* inputs, size_t n, const InputPlan& pl, int k, int m,
+                         Pipe& p, bool* overflow);
 // simplitig.cu: extension table of n sorted distinct keys (lo, hi host arrays)
 // into ext_host (n x SIMPLITIG_STRIDE words; see host_io.h)
 int32_t simplitig_extensions(mczi_ctx* ctx, const uint64_t* lo, const uint64_t* hi, uint64_t n, int k,

@@ -603,31 +603,20 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
 // rest of the pipeline is run_count's.  Inputs that need several key-range
 // passes, the minimizer pre-count or no device work at all take the plain
 // path (stage, then count).
-int32_t run_count_streamed(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, const mczi_input* inputs,
-                           size_t n, uint64_t* n_records) {
+}  // namespace
+
+// segments of >= 32 MiB of text (4096 pack tiles) unless set
+static uint64_t stream_seg_min(const mczi_ctx* ctx) { return ctx->stream_seg_tiles > 0 ? ctx->stream_seg_tiles : 4096; }
+
+bool streamed_worthwhile(const mczi_ctx* ctx, const InputPlan& pl) {
+  return ctx->streamed && pl.n_tiles >= 2 * stream_seg_min(ctx);
+}
+
+int32_t stream_pack_scan(mczi_ctx* ctx, const mczi_input* inputs, size_t n, const InputPlan& pl, int k, int m,
+                         Pipe& p, bool* overflow) {
   int32_t rc;
-  InputPlan pl;
-  if ((rc = plan_inputs(ctx, inputs, n, pl))) return rc;
-  if ((rc = stage_layout(ctx, pl, n))) return rc;
-  ctx->mask_words = 0;
-  const int k = (int)cfg->k, m = (int)cfg->minimizer;
-  const uint32_t passes = key_range_passes(ctx, k, m, 0);
-  // segments of >= 32 MiB of text, about 16 per batch
-  const uint64_t seg_min = ctx->stream_seg_tiles > 0 ? ctx->stream_seg_tiles : 4096;
-  // the text-length estimate over-counts bases (headers, line breaks): up to
-  // two estimated passes are tried as one, with the plain path as fallback
-  const bool plain = passes > 2 || ctx->precount || !ctx->streamed || pl.n_tiles < 2 * seg_min ||
-                     (mode == MCZI_MODE_PRESENCE && cfg->threshold >= (uint64_t)n);
-  if (plain) {
-    if ((rc = copy_text_range(ctx, inputs, n, pl, 0, pl.text_len, ctx->stream))) return rc;
-    CK(cudaStreamSynchronize(ctx->stream));
-    ctx->staged = true;
-    return run_count(ctx, cfg, mode, n_records);
-  }
+  *overflow = false;
   cudaStream_t s = ctx->stream, cs = ctx->copy_stream;
-  for (int i = 0; i < N_PHASES; i++) ctx->phase_ms[i] = 0.f;
-  Pipe p;
-  std::memset(ctx->stats, 0, sizeof ctx->stats);
   PackArgs pa;
   if ((rc = pack_prepare(ctx, p, pa))) return rc;
   // scan buffers, as pipe_scan sizes them
@@ -667,8 +656,9 @@ int32_t run_count_streamed(mczi_ctx* ctx, const mczi_counter_config* cfg, int mo
   CK(cudaStreamWaitEvent(cs, ctx->ev_copy, 0));
   CK(cudaEventRecord(ctx->ev[0], s));
   const uint64_t nseg_target = 16;
-  const uint64_t seg = ctx->stream_seg_tiles > 0 ? ctx->stream_seg_tiles
-                                                 : std::max<uint64_t>(seg_min, (pl.n_tiles + nseg_target - 1) / nseg_target);
+  const uint64_t seg = ctx->stream_seg_tiles > 0
+                           ? ctx->stream_seg_tiles
+                           : std::max<uint64_t>(stream_seg_min(ctx), (pl.n_tiles + nseg_target - 1) / nseg_target);
   for (uint64_t t0 = 0; t0 < pl.n_tiles; t0 += seg) {
     const uint64_t t1 = std::min(pl.n_tiles, t0 + seg);
     const bool last = t1 == pl.n_tiles;
@@ -694,14 +684,44 @@ int32_t run_count_streamed(mczi_ctx* ctx, const mczi_counter_config* cfg, int mo
   CK(cudaMemcpyAsync(h + 1, sc + SC_STATUS, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (h[1] & ST_DESC_OVERFLOW) {
-    // more superkmers than the streamed pass holds: the inputs are staged,
-    // so the plain path (which sizes its passes from the packed bases) redoes it
-    return run_count(ctx, cfg, mode, n_records);
-  } else {
-    p.n_desc = h[0];
-    p.desc_cap = desc_cap;
-    ctx->cap_desc = std::max(ctx->cap_desc, desc_cap);
+    *overflow = true;
+    return MCZI_OK;
   }
+  p.n_desc = h[0];
+  p.desc_cap = desc_cap;
+  ctx->cap_desc = std::max(ctx->cap_desc, desc_cap);
+  return MCZI_OK;
+}
+
+namespace {
+
+int32_t run_count_streamed(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, const mczi_input* inputs,
+                           size_t n, uint64_t* n_records) {
+  int32_t rc;
+  InputPlan pl;
+  if ((rc = plan_inputs(ctx, inputs, n, pl))) return rc;
+  if ((rc = stage_layout(ctx, pl, n))) return rc;
+  ctx->mask_words = 0;
+  const int k = (int)cfg->k, m = (int)cfg->minimizer;
+  const uint32_t passes = key_range_passes(ctx, k, m, 0);
+  // the text-length estimate over-counts bases (headers, line breaks): up to
+  // two estimated passes are tried as one, with the plain path as fallback
+  const bool plain = passes > 2 || ctx->precount || !streamed_worthwhile(ctx, pl) ||
+                     (mode == MCZI_MODE_PRESENCE && cfg->threshold >= (uint64_t)n);
+  if (plain) {
+    if ((rc = copy_text_range(ctx, inputs, n, pl, 0, pl.text_len, ctx->stream))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->staged = true;
+    return run_count(ctx, cfg, mode, n_records);
+  }
+  for (int i = 0; i < N_PHASES; i++) ctx->phase_ms[i] = 0.f;
+  Pipe p;
+  std::memset(ctx->stats, 0, sizeof ctx->stats);
+  bool overflow = false;
+  if ((rc = stream_pack_scan(ctx, inputs, n, pl, k, m, p, &overflow))) return rc;
+  // more superkmers than the streamed pass holds: the inputs are staged, so
+  // the plain path (which sizes its passes from the packed bases) redoes it
+  if (overflow) return run_count(ctx, cfg, mode, n_records);
   uint64_t n_out = 0;
   if ((rc = pipe_partition(ctx, p))) return rc;
   if ((rc = pipe_count(ctx, p, k, cfg->threshold, mode, false, &n_out, false))) return rc;

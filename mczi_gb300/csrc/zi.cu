@@ -1179,15 +1179,26 @@ int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, u
   if (!z.built) return fail(ctx, MCZI_ERR_STATE, "no ZI index: call mczi_zi_build first");
   int32_t rc;
   if (n == 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "at least one query FASTA is required");
-  if ((rc = stage_inputs(ctx, q, n))) return rc;
+  InputPlan pl;
+  if ((rc = plan_inputs(ctx, q, n, pl))) return rc;
+  if ((rc = stage_layout(ctx, pl, n))) return rc;
   ctx->have_result = false;
   ctx->mask_words = 0;
   for (int i = 0; i < N_PHASES; i++) ctx->phase_ms[i] = 0.f;
   std::memset(ctx->stats, 0, sizeof ctx->stats);
   cudaStream_t s = ctx->stream;
   Pipe p;
-  if ((rc = pipe_pack(ctx, p))) return rc;
-  if ((rc = pipe_scan(ctx, p, z.k, z.m))) return rc;
+  if (streamed_worthwhile(ctx, pl)) {  // the copy overlaps the pack and the scan
+    bool overflow = false;
+    if ((rc = stream_pack_scan(ctx, q, n, pl, z.k, z.m, p, &overflow))) return rc;
+    if (overflow && (rc = pipe_scan(ctx, p, z.k, z.m))) return rc;
+  } else {
+    if ((rc = copy_text_range(ctx, q, n, pl, 0, pl.text_len, s))) return rc;
+    CK(cudaStreamSynchronize(s));
+    ctx->staged = true;
+    if ((rc = pipe_pack(ctx, p))) return rc;
+    if ((rc = pipe_scan(ctx, p, z.k, z.m))) return rc;
+  }
   const uint64_t n_query_sk = p.n_desc;
   uint64_t* sc = ctx->scalars.as<uint64_t>();
   // probe: absent-window runs into (desc2, key2)

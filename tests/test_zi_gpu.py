@@ -116,6 +116,27 @@ def test_zi_partition_paths(gpu_ctx, oracle, k, m, bucket):
         gpu_ctx.set_zi_bucket_records(0)
 
 
+@pytest.mark.parametrize("seg", [8192, 3 * 8192])
+def test_zi_streamed_staging(gpu_ctx, oracle, seg):
+    """Queries copied in segments while earlier segments are packed and
+    scanned give the same absent sets, for the union and per input."""
+    from mczi_gb300 import zi
+    rng = np.random.default_rng(seg)
+    g = rand_seq(rng, 40000)
+    index = b">g\n" + g + b"\n"
+    qs = [reads(rng, g, 300, 150, 0.01), reads(rng, rand_seq(rng, 20000), 400, 150, 0.01),
+          b">n\nNNNNACGTNN\n>s\nAC\n", reads(rng, g, 200, 150, 0.02)]
+    gpu_ctx.set_streamed_staging(True, seg)
+    try:
+        zi.build_dictionary(index, 31, 19, ctx=gpu_ctx)
+        assert zi.collect_query_kmers_absent_from_index(gpu_ctx, qs).encoded() == oracle_absent(oracle, index, qs, 31)
+        zi.query_per_input(gpu_ctx, qs)
+        for i, q in enumerate(qs):
+            assert zi.input_result(gpu_ctx, i) == oracle_absent(oracle, index, [q], 31), i
+    finally:
+        gpu_ctx.set_streamed_staging(True, 0)
+
+
 def test_zi_widest_split(gpu_ctx, oracle):
     """2^17 final buckets (8 + 9 bits) from about 3 M absent windows."""
     from mczi_gb300 import zi
