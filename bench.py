@@ -552,9 +552,11 @@ def run_zi(args):
 
 
 def run_zi_serve(args):
-    """ZI serving: the index stays resident; requests of log-uniform size
-    (10 kbp .. max) arrive as a Poisson process at offered loads 0.2 .. 1.0 of
-    the measured batched peak; p50/p99 latency and aggregate lookups/s."""
+    """ZI serving through the library's native loop (mczi_serve_*): the index
+    stays resident; requests of log-uniform size (10 kbp .. 200 Mbp, sliced
+    from a pool of reads) arrive as a Poisson process at offered loads
+    0.2 .. 1.0 of the measured batched peak; p50/p99 latency (submit to
+    result) and aggregate bases/s."""
     import numpy as np
     from mczi_gb300 import build, gen, zi
     from mczi_gb300.mc import Context
@@ -587,6 +589,7 @@ def run_zi_serve(args):
     points = []
     with ZIServer(index, k, m, workers=args.serve_workers, max_batch=64) as srv:
         for load in (0.2, 0.4, 0.6, 0.8, 1.0):
+            st0 = srv.stats()
             reqs = [make_request() for _ in range(args.serve_requests)]
             mean = sum(len(r) for r in reqs) / len(reqs)
             rate = load * peak_bps / mean
@@ -601,14 +604,16 @@ def run_zi_serve(args):
             for f in futs:
                 f.result()
             t_end = time.perf_counter()
-            lat = [(f.request.finished - f.request.arrival) * 1e3 for f in futs]
-            win = sum(max(0, len(r) - 2 * (len(r) // 157)) for r in reqs)  # ~bases; lookups ~ bases
+            st1 = srv.stats()
+            lat = [f.latency_ms for f in futs]  # submit to result, timed by the native server
+            nb = st1["batches"] - st0["batches"]
             points.append({"offered_load": load, "requests": len(reqs), "p50_ms": round(percentile(lat, 50), 3),
                            "p99_ms": round(percentile(lat, 99), 3),
+                           "queue_p99_ms": round(percentile([f.queue_ms for f in futs], 99), 3),
                            "throughput_bases_per_s": round(sum(len(r) for r in reqs) / (t_end - t_start), 1),
-                           "mean_batch": round(float(np.mean(srv.batch_sizes[-50:])), 2),
-                           "batches": srv.batches, "query_s_total": round(srv.t_query, 3),
-                           "results_s_total": round(srv.t_results, 3)})
+                           "mean_batch": round((st1["requests"] - st0["requests"]) / max(1, nb), 2),
+                           "batches": int(nb), "query_s": round(st1["query_s"] - st0["query_s"], 3),
+                           "results_s": round(st1["results_s"] - st0["results_s"], 3)})
     line = {"metric": "ZI-serve p99 ms", "value": points[-1]["p99_ms"], "unit": "ms", "impl": "ours",
             "higher_is_better": False, "n_gpus": 1,
             "config": {"workload": "zi_serve_k31", "index_genome_bp": glen, "workers": args.serve_workers,
@@ -634,8 +639,8 @@ def main():
     ap.add_argument("--zi-files", type=int, default=200)
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-workers", type=int, default=2)
-    ap.add_argument("--serve-max-bytes", type=float, default=20e6)
-    ap.add_argument("--serve-pool-bases", type=float, default=400e6)
+    ap.add_argument("--serve-max-bytes", type=float, default=200e6)
+    ap.add_argument("--serve-pool-bases", type=float, default=600e6)
     args = ap.parse_args()
     if args.workload == "zi" and args.impl == "ours":
         return run_zi(args)

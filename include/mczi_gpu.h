@@ -230,6 +230,56 @@ int32_t mczi_zi_info(mczi_ctx* ctx, uint64_t* out, int32_t cap);
  * Smaller values only add partition work; results are identical. */
 int32_t mczi_set_zi_bucket_records(mczi_ctx* ctx, uint32_t records);
 
+/* ------------------------------------------------------------- ZI serving */
+
+/* A resident ZI dictionary answering subtraction requests with continuous
+ * batching (no counterpart in the reference: ZI is a one-shot CLI,
+ * src/zi.rs:64-101).  `workers` host threads each own a context (its own
+ * stream and buffers) holding the dictionary of `index_fasta`, built at open
+ * (src/zi.rs:114-141 semantics).  Whenever a worker is idle it takes every
+ * waiting request that fits -- at most `max_batch` requests and at most its
+ * share of `hbm_budget` bytes of device memory (0 = 60 % of the free memory
+ * at open), estimated at 8 device bytes per query byte; a larger request runs
+ * alone -- and answers them with one mczi_zi_query_per_input, so each request
+ * gets exactly the absent set it gets alone.  Batches of different workers
+ * overlap on the device. */
+typedef struct mczi_server mczi_server;
+
+int32_t mczi_serve_open(int32_t device, const uint8_t* index_fasta, uint64_t len, uint32_t k, uint32_t m,
+                        int32_t workers, int32_t max_batch, uint64_t hbm_budget, mczi_server** out);
+
+/* Queues one query FASTA.  The bytes are not copied: they must stay valid and
+ * unchanged until mczi_serve_next has reported the request. */
+int32_t mczi_serve_submit(mczi_server* srv, const uint8_t* query_fasta, uint64_t len, uint64_t* request_id);
+
+/* Waits up to timeout_ms (< 0: no limit) for the next finished request and
+ * reports its id, its status (MCZI_OK or the failing call's code), the size of
+ * its absent set, its latency (submit to result) and its time in the queue.
+ * Returns MCZI_ERR_TIMEOUT when none finished in time. */
+int32_t mczi_serve_next(mczi_server* srv, int32_t timeout_ms, uint64_t* request_id, int32_t* status,
+                        uint64_t* n_kmers, double* latency_ms, double* queue_ms);
+
+/* Copies a reported request's absent canonical k-mers (a set, in no
+ * particular order; key_hi may be NULL for k <= 32) and releases the request.
+ * With key_lo == NULL only *n is set and the request is kept.  A failed
+ * request returns its status (and is released when key_lo is not NULL);
+ * mczi_serve_error gives its message until then. */
+int32_t mczi_serve_result(mczi_server* srv, uint64_t request_id, uint64_t* key_lo, uint64_t* key_hi, uint64_t cap,
+                          uint64_t* n);
+/* mczi_serve_error(NULL, 0) gives the message of this thread's last failed
+ * mczi_serve_open. */
+const char* mczi_serve_error(mczi_server* srv, uint64_t request_id);
+
+/* Counters: [0] batches, [1] requests answered, [2] largest batch, [3] seconds
+ * in mczi_zi_query_per_input, [4] seconds splitting batch results, [5]
+ * requests waiting, [6] admitted query bytes per worker.  Returns the number
+ * written. */
+int32_t mczi_serve_stats(mczi_server* srv, double* out, int32_t cap);
+
+/* Stops accepting requests, lets the workers finish the queued ones, joins
+ * them and frees everything (results not yet copied are dropped). */
+int32_t mczi_serve_close(mczi_server* srv);
+
 /* ------------------------------------------------ packing without allocation */
 
 /* The 2-bit packer of mczi_count's first phase, for callers that cannot

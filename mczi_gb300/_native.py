@@ -94,6 +94,16 @@ SIGNATURES = [
     ("mczi_zi_info", C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64), C.c_int32]),
     ("mczi_pack_fastx_noalloc", C.c_int32, [C.c_void_p, C.c_uint64, C.c_int32, C.c_void_p, C.c_uint64, C.c_void_p,
                                             C.c_uint64, C.POINTER(C.c_uint64), C.c_void_p]),
+    ("mczi_serve_open", C.c_int32, [C.c_int32, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_int32, C.c_int32,
+                                    C.c_uint64, C.POINTER(C.c_void_p)]),
+    ("mczi_serve_submit", C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    ("mczi_serve_next", C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_uint64), C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("mczi_serve_result", C.c_int32, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint64,
+                                      C.POINTER(C.c_uint64)]),
+    ("mczi_serve_error", C.c_char_p, [C.c_void_p, C.c_uint64]),
+    ("mczi_serve_stats", C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int32]),
+    ("mczi_serve_close", C.c_int32, [C.c_void_p]),
 ]
 
 _lib = None

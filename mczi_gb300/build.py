@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-fsigne
               "-I", str(ROOT / "include")] + ARCH
 CUDA_SOURCES = ["mc_pack.cu", "mc_scan.cu", "mc_partition.cu", "mc_count.cu", "mczi_api.cu", "zi.cu",
                 "mc_pack_noalloc.cu", "mc_precount.cu", "simplitig.cu"]
-CXX_SOURCES = ["host_io.cpp"]
+CXX_SOURCES = ["host_io.cpp", "serve.cpp"]
 
 
 def nvcc() -> str:

@@ -50,6 +50,28 @@ def test_no_device_fails_loudly(lib):
     from mczi_gb300.mc import Context
     with pytest.raises(_native.MCZIError):
         Context(0)
+    # the native serving loop opens its worker contexts the same way
+    srv = C.c_void_p()
+    idx = b">i\nACGTACGTACGTACGT\n"
+    assert lib.mczi_serve_open(0, idx, len(idx), 5, 3, 1, 4, 0, C.byref(srv)) == _native.MCZI_ERR_DEVICE
+    assert not srv.value
+    assert lib.mczi_serve_error(None, 0) == b"no usable CUDA device"
+    from mczi_gb300.serve import ZIServer
+    with pytest.raises(_native.MCZIError):
+        ZIServer(idx, 5, 3, workers=1)
+
+
+def test_serve_open_validates_before_device_work(lib):
+    import ctypes as C
+    from mczi_gb300 import _native
+    srv = C.c_void_p()
+    idx = b">i\nACGTACGT\n"
+    assert lib.mczi_serve_open(0, idx, len(idx), 5, 3, 0, 4, 0, C.byref(srv)) == _native.MCZI_ERR_INVALID_CONFIG
+    assert lib.mczi_serve_error(None, 0) == b"workers must be in [1, 64]"
+    assert lib.mczi_serve_open(0, idx, len(idx), 5, 3, 1, 0, 0, C.byref(srv)) == _native.MCZI_ERR_INVALID_CONFIG
+    assert lib.mczi_serve_error(None, 0) == b"max_batch must be in [1, 4096]"
+    assert lib.mczi_serve_submit(None, idx, len(idx), C.byref(C.c_uint64())) == _native.MCZI_ERR_STATE
+    assert lib.mczi_serve_close(None) == _native.MCZI_ERR_STATE
 
 
 def test_oracle_not_imported_by_product():

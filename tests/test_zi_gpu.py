@@ -185,3 +185,21 @@ def test_serving_results_match_alone(gpu_ctx, oracle):
         assert srv.batches < len(reqs)  # requests were batched
     for i in range(len(reqs)):
         assert sorted(int(v) for v in got[i]) == alone[i], i
+        assert futs[i].latency_ms >= futs[i].queue_ms >= 0.0
+
+
+def test_serving_wide_keys_and_empty_requests(gpu_ctx, oracle):
+    """k > 32 results come back as (lo, hi) pairs; requests with no k-mer
+    (empty, too short, not FASTX) get empty sets, not errors."""
+    from mczi_gb300.serve import ZIServer
+    rng = np.random.default_rng(33)
+    g = rand_seq(rng, 20000)
+    index = b">g\n" + g + b"\n"
+    reqs = [reads(rng, g if i % 2 else rand_seq(rng, 3000), 30, 150, 0.01) for i in range(12)]
+    reqs += [b"", b">s\nACGT\n", b"no record here\n"]
+    with ZIServer(index, 45, 21, workers=1, max_batch=8) as srv:
+        got = [f.result(timeout=120) for f in [srv.submit(r) for r in reqs]]
+        assert srv.stats()["requests"] == len(reqs)
+    for r, x in zip(reqs, got):
+        want = oracle_absent(oracle, index, [r], 45) if r.startswith(b">") else []
+        assert sorted((int(h) << 64) | int(l) for l, h in x) == want
