@@ -45,13 +45,6 @@ METRIC = "MC Gbases/s"
 UNIT = "Gbases/s"
 
 
-def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
-
-
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -170,10 +163,10 @@ def algorithmic_bytes(stats, k: int, text_bytes: int):
 def run_ours(args):
     import numpy as np
     import torch
-    ws, rank, local = dist_env()
-    if ws > 1:
-        torch.distributed.init_process_group("nccl")
+    from mczi_gb300.replicas import ReplicaGroup, env
+    ws, rank, local = env()
     torch.cuda.set_device(local)
+    group = ReplicaGroup("nccl")  # replicas: each rank counts its own copy of the workload
     from mczi_gb300 import build
     build.build_all()
     from mczi_gb300.mc import Context, CounterConfig
@@ -193,17 +186,8 @@ def run_ours(args):
         sample = gen.c2_reads(min(args.scale, 1.0) * 0.05)
         _, tuning_report = autotune.tune(ctx, [sample], cfg, 0, use_cache=False)
 
-    def barrier():
-        if ws > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-
-    def max_over_ranks(v: float) -> float:
-        if ws == 1:
-            return v
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+    barrier = group.barrier
+    max_over_ranks = group.max_over_ranks
 
     # ---- device-resident value
     ctx.stage(inputs)
@@ -242,7 +226,8 @@ def run_ours(args):
         ctx.set_graph_replay(False)
     clk = clocks.stop()
     dev_ms = graph_ms if graph_ms else dev_ms_plain
-    value = nb * ws / (dev_ms * 1e-3) / 1e9
+    nb_all = group.sum_over_ranks(nb)  # bases of all ranks
+    value = nb_all / (dev_ms * 1e-3) / 1e9
 
     # ---- end to end through the C ABI: H2D from pinned + count + D2H of every
     # record into pinned host buffers (allocated once, reused every step)
@@ -269,7 +254,7 @@ def run_ours(args):
     e1.record(stream)
     barrier()
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
-    e2e_value = nb * ws / (e2e_ms * 1e-3) / 1e9
+    e2e_value = nb_all / (e2e_ms * 1e-3) / 1e9
     d2h = n_records * (8 + (8 if k > 32 else 0) + 8)
 
     # ---- roofline of the dominant kernel
@@ -321,8 +306,7 @@ def run_ours(args):
     ctx.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if ws > 1:
-        torch.distributed.destroy_process_group()
+    group.close()
 
 
 def cpu_baseline(args, sample_scale: float | None = None):
@@ -345,7 +329,8 @@ def cpu_baseline(args, sample_scale: float | None = None):
 
 
 def run_reference(args):
-    ws, rank, _ = dist_env()
+    from mczi_gb300.replicas import env
+    ws, rank, _ = env()
     if rank != 0:
         return
     steps = []
