@@ -165,6 +165,86 @@ __device__ __forceinline__ bool acgt32(const uint8_t* src, uint64_t* codes) {
   return ok == 0x80808080u;
 }
 
+// bit i set where byte i of the four-byte word is 0x80-flagged by zero_bytes,
+// gathered into 4 bits (the products of the flags do not overlap)
+__device__ __forceinline__ uint32_t gather4(uint32_t z) { return (((z >> 7) * 0x00204081u) >> 21) & 0xFu; }
+
+// 32 bytes of FASTA classified at once from the line state before them.
+// base: bit i = byte i is a base (A/C/G/T either case, not in a header);
+// brk: bit i = byte i ends the current fragment (any other byte, except
+// '\n' and a '\r' outside a header); codes: MC codes MSB-first (byte 0 in
+// bits 63-62), meaningful where base is set.  Same answers as step_fasta
+// byte by byte, st updated the same way.
+struct Fasta32 {
+  uint32_t base, brk;
+  uint64_t codes;
+};
+
+__device__ __forceinline__ Fasta32 fasta32(const uint8_t* src, uint32_t& st) {
+  const uint4 v0 = *reinterpret_cast<const uint4*>(src);
+  const uint4 v1 = *reinterpret_cast<const uint4*>(src + 16);
+  const uint32_t w[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+  uint32_t nl = 0, cr = 0, gt = 0, acgt = 0;
+  uint64_t codes = 0;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const uint32_t l = w[j] | 0x20202020u;
+    nl |= gather4(zero_bytes(w[j] ^ 0x0a0a0a0au)) << (4 * j);
+    cr |= gather4(zero_bytes(w[j] ^ 0x0d0d0d0du)) << (4 * j);
+    gt |= gather4(zero_bytes(w[j] ^ 0x3e3e3e3eu)) << (4 * j);
+    acgt |= gather4(zero_bytes(l ^ 0x61616161u) | zero_bytes(l ^ 0x63636363u) | zero_bytes(l ^ 0x67676767u) |
+                    zero_bytes(l ^ 0x74747474u)) << (4 * j);
+    const uint32_t t = (w[j] >> 1) & 0x03030303u;
+    const uint32_t mc = t ^ ((t >> 1) & 0x01010101u);
+    const uint32_t v8 = ((mc & 3u) << 6) | (((mc >> 8) & 3u) << 4) | (((mc >> 16) & 3u) << 2) | ((mc >> 24) & 3u);
+    codes |= (uint64_t)v8 << (56 - 8 * j);
+  }
+  // header lines: from a '>' at a line start (or an open header) to the next '\n'
+  const uint32_t ls = (nl << 1) | (st == LS ? 1u : 0u);
+  uint32_t starts = (ls & gt) | (st == HDR ? 1u : 0u);
+  uint32_t hdr = 0;
+  while (starts) {
+    const int s0 = __ffs(starts) - 1;
+    const uint32_t after = nl & (0xffffffffu << s0);
+    const uint32_t upto = after ? ((1u << (__ffs(after) - 1)) - 1u) : 0xffffffffu;
+    hdr |= upto & (0xffffffffu << s0);
+    starts &= ~(upto | (1u << s0));
+  }
+  Fasta32 c;
+  c.base = acgt & ~hdr;
+  c.brk = ~(c.base | nl | (cr & ~hdr));
+  c.codes = codes;
+  st = (nl >> 31) ? (uint32_t)LS : ((hdr >> 31) ? (uint32_t)HDR : (uint32_t)SEQ);
+  return c;
+}
+
+// a chunk's base count and breaks as one BaseSum term
+__device__ __forceinline__ BaseSum fasta32_sum(const Fasta32& f) {
+  BaseSum c{0, 0, 0, 0};
+  c.nb = (uint32_t)__popc(f.base);
+  if (c.nb == 0) {
+    c.fb = c.lb = f.brk ? 1u : 0u;
+  } else {
+    const int a = __ffs(f.base) - 1, b = 31 - __clz(f.base);
+    c.fb = (f.brk & ((1u << a) - 1u)) ? 1u : 0u;
+    c.lb = ((f.brk >> b) >> 1) ? 1u : 0u;
+  }
+  return c;
+}
+
+// OR 2*len code bits (top-aligned in v) into the staging words at base p
+__device__ __forceinline__ void stage_codes(uint32_t* spk, uint64_t p, uint64_t w0, uint64_t v) {
+  const uint64_t q = (p >> 4) - w0;
+  const uint32_t r2 = 2 * (uint32_t)(p & 15);
+  const uint32_t a = (uint32_t)(v >> (32 + r2)), b = (uint32_t)(v >> r2);
+  if (a) atomicOr(&spk[q], a);
+  if (b) atomicOr(&spk[q + 1], b);
+  if (r2) {
+    const uint32_t c = (uint32_t)(v << (32 - r2));
+    if (c) atomicOr(&spk[q + 2], c);
+  }
+}
+
 __device__ __forceinline__ void tile_line_state(const uint8_t* __restrict__ text, const uint32_t* __restrict__ tile_info,
                                                 const uint64_t* __restrict__ input_tile0, const LineSum* __restrict__ line_pre,
                                                 uint64_t tile, bool& fastq, uint32_t& st, uint32_t& line4) {
@@ -269,9 +349,11 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_count(const uint8_t* __re
     if (seq_line && acgt32(sb + f, &codes)) {
       c.nb = 32;  // 32 bases, no break; a FASTA line that started here is now mid-sequence
       if (!fastq) st = SEQ;
+    } else if (!fastq) {
+      c = fasta32_sum(fasta32(sb + f, st));
     } else {
       for (int i = 0; i < 32; i++) {
-        const uint32_t r = fastq ? step_fastq(sb[f + i], st) : step_fasta(sb[f + i], st);
+        const uint32_t r = step_fastq(sb[f + i], st);
         if (r < 4) { c.nb++; c.lb = 0; }
         else if (r == 4) { if (c.nb == 0) c.fb = 1; c.lb = 1; }
       }
@@ -324,9 +406,11 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __re
     if (fast[h]) {
       c.nb = 32;
       if (!fastq) st = SEQ;  // 32 letters: a FASTA line that started here is now mid-sequence
+    } else if (!fastq) {
+      c = fasta32_sum(fasta32(sb + f, st));
     } else {
       for (int i = 0; i < 32; i++) {
-        const uint32_t r = fastq ? step_fastq(sb[f + i], st) : step_fasta(sb[f + i], st);
+        const uint32_t r = step_fastq(sb[f + i], st);
         if (r < 4) { c.nb++; c.lb = 0; }
         else if (r == 4) { if (c.nb == 0) c.fb = 1; c.lb = 1; }
       }
@@ -349,18 +433,34 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __re
     const int f = first + 32 * h;
     if (fast[h]) {
       // 32 bases at p: spread the 64 code bits over (up to) three staging words
-      const uint64_t q = (p >> 4) - w0;
-      const uint32_t r2 = 2 * (uint32_t)(p & 15);
-      atomicOr(&spk[q], (uint32_t)(codes[h] >> (32 + r2)));
-      atomicOr(&spk[q + 1], (uint32_t)(codes[h] >> r2));
-      if (r2) atomicOr(&spk[q + 2], (uint32_t)(codes[h] << (32 - r2)));
+      stage_codes(spk, p, w0, codes[h]);
       if (pending) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
       pending = 0;
       p += 32;
       if (!fastq) st = SEQ;
+    } else if (!fastq) {
+      // runs of consecutive bases, each staged like a fast chunk; a break
+      // before a run makes its first base a fragment start
+      const Fasta32 fc = fasta32(sb + f, st);
+      uint32_t m = fc.base;
+      int done = 0;  // bytes [0, done) handled
+      while (m) {
+        const int a = __ffs(m) - 1;
+        const uint32_t rest = ~(m >> a);
+        const int len = rest ? __ffs(rest) - 1 : 32 - a;
+        if (fc.brk & ((1u << a) - 1u) & (0xffffffffu << done)) pending = 1;
+        const uint64_t run = (fc.codes << (2 * a)) & (len >= 32 ? ~0ull : ~(~0ull >> (2 * len)));
+        stage_codes(spk, p, w0, run);
+        if (pending) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
+        pending = 0;
+        p += (uint64_t)len;
+        done = a + len;
+        m = done >= 32 ? 0u : (m & (0xffffffffu << done));
+      }
+      if (done < 32 && (fc.brk & (0xffffffffu << done))) pending = 1;
     } else {
       for (int i = 0; i < 32; i++) {
-        const uint32_t r = fastq ? step_fastq(sb[f + i], st) : step_fasta(sb[f + i], st);
+        const uint32_t r = step_fastq(sb[f + i], st);
         if (r < 4) {
           atomicOr(&spk[(p >> 4) - w0], r << (30 - 2 * (uint32_t)(p & 15)));
           if (pending) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
