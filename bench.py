@@ -525,6 +525,20 @@ def run_zi(args):
     ctx.set_stream(stream.cuda_stream)
     zi.build_dictionary(index, k, m, ctx=ctx)
     info = zi.info(ctx)
+    if args.zi_one_group:
+        # for kernel profiles: one 50-file group per input, then as a union
+        group = files[:50]
+        for name, run in (("per_input", zi.query_per_input), ("union", zi.query)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            n = run(ctx, group)
+            torch.cuda.synchronize()
+            print(json.dumps({"query": name, "files": len(group), "records": n,
+                              "ms": round((time.perf_counter() - t0) * 1e3, 3),
+                              "phases_ms": [round(x, 3) for x in ctx.phase_times()[:5]],
+                              "stats": ctx.run_stats()[:8]}), flush=True)
+        ctx.close()
+        return
     # batched: files in balanced groups of at most 64 (one mask word per
     # record), each group one set of launches with a result per file
     ngroups = -(-nfiles // 64)
@@ -686,6 +700,8 @@ def main():
     ap.add_argument("--no-graph", action="store_true", help="skip the graph-replay timing")
     ap.add_argument("--workload", default="mc", choices=["mc", "mc-short", "mc-fof", "zi", "zi-serve"])
     ap.add_argument("--zi-files", type=int, default=200)
+    ap.add_argument("--zi-one-group", action="store_true",
+                    help="run one 50-file group (per input, then union) and exit: the case for ZI kernel profiles")
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-workers", type=int, default=2)
     ap.add_argument("--serve-max-bytes", type=float, default=200e6)
