@@ -526,8 +526,9 @@ def run_zi(args):
     zi.build_dictionary(index, k, m, ctx=ctx)
     info = zi.info(ctx)
     if args.zi_one_group:
-        # for kernel profiles: one 50-file group per input, then as a union
-        group = files[:50]
+        # for kernel profiles: one 50-file group (every 4th file: half in-index
+        # reads, half foreign, like the whole query) per input, then as a union
+        group = files[::4][:50]
         for name, run in (("per_input", zi.query_per_input), ("union", zi.query)):
             torch.cuda.synchronize()
             t0 = time.perf_counter()

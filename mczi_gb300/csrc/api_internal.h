@@ -9,9 +9,29 @@
 
 namespace mczi {
 
+// owns one device allocation: freed when the owner (the context) is deleted;
+// movable (the pipeline swaps buffers), not copyable
 struct DevBuf {
   void* p = nullptr;
   size_t cap = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), cap(o.cap) {
+    o.p = nullptr;
+    o.cap = 0;
+  }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      cap = o.cap;
+      o.p = nullptr;
+      o.cap = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
   // grows by at least half the current size, so a stream of slightly larger
   // requests does not reallocate (cudaFree synchronises the whole device)
   cudaError_t ensure(size_t bytes) {
@@ -55,6 +75,34 @@ struct DevBuf {
   template <class T>
   T* as() const {
     return static_cast<T*>(p);
+  }
+};
+
+// owns one pinned host allocation (device-to-host copies at the link's speed)
+struct HostPinned {
+  void* p = nullptr;
+  size_t cap = 0;
+  HostPinned() = default;
+  HostPinned(const HostPinned&) = delete;
+  HostPinned& operator=(const HostPinned&) = delete;
+  ~HostPinned() { release(); }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (bytes <= cap) return cudaSuccess;
+    const size_t want = cap && bytes < cap + cap / 2 ? cap + cap / 2 : bytes;
+    release();
+    cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    cap = want;
+    return cudaSuccess;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
   }
 };
 
@@ -120,6 +168,8 @@ struct mczi_ctx {
   mczi::DevBuf desc, key, desc2, key2, part_hist, part_tmp, bucket_off;
   mczi::DevBuf out_lo, out_hi, out_cnt, out_mask;
   mczi::DevBuf cnt64;  // counts widened to u64 for direct copies to the caller
+  mczi::DevBuf kff_dev;          // KFF records formatted on the device
+  mczi::HostPinned kff_host;     // their host copy, written to the file as is
   mczi::DevBuf sx_keys, sx_tab, sx_rank, sx_ext;  // simplitig writer: sorted keys, key->rank table, extensions
   mczi::DevBuf stream_scratch;     // streamed staging: pack carries, scan tile range
   cudaStream_t copy_stream = nullptr;  // host-to-device copies of the streamed staging

@@ -137,8 +137,8 @@ void extend_forward(std::string& seq, int k, RemainingSet& rem) {
 
 }  // namespace
 
-bool write_kff_file(const std::string& path, const HostRecords& r, int k, int m, uint64_t x, int count_size,
-                    std::string* err) {
+bool write_kff_records(const std::string& path, int k, int m, uint64_t x, int count_size, uint64_t n,
+                       const uint8_t* rec, uint64_t rec_bytes, std::string* err) {
   File o(path);
   if (!o.f) {
     *err = "failed to create " + path;
@@ -162,28 +162,9 @@ bool write_kff_file(const std::string& path, const HostRecords& r, int k, int m,
     o.put_be(vals[i], 8);
   }
   o.put("r", 1);
-  const size_t n = r.lo.size();
   o.put_be(n, 8);
-  const int nb = (k + 3) / 4;
-  const uint64_t sat = (x + 1) < 255 ? (x + 1) : 255;
-  uint8_t rec[32];
-  for (size_t i = 0; i < n; i++) {
-    uint8_t be[16];
-    const uint64_t hi = r.hi.empty() ? 0 : r.hi[i], lo = r.lo[i];
-    for (int j = 0; j < 8; j++) {
-      be[j] = (uint8_t)(hi >> (56 - 8 * j));
-      be[8 + j] = (uint8_t)(lo >> (56 - 8 * j));
-    }
-    std::memcpy(rec, be + 16 - nb, (size_t)nb);
-    int len = nb;
-    const uint64_t c = r.count[i];
-    if (count_size == 1) {
-      rec[len++] = (uint8_t)(c < sat ? c : sat);
-    } else {
-      for (int j = 0; j < count_size; j++) rec[len++] = (uint8_t)(c >> (8 * (count_size - 1 - j)));
-    }
-    o.put(rec, (size_t)len);
-  }
+  o.flush();
+  if (o.f && rec_bytes && std::fwrite(rec, 1, rec_bytes, o.f) != rec_bytes) o.ok = false;
   o.put("KFF", 3);
   if (!o.close()) {
     *err = "failed to write " + path;

@@ -11,9 +11,11 @@ struct HostRecords {
   std::vector<uint64_t> lo, hi, count;  // hi empty for k <= 32
 };
 
-// KFF file (src/lib.rs:1633-1670, 3071-3121).  count_size: 1, 4 or 8.
-bool write_kff_file(const std::string& path, const HostRecords& r, int k, int m, uint64_t x, int count_size,
-                    std::string* err);
+// KFF file (src/lib.rs:1633-1670, 3071-3121) around n records already laid
+// out as the format stores them (rec_bytes = n x (ceil(k/4) + count_size)).
+// count_size: 1, 4 or 8.
+bool write_kff_records(const std::string& path, int k, int m, uint64_t x, int count_size, uint64_t n,
+                       const uint8_t* rec, uint64_t rec_bytes, std::string* err);
 
 // Greedy simplitig FASTA (src/lib.rs:1469-1533).  Returns false on I/O error.
 bool write_simplitig_file(const std::string& path, const HostRecords& r, int k, std::string* err);

@@ -866,6 +866,39 @@ __global__ void k_widen_counts(const uint32_t* __restrict__ in, uint64_t n, unsi
     out[i] = in[i];
 }
 
+// KFF records (src/lib.rs:3089-3117): the k-mer as ceil(k/4) big-endian bytes
+// of its 2k-bit value, then the count (count_size 1: saturated at sat; 4 or
+// 8: big-endian)
+__global__ void k_kff_records(const uint64_t* __restrict__ lo, const uint64_t* __restrict__ hi,
+                              const uint32_t* __restrict__ cnt, uint64_t n, int nb, int count_size, uint32_t sat,
+                              uint8_t* __restrict__ out) {
+  const int rl = nb + count_size;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint8_t* o = out + i * (uint64_t)rl;
+    const uint64_t l = lo[i], h = hi ? hi[i] : 0ull;
+    for (int j = 0; j < nb; j++) {
+      const int bit = 8 * (nb - 1 - j);
+      o[j] = (uint8_t)(bit >= 64 ? (h >> (bit - 64)) : (l >> bit));
+    }
+    const uint32_t c = cnt[i];
+    if (count_size == 1) {
+      o[nb] = (uint8_t)(c < sat ? c : sat);
+    } else {
+      for (int j = 0; j < count_size; j++) {
+        const int bit = 8 * (count_size - 1 - j);
+        o[nb + j] = (uint8_t)(bit >= 32 ? 0u : (c >> bit));
+      }
+    }
+  }
+}
+
+void launch_kff_records(const uint64_t* lo, const uint64_t* hi, const uint32_t* cnt, uint64_t n, int nb,
+                        int count_size, uint32_t sat, uint8_t* out, int sm_count, cudaStream_t s) {
+  const uint64_t g = (n + 255) / 256;
+  const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)sm_count * 16));
+  k_kff_records<<<grid, 256, 0, s>>>(lo, hi, cnt, n, nb, count_size, sat, out);
+}
+
 int32_t fetch_records(mczi_ctx* ctx, HostRecords* r) {
   const uint64_t n = ctx->n_out;
   r->lo.resize(n);
@@ -948,14 +981,8 @@ int32_t mczi_close(mczi_ctx* ctx) {
   if (!ctx) return MCZI_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  DevBuf* bufs[] = {&ctx->text, &ctx->tile_info, &ctx->input_tile0, &ctx->line_sum, &ctx->line_pre, &ctx->line_tmp,
-                    &ctx->base_sum, &ctx->base_pre, &ctx->base_tmp, &ctx->packed, &ctx->fbits, &ctx->input_base,
-                    &ctx->desc, &ctx->key, &ctx->desc2, &ctx->key2, &ctx->part_hist, &ctx->part_tmp,
-                    &ctx->bucket_off, &ctx->out_lo, &ctx->out_hi, &ctx->out_cnt, &ctx->scalars,
-                    &ctx->mintab, &ctx->pairtab, &ctx->out_mask, &ctx->zi_tmp0, &ctx->zi_tmp1,
-                    &ctx->zi_tmp2, &ctx->zi.packed, &ctx->zi.sk, &ctx->zi.bucket_off, &ctx->zi.bits,
-                    &ctx->zi.rank};
-  for (DevBuf* b : bufs) b->release();
+  if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+  // every device buffer is a DevBuf member: deleting the context frees them
   for (auto& ev : ctx->ev) if (ev) cudaEventDestroy(ev);
   for (auto& ev : ctx->ev_pre) if (ev) cudaEventDestroy(ev);
   for (auto& ev : ctx->ev_graph) if (ev) cudaEventDestroy(ev);
@@ -1056,12 +1083,29 @@ int32_t mczi_result_write_kff(mczi_ctx* ctx, const char* path) {
   if (!ctx) return MCZI_ERR_STATE;
   if (!ctx->have_result) return fail(ctx, MCZI_ERR_STATE, "no result");
   cudaSetDevice(ctx->device);
-  HostRecords r;
-  int32_t rc = fetch_records(ctx, &r);
-  if (rc) return rc;
+  // records formatted on the device as the file stores them, copied once
   const int count_size = ctx->mode == MCZI_MODE_PRESENCE ? 4 : (ctx->k <= 32 ? 1 : 8);
+  const int nb = (ctx->k + 3) / 4;
+  const uint64_t n = ctx->n_out, bytes = n * (uint64_t)(nb + count_size);
+  if (n) {
+    CKA(ctx->kff_dev, bytes);
+    const cudaError_t he = ctx->kff_host.ensure(bytes);
+    if (he != cudaSuccess) {
+      cudaGetLastError();
+      return fail(ctx, MCZI_ERR_OOM, "pinned host allocation for the KFF records failed");
+    }
+    const uint64_t sat = ctx->x + 1 < 255 ? ctx->x + 1 : 255;
+    launch_kff_records(ctx->out_lo.as<uint64_t>(), ctx->k > 32 ? ctx->out_hi.as<uint64_t>() : nullptr,
+                       ctx->out_cnt.as<uint32_t>(), n, nb, count_size, (uint32_t)sat, ctx->kff_dev.as<uint8_t>(),
+                       ctx->sm_count, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ctx->kff_host.p, ctx->kff_dev.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
   std::string e;
-  if (!write_kff_file(path, r, ctx->k, ctx->m, ctx->x, count_size, &e)) return fail(ctx, MCZI_ERR_IO, e);
+  if (!write_kff_records(path, ctx->k, ctx->m, ctx->x, count_size, n, static_cast<const uint8_t*>(ctx->kff_host.p),
+                         bytes, &e))
+    return fail(ctx, MCZI_ERR_IO, e);
   return MCZI_OK;
 }
 

@@ -195,19 +195,24 @@ def test_kff_output(gpu_ctx, oracle, tmp_path):
     from mczi_gb300 import gen
     from mczi_gb300.mc import CounterConfig
     data = gen.c1_reads(scale=0.004)
-    cases = [(31, 21, 2, 0, 1), (45, 21, 1, 0, 8)]
+    half = data[: data.size // 2]
+    # (k, m, x, mode, count bytes): 1-byte saturated, 8-byte, 4-byte presence,
+    # 16-byte keys, 2-byte keys, and an empty result
+    cases = [(31, 21, 2, 0, 1), (45, 21, 1, 0, 8), (21, 11, 1, 1, 4), (63, 21, 1, 0, 8), (5, 3, 3, 0, 1),
+             (31, 21, 254, 0, 1)]
     for k, m, x, mode, cs in cases:
-        gpu_ctx.count([data], CounterConfig(k, m, x), mode)
-        p = tmp_path / f"g{k}.kff"
+        ins = [data, half] if mode else [data]
+        gpu_ctx.count(ins, CounterConfig(k, m, x), mode)
+        p = tmp_path / f"g{k}_{x}.kff"
         gpu_ctx.write_kff(p)
         head, recs, ok = parse_kff(p.read_bytes())
         assert ok
-        lo, hi, cnt = oracle.count([data], k, x, mode)
+        lo, hi, cnt = oracle.count(ins, k, x, mode)
         exp = dict(zip(to_int(lo, hi), (int(c) for c in cnt)))
         if cs == 1:
             exp = {e: min(c, x + 1, 255) for e, c in exp.items()}
         assert recs == exp
-        q = tmp_path / f"o{k}.kff"
+        q = tmp_path / f"o{k}_{x}.kff"
         oracle.write_kff(q, lo, hi, cnt, k, m, x, cs)
         ohead, _, _ = parse_kff(q.read_bytes())
         assert head["head"] == ohead["head"]  # header bytes identical, record count included
