@@ -277,7 +277,9 @@ const char* mczi_serve_error(mczi_server* srv, uint64_t request_id);
 int32_t mczi_serve_stats(mczi_server* srv, double* out, int32_t cap);
 
 /* Stops accepting requests, lets the workers finish the queued ones, joins
- * them and frees everything (results not yet copied are dropped). */
+ * them and frees everything (results not yet copied are dropped).  No other
+ * call on the same server may run during or after it: stop the thread that
+ * waits in mczi_serve_next first. */
 int32_t mczi_serve_close(mczi_server* srv);
 
 /* ------------------------------------------------ packing without allocation */
