@@ -366,8 +366,15 @@ int32_t pipe_partition(mczi_ctx* ctx, Pipe& p) {
   qa.bucket_off = ctx->bucket_off.as<uint64_t>();
   qa.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
   if (p.n_desc > 0) {
-    launch_partition(qa, s, !ctx->fuse_part2);
-    p.launches += 7;
+    if (ctx->fuse_part2) {
+      // two tile-sorted levels: desc -> (desc2, key2 as u16 p1) -> desc,
+      // which the counting kernel then reads as unsorted buckets
+      launch_partition_tiled(qa, qa.hist, reinterpret_cast<uint16_t*>(ctx->key2.p), ctx->desc.as<uint64_t>(), s);
+      p.launches += 5;
+    } else {
+      launch_partition(qa, s, true);
+      p.launches += 7;
+    }
   }
   CK(cudaGetLastError());
   if (!p.capture) CK(cudaEventRecord(ctx->ev[3], s));
@@ -442,8 +449,11 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       CK(cudaMemsetAsync(sc + SC_WORK, 0, 8, s));
       CountArgs ca;
       ca.packed = ctx->packed.as<uint32_t>();
-      ca.desc = ctx->desc.as<uint64_t>();
-      ca.desc_unsorted = ctx->fuse_part2 ? ctx->desc2.as<uint64_t>() : nullptr;
+      // fused: the partition leaves the buckets (unsorted by p2) in desc and
+      // the counting kernel sorts each into desc2; otherwise desc2 -> desc
+      // by k_part2 and the kernel reads desc
+      ca.desc = ctx->fuse_part2 ? ctx->desc2.as<uint64_t>() : ctx->desc.as<uint64_t>();
+      ca.desc_unsorted = ctx->fuse_part2 ? ctx->desc.as<uint64_t>() : nullptr;
       ca.key = ctx->key.as<uint32_t>();
       ca.bucket_off = ctx->bucket_off.as<uint64_t>();
       ca.k = k;

@@ -93,6 +93,12 @@ struct PartArgs {
   uint32_t* status;
 };
 void launch_partition(const PartArgs& a, cudaStream_t s, bool with_pass2 = true);
+// pass 1 in two tile-sorted levels: (desc_in, key_in) -> (desc_out, tmp_p1)
+// grouped by the top p1 bits -> final_out grouped by p1 (bucket_off set);
+// scratch holds NP1 + 64 + NP1 u32 (histogram and cursors).  final_out may
+// be desc_in (level A has read it by then).
+void launch_partition_tiled(const PartArgs& a, uint32_t* scratch, uint16_t* tmp_p1, uint64_t* final_out,
+                            cudaStream_t s);
 
 // ---------------------------------------------------------------- K4 pre-count
 struct PrecountArgs {
