@@ -165,7 +165,7 @@ struct mczi_ctx {
 
   mczi::DevBuf text, tile_info, input_tile0, line_sum, line_pre, line_tmp, base_sum, base_pre, base_tmp;
   mczi::DevBuf packed, fbits, input_base;
-  mczi::DevBuf desc, key, desc2, key2, part_hist, part_tmp, bucket_off;
+  mczi::DevBuf desc, key, desc2, key2, part_hist, bucket_off;
   mczi::DevBuf out_lo, out_hi, out_cnt, out_mask;
   mczi::DevBuf cnt64;  // counts widened to u64 for direct copies to the caller
   mczi::DevBuf kff_dev;          // KFF records formatted on the device
@@ -175,7 +175,6 @@ struct mczi_ctx {
   cudaStream_t copy_stream = nullptr;  // host-to-device copies of the streamed staging
   cudaEvent_t ev_copy = nullptr;       // last copied segment
   int streamed = 1;                    // one-shot counts overlap staging with pack + scan
-  int fuse_part2 = 1;                  // partition pass 2 runs inside the counting kernel
   uint64_t stream_seg_tiles = 0;       // segment size in pack tiles (0 = automatic)
   uint32_t zi_bucket_records = 0;      // records per final ZI dedup bucket (0 = half a table)
   mczi::DevBuf scalars;

@@ -350,9 +350,7 @@ int32_t pipe_partition(mczi_ctx* ctx, Pipe& p) {
   if (!p.capture) CK(cudaEventRecord(ctx->ev[2], s));
   CKA(ctx->desc2, p.desc_cap * 8);
   CKA(ctx->key2, p.desc_cap * 4);
-  const uint64_t nh = (uint64_t)NP1 * PART_CTAS;
-  CKA(ctx->part_hist, (2 * nh + 2) * sizeof(uint32_t));
-  CKA(ctx->part_tmp, (nh / SCAN_CHUNK + 2) * sizeof(uint32_t));
+  CKA(ctx->part_hist, (2 * NP1 + 128) * sizeof(uint32_t));  // histogram + the two levels' cursors
   CKA(ctx->bucket_off, (NP1 + 1) * sizeof(uint64_t));
   PartArgs qa;
   qa.desc_in = ctx->desc.as<uint64_t>();
@@ -362,19 +360,13 @@ int32_t pipe_partition(mczi_ctx* ctx, Pipe& p) {
   qa.n_desc = reinterpret_cast<const unsigned long long*>(sc + SC_NDESC);
   qa.desc_cap = p.desc_cap;
   qa.hist = ctx->part_hist.as<uint32_t>();
-  qa.hist_tmp = ctx->part_tmp.as<uint32_t>();
   qa.bucket_off = ctx->bucket_off.as<uint64_t>();
   qa.status = reinterpret_cast<uint32_t*>(sc + SC_STATUS);
   if (p.n_desc > 0) {
-    if (ctx->fuse_part2) {
-      // two tile-sorted levels: desc -> (desc2, key2 as u16 p1) -> desc,
-      // which the counting kernel then reads as unsorted buckets
-      launch_partition_tiled(qa, qa.hist, reinterpret_cast<uint16_t*>(ctx->key2.p), ctx->desc.as<uint64_t>(), s);
-      p.launches += 5;
-    } else {
-      launch_partition(qa, s, true);
-      p.launches += 7;
-    }
+    // two tile-sorted levels: desc -> (desc2, key2 as u16 p1) -> desc, which
+    // the counting kernel then reads as buckets unsorted by p2
+    launch_partition_tiled(qa, qa.hist, reinterpret_cast<uint16_t*>(ctx->key2.p), ctx->desc.as<uint64_t>(), s);
+    p.launches += 5;
   }
   CK(cudaGetLastError());
   if (!p.capture) CK(cudaEventRecord(ctx->ev[3], s));
@@ -449,11 +441,10 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       CK(cudaMemsetAsync(sc + SC_WORK, 0, 8, s));
       CountArgs ca;
       ca.packed = ctx->packed.as<uint32_t>();
-      // fused: the partition leaves the buckets (unsorted by p2) in desc and
-      // the counting kernel sorts each into desc2; otherwise desc2 -> desc
-      // by k_part2 and the kernel reads desc
-      ca.desc = ctx->fuse_part2 ? ctx->desc2.as<uint64_t>() : ctx->desc.as<uint64_t>();
-      ca.desc_unsorted = ctx->fuse_part2 ? ctx->desc.as<uint64_t>() : nullptr;
+      // the partition leaves the buckets (unsorted by p2) in desc; the
+      // counting kernel sorts each into desc2 and counts from there
+      ca.desc = ctx->desc2.as<uint64_t>();
+      ca.desc_unsorted = ctx->desc.as<uint64_t>();
       ca.key = ctx->key.as<uint32_t>();
       ca.bucket_off = ctx->bucket_off.as<uint64_t>();
       ca.k = k;

@@ -87,13 +87,11 @@ struct PartArgs {
   uint32_t* key_out;
   const unsigned long long* n_desc;  // device scalar
   uint64_t desc_cap;
-  uint32_t* hist;       // [NP1][PART_CTAS] then scanned in place
-  uint32_t* hist_tmp;   // scan temporaries
+  uint32_t* hist;       // scratch: NP1 histogram + the two levels' cursors
   uint64_t* bucket_off; // NP1 + 1 bucket offsets (p1 buckets)
   uint32_t* status;
 };
-void launch_partition(const PartArgs& a, cudaStream_t s, bool with_pass2 = true);
-// pass 1 in two tile-sorted levels: (desc_in, key_in) -> (desc_out, tmp_p1)
+// p1 in two tile-sorted levels: (desc_in, key_in) -> (desc_out, tmp_p1)
 // grouped by the top p1 bits -> final_out grouped by p1 (bucket_off set);
 // scratch holds NP1 + 64 + NP1 u32 (histogram and cursors).  final_out may
 // be desc_in (level A has read it by then).
