@@ -17,6 +17,7 @@
 //                     memory, interior words stored, edge words OR-ed.
 #include <algorithm>
 
+#include "fasta_classify.cuh"
 #include "mczi_internal.h"
 #include "scan.cuh"
 
@@ -24,18 +25,7 @@ namespace mczi {
 
 namespace {
 
-enum : uint32_t { LS = 0, HDR = 1, SEQ = 2 };
-
-__device__ __forceinline__ int8_t code_of(uint32_t c) {
-  // A/a 0, C/c 1, G/g 2, T/t 3, else -1
-  switch (c | 0x20u) {
-    case 'a': return 0;
-    case 'c': return 1;
-    case 'g': return 2;
-    case 't': return 3;
-    default: return -1;
-  }
-}
+using namespace fasta;
 
 struct LineOp {
   static __device__ LineSum identity() { return LineSum{-1, 0, 0, 0}; }
@@ -66,12 +56,6 @@ struct NlOp {
     return NlSum{a.last > b.last ? a.last : b.last, a.nl + b.nl};
   }
 };
-
-// exact per-byte zero test: high bit of each byte set where the byte is 0
-__device__ __forceinline__ uint32_t zero_bytes(uint32_t x) {
-  const uint32_t y = ((x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | x;
-  return ~y & 0x80808080u;
-}
 
 __device__ __forceinline__ void load_tile(const uint8_t* __restrict__ text, uint64_t tile, uint8_t* sb) {
   const uint4* src = reinterpret_cast<const uint4*>(text + tile * PACK_TILE);
@@ -116,19 +100,6 @@ __device__ __forceinline__ uint32_t thread_state(const uint8_t* sb, bool fastq, 
   return tile_state;
 }
 
-// Classify one byte.  Returns 0..3 for a base, 4 for a break, 5 for skip.
-__device__ __forceinline__ uint32_t step_fasta(uint32_t c, uint32_t& st) {
-  if (c == '\n') { st = LS; return 5; }
-  if (st == LS) {
-    if (c == '>') { st = HDR; return 4; }
-    st = SEQ;
-  }
-  if (st == HDR) return 4;
-  if (c == '\r') return 5;
-  int8_t code = code_of(c);
-  return code < 0 ? 4u : (uint32_t)code;
-}
-
 __device__ __forceinline__ uint32_t step_fastq(uint32_t c, uint32_t& line) {
   if (c == '\n') {
     uint32_t r = ((line & 3u) == 1u) ? 4u : 5u;  // end of a sequence line ends the fragment
@@ -165,71 +136,11 @@ __device__ __forceinline__ bool acgt32(const uint8_t* src, uint64_t* codes) {
   return ok == 0x80808080u;
 }
 
-// bit i set where byte i of the four-byte word is 0x80-flagged by zero_bytes,
-// gathered into 4 bits (the products of the flags do not overlap)
-__device__ __forceinline__ uint32_t gather4(uint32_t z) { return (((z >> 7) * 0x00204081u) >> 21) & 0xFu; }
-
-// 32 bytes of FASTA classified at once from the line state before them.
-// base: bit i = byte i is a base (A/C/G/T either case, not in a header);
-// brk: bit i = byte i ends the current fragment (any other byte, except
-// '\n' and a '\r' outside a header); codes: MC codes MSB-first (byte 0 in
-// bits 63-62), meaningful where base is set.  Same answers as step_fasta
-// byte by byte, st updated the same way.
-struct Fasta32 {
-  uint32_t base, brk;
-  uint64_t codes;
-};
-
-__device__ __forceinline__ Fasta32 fasta32(const uint8_t* src, uint32_t& st) {
-  const uint4 v0 = *reinterpret_cast<const uint4*>(src);
-  const uint4 v1 = *reinterpret_cast<const uint4*>(src + 16);
-  const uint32_t w[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
-  uint32_t nl = 0, cr = 0, gt = 0, acgt = 0;
-  uint64_t codes = 0;
-#pragma unroll
-  for (int j = 0; j < 8; j++) {
-    const uint32_t l = w[j] | 0x20202020u;
-    nl |= gather4(zero_bytes(w[j] ^ 0x0a0a0a0au)) << (4 * j);
-    cr |= gather4(zero_bytes(w[j] ^ 0x0d0d0d0du)) << (4 * j);
-    gt |= gather4(zero_bytes(w[j] ^ 0x3e3e3e3eu)) << (4 * j);
-    acgt |= gather4(zero_bytes(l ^ 0x61616161u) | zero_bytes(l ^ 0x63636363u) | zero_bytes(l ^ 0x67676767u) |
-                    zero_bytes(l ^ 0x74747474u)) << (4 * j);
-    const uint32_t t = (w[j] >> 1) & 0x03030303u;
-    const uint32_t mc = t ^ ((t >> 1) & 0x01010101u);
-    const uint32_t v8 = ((mc & 3u) << 6) | (((mc >> 8) & 3u) << 4) | (((mc >> 16) & 3u) << 2) | ((mc >> 24) & 3u);
-    codes |= (uint64_t)v8 << (56 - 8 * j);
-  }
-  // header lines: from a '>' at a line start (or an open header) to the next '\n'
-  const uint32_t ls = (nl << 1) | (st == LS ? 1u : 0u);
-  uint32_t starts = (ls & gt) | (st == HDR ? 1u : 0u);
-  uint32_t hdr = 0;
-  while (starts) {
-    const int s0 = __ffs(starts) - 1;
-    const uint32_t after = nl & (0xffffffffu << s0);
-    const uint32_t upto = after ? ((1u << (__ffs(after) - 1)) - 1u) : 0xffffffffu;
-    hdr |= upto & (0xffffffffu << s0);
-    starts &= ~(upto | (1u << s0));
-  }
-  Fasta32 c;
-  c.base = acgt & ~hdr;
-  c.brk = ~(c.base | nl | (cr & ~hdr));
-  c.codes = codes;
-  st = (nl >> 31) ? (uint32_t)LS : ((hdr >> 31) ? (uint32_t)HDR : (uint32_t)SEQ);
-  return c;
-}
-
 // a chunk's base count and breaks as one BaseSum term
 __device__ __forceinline__ BaseSum fasta32_sum(const Fasta32& f) {
-  BaseSum c{0, 0, 0, 0};
-  c.nb = (uint32_t)__popc(f.base);
-  if (c.nb == 0) {
-    c.fb = c.lb = f.brk ? 1u : 0u;
-  } else {
-    const int a = __ffs(f.base) - 1, b = 31 - __clz(f.base);
-    c.fb = (f.brk & ((1u << a) - 1u)) ? 1u : 0u;
-    c.lb = ((f.brk >> b) >> 1) ? 1u : 0u;
-  }
-  return c;
+  uint32_t nb, fb, lb;
+  fasta32_counts(f, &nb, &fb, &lb);
+  return BaseSum{nb, fb, lb, 0};
 }
 
 // OR 2*len code bits (top-aligned in v) into the staging words at base p
@@ -442,22 +353,11 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __re
       // runs of consecutive bases, each staged like a fast chunk; a break
       // before a run makes its first base a fragment start
       const Fasta32 fc = fasta32(sb + f, st);
-      uint32_t m = fc.base;
-      int done = 0;  // bytes [0, done) handled
-      while (m) {
-        const int a = __ffs(m) - 1;
-        const uint32_t rest = ~(m >> a);
-        const int len = rest ? __ffs(rest) - 1 : 32 - a;
-        if (fc.brk & ((1u << a) - 1u) & (0xffffffffu << done)) pending = 1;
-        const uint64_t run = (fc.codes << (2 * a)) & (len >= 32 ? ~0ull : ~(~0ull >> (2 * len)));
+      fasta32_runs(fc, pending, [&](int len, uint64_t run, bool start) {
         stage_codes(spk, p, w0, run);
-        if (pending) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
-        pending = 0;
+        if (start) atomicOr(&sfb[(p >> 5) - f0], 1u << (uint32_t)(p & 31));
         p += (uint64_t)len;
-        done = a + len;
-        m = done >= 32 ? 0u : (m & (0xffffffffu << done));
-      }
-      if (done < 32 && (fc.brk & (0xffffffffu << done))) pending = 1;
+      });
     } else {
       for (int i = 0; i < 32; i++) {
         const uint32_t r = step_fastq(sb[f + i], st);
