@@ -246,10 +246,12 @@ def run_ours(args):
     barrier()
     stage_ms = (time.perf_counter() - t0) * 1e3
     barrier()
+    e2e_phase = [0.0] * 4
     t0 = time.perf_counter()
     e0.record(stream)
     for _ in range(args.steps):
         n = ctx.count(inputs, cfg)
+        e2e_phase = [a + b for a, b in zip(e2e_phase, ctx.phase_times()[:4])]
         rec = ctx.records(n, sorted=False, out=out)
     e1.record(stream)
     barrier()
@@ -282,7 +284,10 @@ def run_ours(args):
                        superkmers=stats[1], kept_records=stats[5], scale=args.scale),
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(nbytes),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 3),
-                "staging_ms": round(stage_ms, 3), "staging_gbs": round(nbytes / (stage_ms * 1e-3) / 1e9, 1)},
+                "staging_ms": round(stage_ms, 3), "staging_gbs": round(nbytes / (stage_ms * 1e-3) / 1e9, 1),
+                # device event times of the streamed steps: [0] spans staging + pack + scan
+                "phases_ms": {nm: round(v / args.steps, 3) for nm, v in
+                              zip(["staging_pack_scan", "rescan", "partition", "count"], e2e_phase)}},
         "gpu_launches": int(stats[8]) * args.steps,
         "tuning": tuning_report,
         "device_ms": {"launched": round(dev_ms_plain, 3),
