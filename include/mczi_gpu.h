@@ -285,12 +285,13 @@ int32_t mczi_serve_close(mczi_server* srv);
 /* ------------------------------------------------ packing without allocation */
 
 /* The 2-bit packer of mczi_count's first phase, for callers that cannot
- * allocate device memory where they call it: code running while a stream is
- * being captured into a CUDA graph, services that give out device memory only
- * from their own pre-sized arena, or latency-critical paths where a
- * cudaMalloc (and the synchronisation it may cause) is not allowed.  This
- * entry point has no counterpart in the reference; it allocates nothing and
- * calls no allocating routine.
+ * allocate device memory where they call it: services that give out device
+ * memory only from their own pre-sized arena (an allocation behind the
+ * arena's back breaks its accounting and fails once the arena holds the free
+ * HBM), or latency-critical paths where a cudaMalloc (and the
+ * synchronisation it may cause) is not allowed.  This entry point has no
+ * counterpart in the reference; it allocates nothing and calls no allocating
+ * routine.
  *
  * Inputs and outputs are the caller's device buffers: `d_text` holds one
  * FASTA (fastq = 0) or four-line FASTQ (fastq = 1) input of `text_len` bytes,
@@ -299,14 +300,18 @@ int32_t mczi_serve_close(mczi_server* srv);
  * `d_packed` (>= text_len/16 + 8 words) receives the bases, 16 per word,
  * MSB-first, A0 C1 G2 T3; `d_fbits` (>= text_len/32 + 8 words) one bit per
  * base, set where a fragment (a maximal A/C/G/T run of one record) starts.
- * Both are cleared by the call.  *n_bases (host) receives the base count; the
- * call synchronises `stream` before returning.
+ * Both are cleared by the call.  *n_bases (host) receives the base count: the
+ * call copies it from the device and synchronises `stream` before returning.
  *
- * Scratch: an 8 MiB array in device memory, reserved once per process on every
- * GPU that loads this library and held until exit.  The first call on a device
- * looks its address up (cudaGetSymbolAddress) with that device current; make
- * that first call before any stream capture.  Every call shares the array, so
- * calls that overlap on the GPU race: issue them one at a time. */
+ * Scratch: an 8 MiB array in device memory, part of this library's CUDA
+ * module, reserved on a device when the module loads there (at library load
+ * with eager module loading; at the first use on that device, normally the
+ * first call, with lazy loading) and held until the process exits.  The first
+ * call on a device looks its address up (cudaGetSymbolAddress) with that
+ * device current and keeps it for the life of the device's primary context
+ * (do not call again on a device after cudaDeviceReset); make that first call
+ * before any stream capture.  Every call shares the array, so calls that
+ * overlap on the GPU race: issue them one at a time. */
 int32_t mczi_pack_fastx_noalloc(const uint8_t* d_text, uint64_t text_len, int32_t fastq, uint32_t* d_packed,
                                 uint64_t packed_words, uint32_t* d_fbits, uint64_t fbits_words, uint64_t* n_bases,
                                 void* stream);

@@ -2,22 +2,30 @@
 // allocate device memory.
 //
 // Some callers cannot call cudaMalloc at the point where they need the
-// packer: code running while a CUDA stream is being captured into a graph,
-// services that hand out device memory only from their own pre-sized arena,
-// or real-time request paths where an allocation (and the device-wide
-// synchronisation it can cause) is not acceptable.  For them this entry point
-// runs the same three packing kernels as mczi_count's first phase, but keeps
-// their per-tile scratch (line and base summaries and the scan temporaries)
-// in one file-scope device array of fixed size instead of context buffers.
+// packer: services that hand out device memory only from their own pre-sized
+// arena (a cudaMalloc behind the arena's back breaks its accounting and can
+// fail once the arena holds the free HBM), or real-time request paths where
+// an allocation -- and the device-wide synchronisation it can cause -- is not
+// acceptable.  For them this entry point runs the same three packing kernels
+// as mczi_count's first phase, but keeps their per-tile scratch (line and
+// base summaries and the scan temporaries) in one file-scope device array of
+// fixed size instead of context buffers.  The call ends by copying the base
+// count to the host and synchronising the caller's stream.
 //
-// The array is reserved once per process on every GPU that loads the library
-// and lives until exit.  Its host-side name is only a stand-in: the device
-// address is looked up with cudaGetSymbolAddress, once per device, with that
-// device current, on the first call on that device (make that first call
-// before any stream capture).  All calls share the array and it keeps the
-// contents of the last call; everything that must start at zero is cleared on
-// each call, and calls that overlap on the GPU (several streams, several host
-// threads) race on it -- serialise them.
+// The array belongs to this library's CUDA module: it is reserved on a device
+// when the module is loaded there -- when the library is loaded under eager
+// module loading, at the first kernel launch or symbol lookup on that device
+// under lazy loading (CUDA_MODULE_LOADING=LAZY, the default since CUDA 12) --
+// and held until the process exits.  Its host-side name is only a stand-in:
+// the device address is looked up with cudaGetSymbolAddress, once per device,
+// with that device current, on the first call on that device (make that
+// first call before any stream capture, since the lookup may load the module).
+// The cached address is valid for the life of the device's primary context:
+// a caller that ends it (cudaDeviceReset) must not call this entry point on
+// that device again in the same process.  All calls share the array and it
+// keeps the contents of the last call; everything that must start at zero is
+// cleared on each call, and calls that overlap on the GPU (several streams,
+// several host threads) race on it -- serialise them.
 #include "../../include/mczi_gpu.h"
 #include "mczi_internal.h"
 #include "scan.cuh"

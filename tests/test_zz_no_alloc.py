@@ -1,14 +1,15 @@
 """The no-allocation packer (mczi_pack_fastx_noalloc) against the packer of
-the regular entry point.
+the regular entry point and the oracle.
 
-Callers that cannot allocate device memory -- code inside a CUDA graph
-capture, services that only hand out memory from their own arena, or paths
-where a cudaMalloc is not allowed -- call mczi_pack_fastx_noalloc with their
+Callers that cannot allocate device memory -- services that only hand out
+HBM from their own pre-sized arena, or paths where a cudaMalloc and its
+synchronisation are not allowed -- call mczi_pack_fastx_noalloc with their
 own device buffers; its scratch is a fixed static device array.  This test
 runs it twice in a row (so the second call sees the first call's leftovers in
 the shared scratch) and checks both outputs bit for bit against the codes and
-fragment starts produced by mczi_count.  It lives in its own file, collected
-last, and passes both alone in a fresh process and after the other tests.
+fragment starts produced by mczi_count, and the codes against the oracle's
+fragments.  It lives in its own file, collected last, and passes both alone
+in a fresh process and after the other tests.
 """
 import ctypes as C
 
@@ -44,6 +45,7 @@ def _unpack(packed, fbits, n):
 
 def test_noalloc_packer_matches_count_entry_point():
     torch = pytest.importorskip("torch")
+    import oracle_ref
     from mczi_gb300 import build
     build.build_gpu_lib()
     from mczi_gb300 import _native
@@ -74,6 +76,12 @@ def test_noalloc_packer_matches_count_entry_point():
                                     nb.value)
             assert np.array_equal(codes, exp_codes)
             assert np.array_equal(starts, exp_starts)
+            # and directly against the oracle's fragments of the same bytes
+            o_codes, o_offs, _ = oracle_ref.fragments(raw, 1)
+            o_starts = np.zeros(o_codes.size, dtype=np.uint8)
+            o_starts[o_offs[:-1].astype(np.int64)] = 1
+            assert np.array_equal(codes, o_codes)
+            assert np.array_equal(starts, o_starts)
         # sizes beyond the fixed maximum and unpadded lengths are rejected
         rc = lib.mczi_pack_fastx_noalloc(C.c_void_p(d_text.data_ptr()), (65536 + 1) * TILE, 0,
                                          C.c_void_p(d_packed.data_ptr()), (1 << 40), C.c_void_p(d_fbits.data_ptr()),
