@@ -15,6 +15,13 @@ superkmer partition, per-bucket counting and the `> x` threshold.
           copy of the FASTA from pinned memory, the count, and the
           device->host read of every kept record, inside the timed region.
 The inputs (4 GB) are larger than L2 (126 MB), so no L2 flush is needed.
+* parity: the device digest of the timed run's result against the oracle's
+          digest of the same generator output (tests/golden/digests.json).
+* zi / zi_serve (N = 1): the ZI halves of the metric on the same GPU -- ZI
+          subtraction of a 2 Gbp query against a 60 Mbp index, batched vs one
+          pipeline per file (union checked against the oracle digest), and
+          the serving sweep (p50/p99 at offered loads 0.2..1.0; the request
+          count per load is stated; --workload zi-serve runs 10,000).
 
 `--impl reference` times the CPU implementation of the same path on the host
 cores: the reference is Rust and cannot be built here (no cargo/rustc), so
@@ -258,6 +265,11 @@ def run_ours(args):
     e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / args.steps)
     e2e_value = nb_all / (e2e_ms * 1e-3) / 1e9
     d2h = n_records * (8 + (8 if k > 32 else 0) + 8)
+    # parity of the timed run: the digest of the last end-to-end result
+    # against the oracle's digest of the same generator output
+    from mczi_gb300 import gen
+    parity = digest_check(WORKLOAD["workload"], args.scale, [gen.fingerprint_ptr(buf.data_ptr(), nbytes)],
+                          ctx.digest())
 
     # ---- roofline of the dominant kernel
     names = ["pack", "scan", "partition", "count"]
@@ -306,15 +318,40 @@ def run_ours(args):
                               "onchip_frac": round(sum(own.values()) / (dev_ms * 1e-3) / 1e9 / peak, 4)},
         "clocks": clk,
     }
+    line["parity"] = parity
+    ctx.close()
+    del buf, pin, out, rec
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args)
-    ctx.close()
+    if ws == 1 and not args.no_zi:
+        # the ZI halves of the metric on the same GPU: batched vs plain
+        # subtraction at full size (its union checked against the oracle
+        # digest) and the serving sweep
+        line["zi"] = zi_measure(args.scale, args.zi_files, args.line_zi_steps, 1)
+        line["zi_serve"] = zi_serve_measure(args.scale, args.line_serve_requests, args.serve_workers,
+                                            args.serve_max_bytes, args.serve_pool_bases)
     if rank == 0:
         print(json.dumps(line), flush=True)
     group.close()
 
 
-def cpu_baseline(args, sample_scale: float | None = None):
+def digest_check(name: str, scale: float, fingerprints, got: dict) -> dict:
+    """Compares a GPU result digest with the oracle's digest of the same
+    input, committed in tests/golden/digests.json by
+    tests/golden/make_digests.py (full-size inputs only)."""
+    p = ROOT / "tests" / "golden" / "digests.json"
+    entry = json.loads(p.read_text()).get(name) if p.exists() else None
+    if not entry or entry["scale"] != scale:
+        return {"digest_match": None, "scale": scale, "records": got["records"],
+                "reason": "no committed oracle digest at this scale"}
+    same_input = list(fingerprints) == entry["input_fingerprints"]
+    return {"digest_match": bool(same_input and got == entry["digest"]), "input_match": same_input,
+            "scale": scale, "records": got["records"], "digest": got,
+            "oracle": "digest of the oracle's exact result for the same generator output, committed with the script "
+                      "that made it (tests/golden/digests.json)"}
+
+
+def cpu_baseline(args, sample_scale: float | None = None, data=None):
     """The C restatement (oracle/, OpenMP over all host cores) on a bounded
     sample of the same workload: the same generator at a smaller scale."""
     sys.path.insert(0, str(ROOT / "tests"))
@@ -322,7 +359,8 @@ def cpu_baseline(args, sample_scale: float | None = None):
     from mczi_gb300 import gen
     from mczi_gb300._native import default_threads
     scale = sample_scale if sample_scale is not None else args.cpu_sample_scale
-    data = gen.c2_reads(scale)
+    if data is None:
+        data = gen.c2_reads(scale)
     threads = default_threads()
     t0 = time.perf_counter()
     lo, hi, cnt = oracle_ref.count([data], WORKLOAD["k"], WORKLOAD["x"], 0, threads)
@@ -338,18 +376,22 @@ def run_reference(args):
     ws, rank, _ = env()
     if rank != 0:
         return
+    from mczi_gb300 import gen
+    scale = args.ref_sample_scale
+    data = gen.c2_reads(scale)  # one sample, counted afresh every step
     steps = []
-    for _ in range(args.warmup):
-        pass  # the CPU port has no warm-up state worth priming beyond page-in
     cb = None
+    for _ in range(min(args.warmup, 1)):  # page-in; the port keeps no state between steps
+        cpu_baseline(args, scale, data)
     for _ in range(args.steps):
-        cb = cpu_baseline(args, args.ref_sample_scale)
+        cb = cpu_baseline(args, scale, data)
         steps.append(cb["value"])
     value = statistics.median(steps)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "impl": "reference", "dtype": "u8/u128", "data": "synthetic (seeded generator, no dataset)",
-            "config": dict(WORKLOAD, parallelism="cpu"),
+            "config": dict(WORKLOAD, parallelism="cpu", scale=scale, bases=int(WORKLOAD["read_bases"] * scale),
+                           warmup_steps_run=min(args.warmup, 1)),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cb["cores"], "kind": "port",
                              "sample": cb["sample"] + "; the Rust reference cannot be built here (no cargo/rustc)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -500,28 +542,33 @@ def _record_starts(buf) -> "np.ndarray":
     return np.flatnonzero(buf == ord(">"))
 
 
-def run_zi(args):
+def zi_measure(scale: float, nfiles: int, steps: int, warmup: int, one_group: bool = False) -> dict:
     """ZI subtraction, batched vs plain: the index is the k-mer set of a 60 Mbp
     random genome (as overlapping chunks, the same set as MC's k=31 x=1 FASTA of
     that genome fed twice); the query is 2 Gbp of 150 bp reads, half from that
     genome and half from an independent one, 1 % errors, split into files.
-    Batched = all files in one set of launches; plain = one pipeline per file
-    (its own launches and syncs), absent sets merged on the host."""
+    Batched = all files in groups of <= 64, one set of launches per group with
+    a result per file; plain = one pipeline per file (its own launches and
+    syncs).  The union query (the reference's one absent set over all files)
+    is checked against the oracle digest committed for the full-size input."""
     import numpy as np
     import torch
     from mczi_gb300 import build, gen, zi
     from mczi_gb300.mc import Context
     build.build_all()
     k, m = 31, 19
-    glen = int(60_000_000 * args.scale)
-    qbases = int(2_000_000_000 * args.scale)
+    glen = int(60_000_000 * scale)
+    qbases = int(2_000_000_000 * scale)
+    t0 = time.perf_counter()
     index, query = gen.c4_index_and_query(genome_len=glen, query_bases=qbases, k=k)
+    gen_s = time.perf_counter() - t0
+    fps = [gen.fingerprint(index), gen.fingerprint(query)]
     # the query sits in pinned host memory, as a server's receive buffers would
     pinned = torch.empty(query.size, dtype=torch.uint8, pin_memory=True)
     pinned.numpy()[:] = query
+    del query
     query = pinned.numpy()
     starts = _record_starts(query)
-    nfiles = args.zi_files
     cuts = [int(starts[int(i * len(starts) / nfiles)]) for i in range(nfiles)] + [query.size]
     files = [query[cuts[i]:cuts[i + 1]] for i in range(nfiles)]
     windows = int(qbases / 150) * (150 - k + 1)
@@ -530,33 +577,31 @@ def run_zi(args):
     ctx.set_stream(stream.cuda_stream)
     zi.build_dictionary(index, k, m, ctx=ctx)
     info = zi.info(ctx)
-    if args.zi_one_group:
+    if one_group:
         # for kernel profiles: one 50-file group (every 4th file: half in-index
         # reads, half foreign, like the whole query) per input, then as a union
         group = files[::4][:50]
+        out = []
         for name, run in (("per_input", zi.query_per_input), ("union", zi.query)):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             n = run(ctx, group)
             torch.cuda.synchronize()
-            print(json.dumps({"query": name, "files": len(group), "records": n,
-                              "ms": round((time.perf_counter() - t0) * 1e3, 3),
-                              "phases_ms": [round(x, 3) for x in ctx.phase_times()[:5]],
-                              "stats": ctx.run_stats()[:8]}), flush=True)
+            out.append({"query": name, "files": len(group), "records": n,
+                        "ms": round((time.perf_counter() - t0) * 1e3, 3),
+                        "phases_ms": [round(x, 3) for x in ctx.phase_times()[:5]], "stats": ctx.run_stats()[:8]})
         ctx.close()
-        return
-    # batched: files in balanced groups of at most 64 (one mask word per
-    # record), each group one set of launches with a result per file
+        return {"one_group": out}
     ngroups = -(-nfiles // 64)
     groups = [files[i * nfiles // ngroups:(i + 1) * nfiles // ngroups] for i in range(ngroups)]
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         for g in groups:
             zi.query_per_input(ctx, g)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     phases = [0.0] * 5
-    qsk = qbases_packed = 0
-    for _ in range(args.steps):
+    qsk = qbases_packed = n_rec = 0
+    for _ in range(steps):
         n_rec = 0
         qsk = qbases_packed = 0
         for g in groups:
@@ -566,8 +611,8 @@ def run_zi(args):
             qbases_packed += st[0]
             qsk += st[2]
     torch.cuda.synchronize()
-    batched_s = (time.perf_counter() - t0) / args.steps
-    phases = [x / args.steps for x in phases]
+    batched_s = (time.perf_counter() - t0) / steps
+    phases = [x / steps for x in phases]
     # per-file result lists of the last group, split on the device
     t0 = time.perf_counter()
     split = zi.batch_results(ctx, len(groups[-1]))
@@ -581,62 +626,79 @@ def run_zi(args):
         sizes.append(zi.query(ctx, [f]))
         lat.append(time.perf_counter() - t1)
     plain_s = time.perf_counter() - t0
-    # the reference's union semantics (one absent set over all files)
+    # the reference's union semantics (one absent set over all files), with
+    # its digest against the oracle's
     t0 = time.perf_counter()
     n_absent = zi.query(ctx, files)
     union_s = time.perf_counter() - t0
+    union_digest = ctx.digest(unit_counts=True)
+    parity = digest_check("zi_subtract_2gbp_k31", scale, fps, union_digest)
     # spot-check: per-file results of the batch equal the per-file runs
     zi.query_per_input(ctx, files[:4])
     chk = zi.batch_results(ctx, 4)
     for i in range(4):
         assert len(chk[i]) == sizes[i], (i, len(chk[i]), sizes[i])
-    from mczi_gb300.serve import percentile
-    line = {"metric": "ZI queries/s", "value": round(windows / batched_s, 1), "unit": "k-mer lookups/s",
-            "impl": "ours", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-            "config": {"workload": "zi_subtract_2gbp_k31", "k": k, "m": m, "index_genome_bp": glen,
-                       "index_kmers": info["index_bases"], "query_bases": qbases, "query_files": nfiles,
-                       "mphf_levels": info["mphf_levels"], "minimizers": info["minimizers"],
-                       "index_build_ms": info["build_us"] / 1000.0, "records_batched": n_rec},
-            "batched": {"s": round(batched_s, 4), "lookups_per_s": round(windows / batched_s, 1),
-                        "groups": ngroups, "split_last_group_ms": round(split_s * 1e3, 3),
-                        "split_last_group_kmers": int(sum(len(x) for x in split)),
-                        "phases_ms": dict(zip(["pack", "scan", "partition", "dedup_count", "probe"],
-                                              [round(x, 3) for x in phases]))},
-            "plain": {"s": round(plain_s, 4), "lookups_per_s": round(windows / plain_s, 1),
-                      "file_p50_ms": round(percentile(lat, 50) * 1e3, 3),
-                      "file_p99_ms": round(percentile(lat, 99) * 1e3, 3)},
-            "batched_over_plain": round(plain_s / batched_s, 2),
-            # for information (figure of record: FASTA once, 2-bit stream written and
-            # read, 96 B per query superkmer for MPHF / offsets / strings, records out)
-            "roofline": {"bound": "hbm", "kernel": "whole batched query", "unit": "GB/s",
-                         "algorithmic_bytes": int(query.size + qbases_packed / 2 + 96 * qsk + 16 * n_rec),
-                         "achieved": round((query.size + qbases_packed / 2 + 96 * qsk + 16 * n_rec) / batched_s / 1e9, 1),
-                         "peak": load_peaks()[0],
-                         "frac": round((query.size + qbases_packed / 2 + 96 * qsk + 16 * n_rec) / batched_s / 1e9
-                                       / load_peaks()[0], 4)},
-            "union": {"s": round(union_s, 4), "lookups_per_s": round(windows / union_s, 1), "absent_kmers": n_absent},
-            "data": "synthetic (seeded generator, no dataset)"}
     ctx.close()
+    from mczi_gb300.serve import percentile
+    alg = query.size + qbases_packed / 2 + 96 * qsk + 16 * n_rec
+    return {
+        "metric": "ZI queries/s", "value": round(windows / batched_s, 1), "unit": "k-mer lookups/s",
+        "steps": steps, "warmup": warmup,
+        "config": {"workload": "zi_subtract_2gbp_k31", "k": k, "m": m, "index_genome_bp": glen,
+                   "index_kmers": info["index_bases"], "query_bases": qbases, "query_files": nfiles,
+                   "mphf_levels": info["mphf_levels"], "minimizers": info["minimizers"],
+                   "index_build_ms": info["build_us"] / 1000.0, "records_batched": n_rec, "scale": scale,
+                   "generate_s": round(gen_s, 1)},
+        "batched": {"s": round(batched_s, 4), "lookups_per_s": round(windows / batched_s, 1),
+                    "groups": ngroups, "split_last_group_ms": round(split_s * 1e3, 3),
+                    "split_last_group_kmers": int(sum(len(x) for x in split)),
+                    "phases_ms": dict(zip(["pack", "scan", "partition", "dedup_count", "probe"],
+                                          [round(x, 3) for x in phases]))},
+        "plain": {"s": round(plain_s, 4), "lookups_per_s": round(windows / plain_s, 1),
+                  "file_p50_ms": round(percentile(lat, 50) * 1e3, 3),
+                  "file_p99_ms": round(percentile(lat, 99) * 1e3, 3)},
+        "batched_over_plain": round(plain_s / batched_s, 2),
+        # for information (figure of record: FASTA once, 2-bit stream written and
+        # read, 96 B per query superkmer for MPHF / offsets / strings, records out)
+        "roofline": {"bound": "hbm", "kernel": "whole batched query", "unit": "GB/s", "algorithmic_bytes": int(alg),
+                     "achieved": round(alg / batched_s / 1e9, 1), "peak": load_peaks()[0],
+                     "frac": round(alg / batched_s / 1e9 / load_peaks()[0], 4)},
+        "union": {"s": round(union_s, 4), "lookups_per_s": round(windows / union_s, 1), "absent_kmers": n_absent,
+                  "digest": union_digest},
+        "parity": parity,
+    }
+
+
+def run_zi(args):
+    r = zi_measure(args.scale, args.zi_files, args.steps, args.warmup, args.zi_one_group)
+    if "one_group" in r:
+        for x in r["one_group"]:
+            print(json.dumps(x), flush=True)
+        return
+    line = dict(r, impl="ours", n_gpus=1, higher_is_better=True, data="synthetic (seeded generator, no dataset)")
     print(json.dumps(line), flush=True)
 
 
-def run_zi_serve(args):
+def zi_serve_measure(scale: float, requests: int, workers: int, max_bytes: float, pool_bases: float,
+                     loads=(0.2, 0.4, 0.6, 0.8, 1.0)) -> dict:
     """ZI serving through the library's native loop (mczi_serve_*): the index
-    stays resident; requests of log-uniform size (10 kbp .. 200 Mbp, sliced
-    from a pool of reads) arrive as a Poisson process at offered loads
-    0.2 .. 1.0 of the measured batched peak; p50/p99 latency (submit to
-    result) and aggregate bases/s."""
+    stays resident; requests of log-uniform size (10 kbp .. max_bytes, sliced
+    without copying from a pool of reads) arrive as a Poisson process at
+    offered loads of the measured batched peak; p50/p99 latency (submit to
+    result, timed by the native server) and aggregate bases/s.  Each answered
+    request's absent set is copied to the host and then dropped, so a sweep of
+    10,000 requests per load holds only the requests in flight."""
     import numpy as np
     from mczi_gb300 import build, gen, zi
     from mczi_gb300.mc import Context
     from mczi_gb300.serve import ZIServer, percentile
     build.build_all()
     k, m = 31, 19
-    glen = int(60_000_000 * args.scale)
-    index, pool = gen.c4_index_and_query(genome_len=glen, query_bases=int(args.serve_pool_bases), k=k)
+    glen = int(60_000_000 * scale)
+    index, pool = gen.c4_index_and_query(genome_len=glen, query_bases=int(pool_bases), k=k)
     starts = _record_starts(pool)
     rng = np.random.default_rng(5)
-    lo_b, hi_b = 10_000, int(args.serve_max_bytes)
+    lo_b, hi_b = 10_000, int(max_bytes)
 
     def make_request():
         size = int(np.exp(rng.uniform(np.log(lo_b), np.log(hi_b))))
@@ -644,7 +706,7 @@ def run_zi_serve(args):
         a = int(starts[i0])
         j = int(np.searchsorted(starts, a + size))
         b = int(starts[j]) if j < len(starts) else pool.size
-        return pool[a:b].tobytes()
+        return pool[a:b]  # a view: the server reads the pool's bytes in place
 
     # measured peak: one large batched request stream
     ctx = Context(0)
@@ -656,40 +718,50 @@ def run_zi_serve(args):
     peak_bps = sum(len(p) for p in probe) / (time.perf_counter() - t0)
     ctx.close()
     points = []
-    with ZIServer(index, k, m, workers=args.serve_workers, max_batch=64) as srv:
-        for load in (0.2, 0.4, 0.6, 0.8, 1.0):
+    with ZIServer(index, k, m, workers=workers, max_batch=64) as srv:
+        for load in loads:
             st0 = srv.stats()
-            reqs = [make_request() for _ in range(args.serve_requests)]
+            reqs = [make_request() for _ in range(requests)]
             mean = sum(len(r) for r in reqs) / len(reqs)
             rate = load * peak_bps / mean
             arr = np.cumsum(rng.exponential(1.0 / rate, size=len(reqs)))
-            futs = []
+            lat, queue = [], []
+            done = threading.Semaphore(0)
+
+            def finished(f):
+                lat.append(f.latency_ms)
+                queue.append(f.queue_ms)
+                done.release()  # the future (and its absent set) is dropped after this
+
             t_start = time.perf_counter()
             for r, at in zip(reqs, arr):
                 d = t_start + at - time.perf_counter()
                 if d > 0:
                     time.sleep(d)
-                futs.append(srv.submit(r))
-            for f in futs:
-                f.result()
+                srv.submit(r).add_done_callback(finished)
+            for _ in reqs:
+                done.acquire()
             t_end = time.perf_counter()
             st1 = srv.stats()
-            lat = [f.latency_ms for f in futs]  # submit to result, timed by the native server
             nb = st1["batches"] - st0["batches"]
             points.append({"offered_load": load, "requests": len(reqs), "p50_ms": round(percentile(lat, 50), 3),
-                           "p99_ms": round(percentile(lat, 99), 3),
-                           "queue_p99_ms": round(percentile([f.queue_ms for f in futs], 99), 3),
+                           "p99_ms": round(percentile(lat, 99), 3), "queue_p99_ms": round(percentile(queue, 99), 3),
                            "throughput_bases_per_s": round(sum(len(r) for r in reqs) / (t_end - t_start), 1),
+                           "mean_request_bytes": round(mean), "wall_s": round(t_end - t_start, 2),
                            "mean_batch": round((st1["requests"] - st0["requests"]) / max(1, nb), 2),
                            "batches": int(nb), "query_s": round(st1["query_s"] - st0["query_s"], 3),
                            "results_s": round(st1["results_s"] - st0["results_s"], 3)})
-    line = {"metric": "ZI-serve p99 ms", "value": points[-1]["p99_ms"], "unit": "ms", "impl": "ours",
-            "higher_is_better": False, "n_gpus": 1,
-            "config": {"workload": "zi_serve_k31", "index_genome_bp": glen, "workers": args.serve_workers,
-                       "request_bytes": [lo_b, hi_b], "requests_per_load": args.serve_requests,
-                       "peak_bytes_per_s": round(peak_bps, 1)},
-            "sweep": points, "data": "synthetic (seeded generator, no dataset)"}
-    print(json.dumps(line), flush=True)
+    return {"metric": "ZI-serve p99 ms", "value": points[-1]["p99_ms"], "unit": "ms", "higher_is_better": False,
+            "config": {"workload": "zi_serve_k31", "index_genome_bp": glen, "workers": workers,
+                       "request_bytes": [lo_b, hi_b], "requests_per_load": requests,
+                       "peak_bytes_per_s": round(peak_bps, 1), "arrivals": "Poisson"},
+            "sweep": points}
+
+
+def run_zi_serve(args):
+    r = zi_serve_measure(args.scale, args.serve_requests, args.serve_workers, args.serve_max_bytes,
+                         args.serve_pool_bases)
+    print(json.dumps(dict(r, impl="ours", n_gpus=1, data="synthetic (seeded generator, no dataset)")), flush=True)
 
 
 def main():
@@ -699,8 +771,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scale", type=float, default=1.0, help="workload scale (1.0 = 4 Gbp)")
-    ap.add_argument("--cpu-sample-scale", type=float, default=0.005)
-    ap.add_argument("--ref-sample-scale", type=float, default=0.004)
+    ap.add_argument("--cpu-sample-scale", type=float, default=0.05)
+    ap.add_argument("--ref-sample-scale", type=float, default=0.05)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the untimed autotuning on a sample")
     ap.add_argument("--no-graph", action="store_true", help="skip the graph-replay timing")
@@ -708,7 +780,12 @@ def main():
     ap.add_argument("--zi-files", type=int, default=200)
     ap.add_argument("--zi-one-group", action="store_true",
                     help="run one 50-file group (per input, then union) and exit: the case for ZI kernel profiles")
-    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-requests", type=int, default=10_000,
+                    help="requests per offered load of --workload zi-serve (the default MC line runs "
+                         "--line-serve-requests)")
+    ap.add_argument("--line-serve-requests", type=int, default=500)
+    ap.add_argument("--line-zi-steps", type=int, default=3)
+    ap.add_argument("--no-zi", action="store_true", help="MC only: skip the ZI keys of the default line")
     ap.add_argument("--serve-workers", type=int, default=2)
     ap.add_argument("--serve-max-bytes", type=float, default=200e6)
     ap.add_argument("--serve-pool-bases", type=float, default=600e6)

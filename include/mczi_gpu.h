@@ -91,6 +91,15 @@ int32_t mczi_count_staged(mczi_ctx* ctx, const mczi_counter_config* cfg, int32_t
 int32_t mczi_result_copy(mczi_ctx* ctx, uint64_t* key_lo, uint64_t* key_hi, uint64_t* counts, uint64_t cap,
                          int32_t sorted);
 
+/* Order-independent digest of the last result's records, computed on the
+ * device (no reference counterpart: a check for comparing a large result with
+ * one computed elsewhere without moving the records).  out[0] = records,
+ * out[1] = sum of counts, out[2] = wrapping sum and out[3] = xor over the
+ * records of mix(mix(mix(lo) ^ hi) + count), mix = the murmur3 64-bit
+ * finaliser, hi = 0 for k <= 32; unit_counts != 0 digests every count as 1
+ * (a ZI absent set compared as a set). */
+int32_t mczi_result_digest(mczi_ctx* ctx, int32_t unit_counts, uint64_t* out);
+
 /* KFF file of the last count (src/lib.rs:1633-1670, 3071-3121): count bytes 1
  * (mode 0, k <= 32, counts saturated at min(x+1, 255)), 8 (mode 0, k > 32) or
  * 4 (mode 1), as MC's count_inputs_to_kff_path / count_datasets_to_kff_path. */
@@ -99,8 +108,11 @@ int32_t mczi_result_write_kff(mczi_ctx* ctx, const char* path);
  * count_inputs_to_fasta_path / count_datasets_to_fasta_path. */
 int32_t mczi_result_write_fasta(mczi_ctx* ctx, const char* path);
 
-/* Path-based drop-ins for the MC library entry points (plain FASTA/FASTQ files;
- * compressed inputs are decompressed by the caller):
+/* Path-based drop-ins for the MC library entry points.  The files are
+ * FASTA/FASTQ, plain or gzip / xz / zstd compressed (recognised by their
+ * magic bytes, decoded with the system's zlib / liblzma / libzstd loaded at
+ * run time, several files on parallel host threads), as MC reads them
+ * (src/lib.rs:3127-3143, 3218-3226):
  *   count_inputs_to_kff_path   src/lib.rs:457
  *   count_inputs_to_fasta_path src/lib.rs:427
  *   count_datasets_to_kff_path src/lib.rs:509
@@ -182,6 +194,14 @@ int32_t mczi_set_streamed_staging(mczi_ctx* ctx, int32_t enable, uint64_t segmen
  * the packed stream; *n_bases receives the base count. */
 int32_t mczi_debug_packed(mczi_ctx* ctx, uint8_t* codes, uint8_t* starts, uint64_t cap, uint64_t* n_bases);
 
+/* Test hook (no reference counterpart): the counting kernel keeps per-bin
+ * occupancies, their prefix and per-k-mer counts in 32-bit counters, each
+ * bounded by the k-mer windows of one minimizer bucket; a bucket with more
+ * than 2^32 - 1 windows makes the count fail with MCZI_ERR_TOO_LARGE instead
+ * of wrapping.  This lowers that limit (0 restores 2^32 - 1) so the error
+ * path can be exercised on small inputs. */
+int32_t mczi_debug_set_bucket_window_limit(mczi_ctx* ctx, uint64_t windows);
+
 /* ---------------------------------------------------------------- ZI */
 
 /* build_dictionary (src/zi.rs:114-141): indexes the canonical k-mers of the
@@ -198,6 +218,13 @@ int32_t mczi_zi_build(mczi_ctx* ctx, const uint8_t* index_fasta, uint64_t len, u
  * (counts are the number of absent occurrences), mczi_result_write_fasta
  * writes them as simplitigs like write_novel_simplitigs (src/zi.rs:177-189). */
 int32_t mczi_zi_query(mczi_ctx* ctx, const mczi_input* queries, size_t n, uint64_t* n_absent);
+
+/* Path-based forms of the two ZI seams (build_dictionary src/zi.rs:114 and
+ * collect_query_kmers_absent_from_index src/zi.rs:152, whose callers pass
+ * paths, src/zi.rs:85-96): the files are plain or gzip / xz / zstd
+ * compressed FASTA, read as the MC path-based entry points read them. */
+int32_t mczi_zi_build_path(mczi_ctx* ctx, const char* index_path, uint32_t k, uint32_t m);
+int32_t mczi_zi_query_paths(mczi_ctx* ctx, const char* const* query_paths, size_t n, uint64_t* n_absent);
 
 /* The same for a batch of independent requests (one input each) in one set
  * of launches: each absent k-mer carries the set of inputs it is absent
@@ -229,6 +256,15 @@ int32_t mczi_zi_info(mczi_ctx* ctx, uint64_t* out, int32_t cap);
  * of <= 256 buckets or two; 0 = automatic (half the shared-memory table).
  * Smaller values only add partition work; results are identical. */
 int32_t mczi_set_zi_bucket_records(mczi_ctx* ctx, uint32_t records);
+
+/* Reads one FASTA/FASTQ file as the path-based entry points do (plain, or
+ * gzip / xz / zstd decoded on the host; no reference counterpart beyond its
+ * readers, src/lib.rs:3127-3143): *data receives a buffer of *len bytes
+ * allocated by the library, released with mczi_free_input.  On failure
+ * (MCZI_ERR_IO: unreadable file, corrupt stream, or the decoding library
+ * missing) the message is written to err (err_cap bytes, may be NULL). */
+int32_t mczi_read_input_file(const char* path, uint8_t** data, uint64_t* len, char* err, uint64_t err_cap);
+void mczi_free_input(uint8_t* data);
 
 /* ------------------------------------------------------------- ZI serving */
 

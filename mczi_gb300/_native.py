@@ -62,6 +62,7 @@ SIGNATURES = [
     ("mczi_stage", C.c_int32, [C.c_void_p, C.POINTER(InputC), C.c_size_t]),
     ("mczi_count_staged", C.c_int32, [C.c_void_p, C.POINTER(CounterConfigC), C.c_int32, C.POINTER(C.c_uint64)]),
     ("mczi_result_copy", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int32]),
+    ("mczi_result_digest", C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_uint64)]),
     ("mczi_result_write_kff", C.c_int32, [C.c_void_p, C.c_char_p]),
     ("mczi_result_write_fasta", C.c_int32, [C.c_void_p, C.c_char_p]),
     ("mczi_count_inputs_to_kff_path", C.c_int32, [C.c_void_p, C.POINTER(C.c_char_p), C.c_size_t,
@@ -83,8 +84,14 @@ SIGNATURES = [
     ("mczi_set_streamed_staging", C.c_int32, [C.c_void_p, C.c_int32, C.c_uint64]),
     ("mczi_set_zi_bucket_records", C.c_int32, [C.c_void_p, C.c_uint32]),
     ("mczi_debug_packed", C.c_int32, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    ("mczi_debug_set_bucket_window_limit", C.c_int32, [C.c_void_p, C.c_uint64]),
     ("mczi_zi_build", C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32]),
     ("mczi_zi_query", C.c_int32, [C.c_void_p, C.POINTER(InputC), C.c_size_t, C.POINTER(C.c_uint64)]),
+    ("mczi_zi_build_path", C.c_int32, [C.c_void_p, C.c_char_p, C.c_uint32, C.c_uint32]),
+    ("mczi_zi_query_paths", C.c_int32, [C.c_void_p, C.POINTER(C.c_char_p), C.c_size_t, C.POINTER(C.c_uint64)]),
+    ("mczi_read_input_file", C.c_int32, [C.c_char_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_char_p,
+                                         C.c_uint64]),
+    ("mczi_free_input", None, [C.c_void_p]),
     ("mczi_zi_query_per_input", C.c_int32, [C.c_void_p, C.POINTER(InputC), C.c_size_t, C.POINTER(C.c_uint64)]),
     ("mczi_zi_input_result", C.c_int32, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_uint64,
                                          C.POINTER(C.c_uint64)]),
@@ -156,6 +163,8 @@ def gen_lib():
     lib.gen_reads_fasta.restype = C.c_uint64
     lib.gen_chunked_fasta.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64, C.c_uint64, C.c_void_p, C.c_uint64]
     lib.gen_chunked_fasta.restype = C.c_uint64
+    lib.gen_fingerprint.argtypes = [C.c_void_p, C.c_uint64, C.c_int]
+    lib.gen_fingerprint.restype = C.c_uint64
     return lib
 
 

@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-fsigne
               "-I", str(ROOT / "include")] + ARCH
 CUDA_SOURCES = ["mc_pack.cu", "mc_scan.cu", "mc_partition.cu", "mc_count.cu", "mczi_api.cu", "zi.cu",
                 "mc_pack_noalloc.cu", "mc_precount.cu", "simplitig.cu"]
-CXX_SOURCES = ["host_io.cpp", "serve.cpp"]
+CXX_SOURCES = ["host_io.cpp", "serve.cpp", "decompress.cpp"]
 
 
 def nvcc() -> str:
@@ -82,7 +82,7 @@ def build_gpu_lib(force: bool = False) -> Path:
         list(ex.map(_run, jobs))
     lib = LIB_DIR / "libmczi_gpu.so"
     if force or jobs or _stale(lib, objs):
-        _run([nv, "-shared", *ARCH, "-o", str(lib), *map(str, objs), "-lcudart", "-lpthread"])
+        _run([nv, "-shared", *ARCH, "-o", str(lib), *map(str, objs), "-lcudart", "-lpthread", "-ldl"])
     return lib
 
 

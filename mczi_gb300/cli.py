@@ -25,7 +25,7 @@ def _mc_parser() -> argparse.ArgumentParser:
     ap = argparse.ArgumentParser(prog="MC", description="Parallel two-pass pseudo k-mer counter using minimizer "
                                                         "pre-counting (GB300)")
     ap.add_argument("-i", "--input", nargs="+", required=True, type=Path,
-                    help="Input FASTA/FASTQ file(s), optionally gzip or xz compressed")
+                    help="Input FASTA/FASTQ file(s), optionally gzip, xz or zstd compressed")
     ap.add_argument("--fofn", action="store_true",
                     help="Treat --input path(s) as file-of-filenames; -x is a dataset-presence threshold")
     ap.add_argument("-k", "--kmer-size", type=int, required=True, help="K-mer size; must be <= 64")
@@ -44,7 +44,7 @@ def _zi_parser() -> argparse.ArgumentParser:
     ap = argparse.ArgumentParser(prog="ZI", description="Subtract an SSHash-style indexed k-mer set from FASTA/FOFN "
                                                         "FASTA input (GB300)")
     ap.add_argument("--index", type=Path, required=True,
-                    help="FASTA containing k-mers/simplitigs to index and subtract; gzip and xz accepted")
+                    help="FASTA containing k-mers/simplitigs to index and subtract; gzip, xz and zstd accepted")
     ap.add_argument("-i", "--input", nargs="+", required=True, type=Path,
                     help="Query FASTA file(s), or FOFN path(s) when --fofn is set")
     ap.add_argument("--fofn", action="store_true", help="Treat --input path(s) as file-of-filenames")

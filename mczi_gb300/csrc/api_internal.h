@@ -168,6 +168,7 @@ struct mczi_ctx {
   mczi::DevBuf desc, key, desc2, key2, part_hist, bucket_off;
   mczi::DevBuf out_lo, out_hi, out_cnt, out_mask;
   mczi::DevBuf cnt64;  // counts widened to u64 for direct copies to the caller
+  mczi::DevBuf digest_acc;  // mczi_result_digest accumulators (3 u64)
   mczi::DevBuf kff_dev;          // KFF records formatted on the device
   mczi::HostPinned kff_host;     // their host copy, written to the file as is
   mczi::DevBuf sx_keys, sx_tab, sx_rank, sx_ext;  // simplitig writer: sorted keys, key->rank table, extensions
@@ -207,6 +208,7 @@ struct mczi_ctx {
   float count_fill = 0.f;
   int count_chunk = 0;
   int count_filter = -1;
+  uint64_t max_bucket_windows = 0;  // 0 = 2^32 - 1 (the 32-bit counters' range); lowered only by a test hook
   int key_passes = 0;  // 0 = chosen from the input size and free HBM  // two-pass bitmap-filtered rounds: -1 auto (when x >= 1), 0 off, 1 on
 
   mczi::ZiIndex zi;

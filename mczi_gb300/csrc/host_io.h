@@ -37,4 +37,17 @@ void sorted_keys(const HostRecords& r, std::vector<uint64_t>* lo, std::vector<ui
 
 bool read_file(const std::string& path, std::vector<uint8_t>* out, std::string* err);
 
+// Compressed inputs (decompress.cpp): the format is recognised by magic
+// bytes; gzip, xz and zstd decode through the system's zlib, liblzma and
+// libzstd, loaded at run time.
+enum class InputFormat { Plain, Gzip, Xz, Zstd };
+InputFormat input_format(const uint8_t* p, size_t n);
+bool decompress_buffer(const std::vector<uint8_t>& in, std::vector<uint8_t>* out, const std::string& name,
+                       std::string* err);
+// a FASTA/FASTQ file, decompressed when it is gzip, xz or zstd
+bool read_input_file(const std::string& path, std::vector<uint8_t>* out, std::string* err);
+// several files, decoded on parallel host threads; the first failure's message
+bool read_input_files(const char* const* paths, size_t n, std::vector<std::vector<uint8_t>>* out,
+                      std::string* err);
+
 }  // namespace mczi

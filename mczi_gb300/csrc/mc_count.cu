@@ -151,6 +151,7 @@ __global__ void k_count(CountArgs a) {
   uint64_t* dsbase = reinterpret_cast<uint64_t*>(smem + off);  // MODE 1
 
   __shared__ uint32_t s_bucket, s_nused, s_over, s_nrounds, s_sp;
+  __shared__ unsigned long long s_bwin;
   __shared__ RoundRange stack[MAX_STACK];
   __shared__ uint32_t warp_tmp[32];
   __shared__ float s_rho;
@@ -185,18 +186,29 @@ __global__ void k_count(CountArgs a) {
     const uint64_t lo = a.bucket_off[b], hi = a.bucket_off[b + 1];
     if (hi <= lo) continue;
 
-    // ---- per-bin occupancy and descriptor counts
+    // ---- per-bin occupancy and descriptor counts, and the bucket's total
+    // windows in 64 bits: every 32-bit counter below (bin occupancy, its
+    // prefix, a slot's count) is bounded by that total
     const uint64_t* src = a.desc_unsorted ? a.desc_unsorted : a.desc;
     for (int i = tid; i <= NP2; i += nth) { occ[i] = 0; dst[i] = 0; }
+    if (tid == 0) s_bwin = 0;
     __syncthreads();
+    uint64_t my_win = 0;
     for (uint64_t i = lo + tid; i < hi; i += nth) {
       const uint64_t bd = src[i];
       const uint32_t bin = bd_p2(bd);
       const uint32_t len = bd_windows(bd);
       atomicAdd(&occ[bin], len);
       atomicAdd(&dst[bin], 1u);
+      my_win += len;
     }
+    for (int o = 16; o > 0; o >>= 1) my_win += __shfl_xor_sync(0xffffffffu, my_win, o);
+    if (lane == 0 && my_win) atomicAdd(&s_bwin, (unsigned long long)my_win);
     __syncthreads();
+    if (s_bwin > a.max_bucket_windows) {
+      if (tid == 0) set_status(a.status, ST_COUNT_WIDTH);
+      continue;  // uniform: every thread read the same s_bwin
+    }
     // exclusive prefix of both arrays (sequential chunks + warp scan)
     {
       const int per = (NP2 + nth - 1) / nth;

@@ -467,6 +467,7 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       ca.fill = ctx->count_fill > 0.f ? ctx->count_fill : (wide ? 0.4f : 0.6f);
       ca.chunk = ctx->count_chunk > 0 ? (uint32_t)ctx->count_chunk : (wide ? 4u : 2u);
       ca.filter_words = fwords;
+      ca.max_bucket_windows = ctx->max_bucket_windows ? ctx->max_bucket_windows : 0xffffffffull;
       launch_count(ca, s);
       p.launches += 1;
       CK(cudaGetLastError());
@@ -478,6 +479,11 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       CK(cudaStreamSynchronize(s));
       const uint32_t st = (uint32_t)h[SC_STATUS];
       if (st & ST_TABLE_STUCK) return fail(ctx, MCZI_ERR_DEVICE, "counting round could not be split further");
+      if (st & ST_COUNT_WIDTH)
+        return fail(ctx, MCZI_ERR_TOO_LARGE,
+                    "a minimizer bucket holds more than " +
+                        std::to_string(ca.max_bucket_windows) +
+                        " k-mer windows, beyond the counting kernel's 32-bit counters");
       if (st & ST_OUT_OVERFLOW) {
         out_cap = h[SC_NOUT] + (1u << 20);
         continue;
@@ -829,8 +835,8 @@ int32_t run_count_graph(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode,
     CK(cudaMemcpyAsync(h, ctx->scalars.p, sizeof h, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     const uint32_t st = (uint32_t)(h[SC_STATUS] | h[SC_SCANST]);
-    if (st & (ST_DESC_OVERFLOW | ST_OUT_OVERFLOW | ST_TABLE_STUCK)) {
-      drop_graph(ctx);  // these inputs outgrew the captured sizes
+    if (st & (ST_DESC_OVERFLOW | ST_OUT_OVERFLOW | ST_TABLE_STUCK | ST_COUNT_WIDTH)) {
+      drop_graph(ctx);  // these inputs outgrew the captured sizes (or fail on the plain path)
       rc = run_count(ctx, cfg, mode, n_records);
       if (rc == MCZI_OK) capture_pipeline(ctx, cfg, mode, passes);
       return rc;
@@ -923,11 +929,12 @@ int32_t count_paths(mczi_ctx* ctx, const char* const* paths, size_t n, const mcz
   if (rc) return rc;
   if (n == 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, mode ? "at least one dataset file is required"
                                                               : "at least one input file is required");
-  std::vector<std::vector<uint8_t>> data(n);
+  // plain, gzip, xz or zstd files, decoded on parallel host threads
+  std::vector<std::vector<uint8_t>> data;
+  std::string e;
+  if (!read_input_files(paths, n, &data, &e)) return fail(ctx, MCZI_ERR_IO, e);
   std::vector<mczi_input> in(n);
   for (size_t i = 0; i < n; i++) {
-    std::string e;
-    if (!read_file(paths[i], &data[i], &e)) return fail(ctx, MCZI_ERR_IO, e);
     in[i].data = data[i].data();
     in[i].len = data[i].size();
   }
@@ -1080,6 +1087,67 @@ int32_t mczi_result_copy(mczi_ctx* ctx, uint64_t* key_lo, uint64_t* key_hi, uint
   return MCZI_OK;
 }
 
+// order-independent digest of the result records: the murmur3 64-bit
+// finaliser chained over (lo, hi, count); summed (wrapping) and xor-ed over
+// the records, so the value does not depend on emission order
+__device__ __forceinline__ uint64_t dg_mix64(uint64_t x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  return x ^ (x >> 33);
+}
+
+__global__ void k_result_digest(const uint64_t* __restrict__ lo, const uint64_t* __restrict__ hi,
+                                const uint32_t* __restrict__ cnt, uint64_t n, int unit_counts,
+                                unsigned long long* __restrict__ acc) {
+  uint64_t cs = 0, sum = 0, x = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t c = unit_counts ? 1ull : (uint64_t)cnt[i];
+    const uint64_t h = dg_mix64(lo[i]) ^ (hi ? hi[i] : 0ull);
+    const uint64_t w = dg_mix64(dg_mix64(h) + c);
+    cs += c;
+    sum += w;
+    x ^= w;
+  }
+  for (int o = 16; o; o >>= 1) {
+    cs += __shfl_xor_sync(0xffffffffu, cs, o);
+    sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    x ^= __shfl_xor_sync(0xffffffffu, x, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&acc[0], (unsigned long long)cs);
+    atomicAdd(&acc[1], (unsigned long long)sum);
+    atomicXor(&acc[2], (unsigned long long)x);
+  }
+}
+
+int32_t mczi_result_digest(mczi_ctx* ctx, int32_t unit_counts, uint64_t* out) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (!out) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "out must not be NULL");
+  if (!ctx->have_result) return fail(ctx, MCZI_ERR_STATE, "no result");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  const uint64_t n = ctx->n_out;
+  CKA(ctx->digest_acc, 4 * sizeof(uint64_t));
+  CK(cudaMemsetAsync(ctx->digest_acc.p, 0, 4 * sizeof(uint64_t), s));
+  if (n) {
+    const unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx->sm_count * 8);
+    k_result_digest<<<grid, 256, 0, s>>>(ctx->out_lo.as<uint64_t>(), ctx->k > 32 ? ctx->out_hi.as<uint64_t>() : nullptr,
+                                         ctx->out_cnt.as<uint32_t>(), n, unit_counts ? 1 : 0,
+                                         ctx->digest_acc.as<unsigned long long>());
+    CK(cudaGetLastError());
+  }
+  uint64_t acc[4] = {0, 0, 0, 0};
+  CK(cudaMemcpyAsync(acc, ctx->digest_acc.p, 3 * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  out[0] = n;
+  out[1] = acc[0];
+  out[2] = acc[1];
+  out[3] = acc[2];
+  return MCZI_OK;
+}
+
 int32_t mczi_result_write_kff(mczi_ctx* ctx, const char* path) {
   if (!ctx) return MCZI_ERR_STATE;
   if (!ctx->have_result) return fail(ctx, MCZI_ERR_STATE, "no result");
@@ -1223,6 +1291,14 @@ int32_t mczi_set_zi_bucket_records(mczi_ctx* ctx, uint32_t records) {
 int32_t mczi_set_minimizer_precount(mczi_ctx* ctx, int32_t enable) {
   if (!ctx) return MCZI_ERR_STATE;
   ctx->precount = enable ? 1 : 0;
+  return MCZI_OK;
+}
+
+int32_t mczi_debug_set_bucket_window_limit(mczi_ctx* ctx, uint64_t windows) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (windows > 0xffffffffull) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "limit above the 32-bit counters' range");
+  ctx->max_bucket_windows = windows;
+  drop_graph(ctx);
   return MCZI_OK;
 }
 

@@ -148,6 +148,10 @@ struct CountArgs {
   float fill;                 // target fill of a round's table
   uint32_t chunk;             // windows per work item in the insert phase
   uint32_t filter_words;      // > 0: two-pass rounds with a bitmap of this many u32 words (needs x >= 1)
+  // k-mer windows one bucket may hold: the bin occupancies, their prefix and
+  // the per-slot counts are 32-bit and each is bounded by the bucket's
+  // windows; a bucket above this sets ST_COUNT_WIDTH and is not counted
+  uint64_t max_bucket_windows;
 };
 void launch_count(const CountArgs& a, cudaStream_t s);
 size_t count_smem_bytes(int k, int mode, int n_datasets, uint32_t table_slots, uint32_t filter_words);

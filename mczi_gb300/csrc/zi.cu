@@ -28,6 +28,7 @@
 // run descriptors, expanded once into (k-mer, input) records bucketed by
 // k-mer hash, and deduplicated per bucket in shared memory (zi_dedup).
 #include "api_internal.h"
+#include "host_io.h"
 #include "mczi_common.cuh"
 #include "scan.cuh"
 
@@ -1288,6 +1289,28 @@ int32_t mczi_zi_query(mczi_ctx* ctx, const mczi_input* queries, size_t n, uint64
   if (!ctx) return MCZI_ERR_STATE;
   cudaSetDevice(ctx->device);
   return zi_query(ctx, queries, n, false, n_absent);
+}
+
+int32_t mczi_zi_build_path(mczi_ctx* ctx, const char* index_path, uint32_t k, uint32_t m) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (!index_path) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "index path must not be NULL");
+  std::vector<uint8_t> data;
+  std::string e;
+  if (!read_input_file(index_path, &data, &e)) return fail(ctx, MCZI_ERR_IO, e);
+  cudaSetDevice(ctx->device);
+  return zi_build(ctx, data.data(), data.size(), k, m);
+}
+
+int32_t mczi_zi_query_paths(mczi_ctx* ctx, const char* const* query_paths, size_t n, uint64_t* n_absent) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (n == 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "at least one query FASTA is required");
+  std::vector<std::vector<uint8_t>> data;
+  std::string e;
+  if (!read_input_files(query_paths, n, &data, &e)) return fail(ctx, MCZI_ERR_IO, e);
+  std::vector<mczi_input> in(n);
+  for (size_t i = 0; i < n; i++) in[i] = mczi_input{data[i].data(), data[i].size()};
+  cudaSetDevice(ctx->device);
+  return zi_query(ctx, in.data(), n, false, n_absent);
 }
 
 int32_t mczi_zi_query_per_input(mczi_ctx* ctx, const mczi_input* queries, size_t n, uint64_t* n_records) {

@@ -91,6 +91,19 @@ def chunked_fasta(g: np.ndarray, chunk: int, overlap: int) -> np.ndarray:
     return buf
 
 
+def fingerprint(buf) -> str:
+    """64-bit fingerprint (hex) of a generated workload's bytes: equal on two
+    machines iff they generated the same input (the generator is
+    arithmetic-only, so x86_64 and aarch64 hosts agree)."""
+    a = buf if isinstance(buf, np.ndarray) else np.frombuffer(buf, dtype=np.uint8)
+    return "%016x" % lib().gen_fingerprint(a.ctypes.data if a.size else None, a.size, N.default_threads())
+
+
+def fingerprint_ptr(address: int, nbytes: int) -> str:
+    """fingerprint() of `nbytes` bytes at a host address (e.g. a pinned buffer)."""
+    return "%016x" % lib().gen_fingerprint(C.c_void_p(address), nbytes, N.default_threads())
+
+
 @dataclass(frozen=True)
 class Workload:
     name: str

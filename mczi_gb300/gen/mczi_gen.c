@@ -273,3 +273,34 @@ uint64_t gen_chunked_fasta(const uint8_t *genome, uint64_t glen, uint64_t chunk,
     }
     return b;
 }
+
+/* Fingerprint of a byte buffer (to tell whether two machines generated the
+ * same workload): every 1 MiB block is folded 8 bytes at a time by a
+ * rotate-xor-multiply chain seeded with its block index, and the blocks'
+ * mixed values are summed, so the result depends on every byte and its
+ * position and the blocks can be hashed in parallel. */
+static inline uint64_t fp_mix(uint64_t x) {
+    x ^= x >> 33; x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL;
+    return x ^ (x >> 33);
+}
+
+uint64_t gen_fingerprint(const uint8_t *buf, uint64_t len, int threads) {
+    const uint64_t block = 1u << 20;
+    int64_t nblocks = (int64_t)((len + block - 1) / block);
+    uint64_t total = 0;
+#pragma omp parallel for num_threads(threads > 0 ? threads : 1) schedule(static) reduction(+ : total)
+    for (int64_t b = 0; b < nblocks; b++) {
+        uint64_t lo = (uint64_t)b * block, hi = lo + block < len ? lo + block : len;
+        uint64_t h = fp_mix((uint64_t)b + 1), i = lo;
+        for (; i + 8 <= hi; i += 8) {
+            uint64_t w;
+            memcpy(&w, buf + i, 8);
+            h ^= w;
+            h = ((h << 29) | (h >> 35)) * 0x9E3779B97F4A7C15ULL;
+        }
+        for (; i < hi; i++) h = (h ^ buf[i]) * 0x100000001B3ULL;
+        total += fp_mix(h ^ (hi - lo));
+    }
+    return total ^ fp_mix(len);
+}

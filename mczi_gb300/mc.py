@@ -187,6 +187,14 @@ class Context:
                                             cnt.ctypes.data if n else None, n, 1 if sorted else 0))
         return Records(lo, hi, cnt, self.k)
 
+    def digest(self, unit_counts: bool = False) -> dict:
+        """Order-independent digest of the last result, computed on the device
+        (the definition of mczi_gb300.digest.records_digest; unit_counts
+        digests every count as 1, for ZI absent sets)."""
+        out = (C.c_uint64 * 4)()
+        self._ck(self._lib.mczi_result_digest(self._h, 1 if unit_counts else 0, out))
+        return {"records": int(out[0]), "count_sum": int(out[1]), "sum": "%016x" % out[2], "xor": "%016x" % out[3]}
+
     def write_kff(self, path: str | os.PathLike) -> None:
         self._ck(self._lib.mczi_result_write_kff(self._h, os.fsencode(str(path))))
 
@@ -258,18 +266,20 @@ def default_context() -> Context:
 # ------------------------------------------------------------------ helpers
 
 def read_input(path: str | os.PathLike) -> bytes:
-    """Reads a FASTA/FASTQ file, decompressing .gz/.gzip and .xz like MC."""
-    p = Path(path)
-    ext = p.suffix.lower()
-    if ext in (".gz", ".gzip"):
-        with gzip.open(p, "rb") as f:
-            return f.read()
-    if ext == ".xz":
-        with lzma.open(p, "rb") as f:
-            return f.read()
-    if ext in (".zst", ".zstd"):
-        raise N.MCZIError(N.MCZI_ERR_IO, f"zstd input {p} needs a zstd decompressor on the host")
-    return p.read_bytes()
+    """Reads a FASTA/FASTQ file as MC does: plain, or gzip / xz / zstd
+    compressed (recognised by magic bytes; src/lib.rs:3127-3143) and decoded
+    by the library's host-side readers (mczi_read_input_file)."""
+    lib = N.load()
+    data = C.c_void_p()
+    n = C.c_uint64()
+    err = C.create_string_buffer(1024)
+    rc = lib.mczi_read_input_file(os.fsencode(str(path)), C.byref(data), C.byref(n), err, len(err))
+    if rc < 0:
+        raise N.MCZIError(rc, err.value.decode(errors="replace"))
+    try:
+        return C.string_at(data, n.value) if n.value else b""
+    finally:
+        lib.mczi_free_input(data)
 
 
 def expand_fofns(fofns: Iterable[str | os.PathLike]) -> list[Path]:

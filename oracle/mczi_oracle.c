@@ -400,6 +400,190 @@ collect:;
 }
 
 /* ------------------------------------------------------------------ */
+/* order-independent digest of a count's kept records                   */
+/* ------------------------------------------------------------------ */
+
+/* One kept record's digest word; the digest of a result is the record
+ * count, the sum of the counts, and the wrapping sum and the xor of these
+ * words, so it does not depend on record order. */
+static inline uint64_t rec_digest(u128 key, uint64_t count) {
+    return mix64(mix64(mix64((uint64_t)key) ^ (uint64_t)(key >> 64)) + count);
+}
+
+/* Pass of a key in the digest's hash-range passes: a mix of the key hash, so
+ * that the keys of one pass spread over all table slots and shards. */
+static inline int key_pass(uint64_t h, int passes) {
+    return (int)(((mix64(h ^ 0x5851f42d4c957f2dULL) >> 32) * (uint64_t)passes) >> 32);
+}
+
+/* The canonical k-mers of fragments [lo, hi) that fall in pass `p`, pushed to
+ * their shard vectors (the rolling update of for_each_kmer, inlined). */
+static void gen_pass_range(const frags_t *f, uint64_t lo, uint64_t hi, int k, int p, int passes,
+                           vec_t *shards, int n_shards, const table_t *index) {
+    const u128 mask = kmer_mask(k);
+    const int hs = 2 * (k - 1);
+    for (uint64_t fi = lo; fi < hi; fi++) {
+        uint64_t a = f->frag_off[fi], b = f->frag_off[fi + 1];
+        if (b - a < (uint64_t)k) continue;
+        u128 fwd = 0, rev = 0;
+        for (uint64_t i = a; i < b; i++) {
+            u128 bits = f->codes[i];
+            fwd = ((fwd << 2) | bits) & mask;
+            rev = (rev >> 2) | ((bits ^ 3) << hs);
+            if (i + 1 - a < (uint64_t)k) continue;
+            u128 c = fwd < rev ? fwd : rev;
+            uint64_t h = key_hash(c);
+            if (passes > 1 && key_pass(h, passes) != p) continue;
+            uint64_t sh = (h >> 32) % (uint64_t)n_shards;
+            if (index && table_contains(&index[sh], c)) continue; /* ZI: present in the index */
+            vec_push(&shards[sh], c);
+        }
+    }
+}
+
+static void insert_pass(const frags_t *f, int k, int p, int passes, int threads, int n_shards,
+                        table_t *tables, int presence, uint32_t d, const table_t *index) {
+    vec_t *all = (vec_t *)calloc((size_t)threads * n_shards, sizeof(vec_t));
+#pragma omp parallel num_threads(threads)
+    {
+        int t = 0, nt = 1;
+#ifdef _OPENMP
+        t = omp_get_thread_num(); nt = omp_get_num_threads();
+#endif
+        uint64_t lo = f->n_frag * (uint64_t)t / nt, hi = f->n_frag * (uint64_t)(t + 1) / nt;
+        gen_pass_range(f, lo, hi, k, p, passes, all + (size_t)t * n_shards, n_shards, index);
+    }
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1)
+    for (int s = 0; s < n_shards; s++) {
+        for (int t = 0; t < threads; t++) {
+            vec_t *v = &all[(size_t)t * n_shards + s];
+            for (uint64_t i = 0; i < v->n; i++) {
+                if (presence) table_add_presence(&tables[s], v->v[i], d);
+                else table_add(&tables[s], v->v[i]);
+            }
+            free(v->v); v->v = NULL;
+        }
+    }
+    free(all);
+}
+
+/* Digest (out[0] records, out[1] sum of counts, out[2] wrapping sum and
+ * out[3] xor of rec_digest) of the records with count > x that
+ * oracle_count would return for the same arguments, computed in `passes`
+ * passes over disjoint ranges of the k-mer hash so that memory stays bounded
+ * (each pass re-enumerates every k-mer and keeps only its own range).
+ * Returns 0, or -1 for an invalid configuration. */
+int oracle_count_digest(const uint8_t *const *bufs, const uint64_t *lens, int n_inputs, int k, uint64_t x,
+                        int mode, int threads, int passes, uint64_t *out, uint64_t *skipped) {
+    out[0] = out[1] = out[2] = out[3] = 0;
+    *skipped = 0;
+    if (k < 1 || k > 64 || n_inputs < 1 || passes < 1) return -1;
+    if (threads < 1) threads = 1;
+    const int n_shards = threads * 4;
+    frags_t all = {0};
+    if (mode == 0) {
+        for (int i = 0; i < n_inputs; i++)
+            if (parse_fastx(bufs[i], lens[i], (uint64_t)k, &all)) (*skipped)++;
+    } else {
+        for (int i = 0; i < n_inputs; i++) {
+            frags_t g = {0};
+            if (parse_fastx(bufs[i], lens[i], (uint64_t)k, &g)) (*skipped)++;
+            frags_free(&g);
+        }
+        if (x >= (uint64_t)n_inputs) return 0; /* src/lib.rs:644-648 */
+    }
+    uint64_t *part = (uint64_t *)calloc((size_t)n_shards * 4, sizeof(uint64_t));
+    for (int p = 0; p < passes; p++) {
+        table_t *tables = (table_t *)calloc(n_shards, sizeof(table_t));
+        for (int s = 0; s < n_shards; s++) table_init(&tables[s], 1024);
+        if (mode == 0) {
+            insert_pass(&all, k, p, passes, threads, n_shards, tables, 0, 0, NULL);
+        } else {
+            for (int d = 0; d < n_inputs; d++) {
+                frags_t g = {0};
+                parse_fastx(bufs[d], lens[d], (uint64_t)k, &g);
+                insert_pass(&g, k, p, passes, threads, n_shards, tables, 1, (uint32_t)d, NULL);
+                frags_free(&g);
+            }
+        }
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1)
+        for (int s = 0; s < n_shards; s++) {
+            uint64_t *q = part + (size_t)s * 4;
+            for (uint64_t i = 0; i < tables[s].cap; i++) {
+                if (tables[s].keys[i] == EMPTY_KEY || tables[s].counts[i] <= x) continue;
+                uint64_t w = rec_digest(tables[s].keys[i], tables[s].counts[i]);
+                q[0]++; q[1] += tables[s].counts[i]; q[2] += w; q[3] ^= w;
+            }
+            table_free(&tables[s]);
+        }
+        free(tables);
+    }
+    for (int s = 0; s < n_shards; s++) {
+        out[0] += part[s * 4]; out[1] += part[s * 4 + 1]; out[2] += part[s * 4 + 2]; out[3] ^= part[s * 4 + 3];
+    }
+    free(part);
+    frags_free(&all);
+    return 0;
+}
+
+/* Digest of the ZI absent set that oracle_zi_absent would return (each
+ * record with count 1), in `passes` hash-range passes over the queries; the
+ * index set is built once, sharded like the passes' tables.  Returns 0, or -1
+ * for an invalid k. */
+int oracle_zi_absent_digest(const uint8_t *index_buf, uint64_t index_len, const uint8_t *const *qbufs,
+                            const uint64_t *qlens, int n_queries, int k, int threads, int passes, uint64_t *out) {
+    out[0] = out[1] = out[2] = out[3] = 0;
+    if (k < 1 || k > 64 || passes < 1) return -1;
+    if (threads < 1) threads = 1;
+    const int n_shards = threads * 4;
+    table_t *index = (table_t *)calloc(n_shards, sizeof(table_t));
+    for (int s = 0; s < n_shards; s++) table_init(&index[s], 1024);
+    frags_t fi = {0};
+    parse_fastx(index_buf, index_len, 1, &fi); /* sequences of any length; only those >= k give k-mers */
+    insert_pass(&fi, k, 0, 1, threads, n_shards, index, 0, 0, NULL);
+    frags_free(&fi);
+    frags_t q = {0};
+    for (int i = 0; i < n_queries; i++) parse_fastx(qbufs[i], qlens[i], (uint64_t)k, &q);
+    uint64_t *part = (uint64_t *)calloc((size_t)n_shards * 4, sizeof(uint64_t));
+    for (int p = 0; p < passes; p++) {
+        table_t *tables = (table_t *)calloc(n_shards, sizeof(table_t));
+        for (int s = 0; s < n_shards; s++) table_init(&tables[s], 1024);
+        insert_pass(&q, k, p, passes, threads, n_shards, tables, 0, 0, index);
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1)
+        for (int s = 0; s < n_shards; s++) {
+            uint64_t *o = part + (size_t)s * 4;
+            for (uint64_t i = 0; i < tables[s].cap; i++) {
+                if (tables[s].keys[i] == EMPTY_KEY) continue;
+                uint64_t w = rec_digest(tables[s].keys[i], 1);
+                o[0]++; o[1] += 1; o[2] += w; o[3] ^= w;
+            }
+            table_free(&tables[s]);
+        }
+        free(tables);
+    }
+    for (int s = 0; s < n_shards; s++) {
+        out[0] += part[s * 4]; out[1] += part[s * 4 + 1]; out[2] += part[s * 4 + 2]; out[3] ^= part[s * 4 + 3];
+        table_free(&index[s]);
+    }
+    free(part);
+    free(index);
+    frags_free(&q);
+    return 0;
+}
+
+/* Digest of given records with the same definition (for checking a result
+ * copied from elsewhere against oracle_count_digest). */
+void oracle_records_digest(const uint64_t *key_lo, const uint64_t *key_hi, const uint64_t *counts, uint64_t n,
+                           uint64_t *out) {
+    out[0] = out[1] = out[2] = out[3] = 0;
+    for (uint64_t i = 0; i < n; i++) {
+        u128 key = ((u128)(key_hi ? key_hi[i] : 0) << 64) | key_lo[i];
+        uint64_t w = rec_digest(key, counts[i]);
+        out[0]++; out[1] += counts[i]; out[2] += w; out[3] ^= w;
+    }
+}
+
+/* ------------------------------------------------------------------ */
 /* exported API (ctypes)                                                */
 /* ------------------------------------------------------------------ */
 

@@ -46,6 +46,14 @@ def load():
                                      C.c_uint64, C.c_int]
     lib.oracle_write_simplitigs.restype = C.c_int64
     lib.oracle_write_simplitigs.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_uint64]
+    lib.oracle_count_digest.restype = C.c_int
+    lib.oracle_count_digest.argtypes = [C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_int, C.c_int, C.c_uint64,
+                                        C.c_int, C.c_int, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    lib.oracle_zi_absent_digest.restype = C.c_int
+    lib.oracle_zi_absent_digest.argtypes = [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
+                                            C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_uint64)]
+    lib.oracle_records_digest.restype = None
+    lib.oracle_records_digest.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]
     _lib = lib
     return lib
 
@@ -169,3 +177,45 @@ def parse_kff(data: bytes):
         recs[key] = c
     trailer = data[p:] == b"KFF"
     return {"free_block": free_block, "values": vals, "n": n, "head": data[:hdr_end]}, recs, trailer
+
+
+def _digest_dict(out) -> dict:
+    return {"records": int(out[0]), "count_sum": int(out[1]), "sum": "%016x" % out[2], "xor": "%016x" % out[3]}
+
+
+def count_digest(bufs, k: int, x: int, mode: int = 0, threads: int | None = None, passes: int = 1) -> dict:
+    """Digest (mczi_gb300.digest's definition) of what count() would return,
+    computed in `passes` hash-range passes so that memory stays bounded."""
+    from mczi_gb300._native import default_threads
+    arrs, ptrs, lens = _arrays(bufs)
+    out = (C.c_uint64 * 4)()
+    skipped = C.c_uint64()
+    rc = load().oracle_count_digest(ptrs, lens, len(arrs), k, x, mode, threads or default_threads(), passes, out,
+                                    C.byref(skipped))
+    if rc != 0:
+        raise ValueError("oracle rejected the configuration")
+    return _digest_dict(out)
+
+
+def records_digest(lo, hi, cnt) -> dict:
+    lo = np.ascontiguousarray(lo, dtype=np.uint64)
+    cnt = np.ascontiguousarray(cnt, dtype=np.uint64)
+    hi = None if hi is None else np.ascontiguousarray(hi, dtype=np.uint64)
+    out = (C.c_uint64 * 4)()
+    load().oracle_records_digest(lo.ctypes.data, hi.ctypes.data if hi is not None else None, cnt.ctypes.data, lo.size,
+                                 out)
+    return _digest_dict(out)
+
+
+def zi_absent_digest(index, queries, k: int, threads: int | None = None, passes: int = 1) -> dict:
+    """Digest of zi_absent()'s set (every record with count 1), in `passes`
+    hash-range passes over the queries."""
+    from mczi_gb300._native import default_threads
+    ia = np.frombuffer(index, dtype=np.uint8) if not isinstance(index, np.ndarray) else index
+    arrs, ptrs, lens = _arrays(queries)
+    out = (C.c_uint64 * 4)()
+    rc = load().oracle_zi_absent_digest(ia.ctypes.data if ia.size else None, ia.size, ptrs, lens, len(arrs), k,
+                                        threads or default_threads(), passes, out)
+    if rc != 0:
+        raise ValueError("oracle rejected k")
+    return _digest_dict(out)

@@ -1,0 +1,108 @@
+"""Compressed inputs of the path-based entry points, on the CPU.
+
+MC and ZI read gzip, xz and zstd inputs (src/lib.rs:3127-3143, 3218-3226).
+The library recognises the format by magic bytes and decodes it with the
+system's zlib / liblzma / libzstd loaded at run time (csrc/decompress.cpp);
+mczi_read_input_file is the host-only entry point these tests call (no
+device needed).  Covered: plain, multi-member gzip, concatenated xz streams,
+multi-frame zstd, a compressed file with a misleading name, an empty file,
+and truncated or corrupt streams, which must fail with MCZI_ERR_IO and a
+message, not return partial data.
+"""
+import ctypes as C
+import ctypes.util
+import gzip
+import lzma
+
+import numpy as np
+import pytest
+
+
+def payload(seed=0, n=300_000):
+    rng = np.random.default_rng(seed)
+    seq = rng.choice(np.frombuffer(b"ACGTN", dtype=np.uint8), size=n).tobytes()
+    return b"".join(b">r%d\n%s\n" % (i, seq[i * 150:(i + 1) * 150]) for i in range(n // 150))
+
+
+def read(path):
+    from mczi_gb300 import mc
+    return mc.read_input(path)
+
+
+def zstd_compress(data: bytes, level=3):
+    name = ctypes.util.find_library("zstd")
+    if not name:
+        pytest.skip("libzstd not on this host")
+    z = C.CDLL(name)
+    z.ZSTD_compressBound.restype = C.c_size_t
+    z.ZSTD_compressBound.argtypes = [C.c_size_t]
+    z.ZSTD_compress.restype = C.c_size_t
+    z.ZSTD_compress.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_int]
+    cap = z.ZSTD_compressBound(len(data))
+    out = C.create_string_buffer(cap)
+    n = z.ZSTD_compress(out, cap, data, len(data), level)
+    return out.raw[:n]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def lib():
+    from mczi_gb300 import build
+    build.build_gpu_lib()
+
+
+def test_plain_and_empty(tmp_path):
+    d = payload(1)
+    (tmp_path / "a.fa").write_bytes(d)
+    (tmp_path / "e.fa").write_bytes(b"")
+    assert read(tmp_path / "a.fa") == d
+    assert read(tmp_path / "e.fa") == b""
+
+
+def test_gzip_multi_member(tmp_path):
+    a, b = payload(2), payload(3)
+    (tmp_path / "x.fa.gz").write_bytes(gzip.compress(a) + gzip.compress(b, compresslevel=1))
+    assert read(tmp_path / "x.fa.gz") == a + b
+
+
+def test_xz_concatenated(tmp_path):
+    a, b = payload(4), payload(5)
+    (tmp_path / "x.fa.xz").write_bytes(lzma.compress(a) + lzma.compress(b))
+    assert read(tmp_path / "x.fa.xz") == a + b
+
+
+def test_zstd_frames(tmp_path):
+    a, b = payload(6), payload(7)
+    (tmp_path / "x.fa.zst").write_bytes(zstd_compress(a) + zstd_compress(b, 9))
+    assert read(tmp_path / "x.fa.zst") == a + b
+
+
+def test_format_by_magic_not_name(tmp_path):
+    d = payload(8)
+    (tmp_path / "looks_plain.fa").write_bytes(gzip.compress(d))
+    assert read(tmp_path / "looks_plain.fa") == d
+    (tmp_path / "looks_gz.gz").write_bytes(d)  # plain text under a .gz name
+    assert read(tmp_path / "looks_gz.gz") == d
+
+
+@pytest.mark.parametrize("kind", ["gz", "xz", "zst"])
+def test_truncated_and_corrupt_fail(tmp_path, kind):
+    from mczi_gb300 import MCZIError, _native as N
+    d = payload(9)
+    comp = {"gz": gzip.compress, "xz": lzma.compress, "zst": zstd_compress}[kind](d)
+    (tmp_path / f"t.{kind}").write_bytes(comp[: len(comp) // 2])
+    with pytest.raises(MCZIError) as e:
+        read(tmp_path / f"t.{kind}")
+    assert e.value.code == N.MCZI_ERR_IO and str(e.value)
+    bad = bytearray(comp)
+    for i in range(len(bad) // 3, len(bad) // 3 + 64):
+        bad[i] ^= 0x5A
+    (tmp_path / f"c.{kind}").write_bytes(bytes(bad))
+    with pytest.raises(MCZIError) as e:
+        read(tmp_path / f"c.{kind}")
+    assert e.value.code == N.MCZI_ERR_IO
+
+
+def test_missing_file(tmp_path):
+    from mczi_gb300 import MCZIError
+    with pytest.raises(MCZIError, match="failed to open"):
+        read(tmp_path / "nope.fa")

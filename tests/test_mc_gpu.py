@@ -135,6 +135,32 @@ def test_packer_parity(gpu_ctx, oracle):
     assert np.array_equal(starts, np.concatenate(exp_starts))
 
 
+def test_bucket_window_guard(gpu_ctx, oracle):
+    """The counting kernel's 32-bit counters are bounded by one minimizer
+    bucket's k-mer windows; a bucket above the limit fails the count with
+    MCZI_ERR_TOO_LARGE instead of wrapping.  The test hook lowers the limit
+    (default 2^32 - 1) so the path runs on a small input."""
+    from mczi_gb300 import MCZIError, _native as N, gen
+    from mczi_gb300.mc import CounterConfig
+    lib = N.load()
+    data = gen.c1_reads(scale=0.002)
+    homopolymer = b">a\n" + b"A" * 5000 + b"\n"  # every window in one bucket
+    try:
+        for limit, inputs in ((10, [data]), (4000, [homopolymer])):
+            assert lib.mczi_debug_set_bucket_window_limit(gpu_ctx.handle, limit) == 0
+            for k in (31, 63):
+                with pytest.raises(MCZIError) as e:
+                    gpu_ctx.count(inputs, CounterConfig(k, 21, 1))
+                assert e.value.code == N.MCZI_ERR_TOO_LARGE and "32-bit" in str(e.value)
+        assert lib.mczi_debug_set_bucket_window_limit(gpu_ctx.handle, 1 << 33) == N.MCZI_ERR_INVALID_CONFIG
+        # 4972 windows fit a limit of 5000
+        assert lib.mczi_debug_set_bucket_window_limit(gpu_ctx.handle, 5000) == 0
+        assert gpu_dict(gpu_ctx, [homopolymer], 29, 21, 1) == oracle_dict(oracle, [homopolymer], 29, 1)
+    finally:
+        lib.mczi_debug_set_bucket_window_limit(gpu_ctx.handle, 0)
+    assert gpu_dict(gpu_ctx, [data], 31, 21, 1) == oracle_dict(oracle, [data], 31, 1)
+
+
 def test_tuning_invariance(gpu_ctx, oracle):
     from mczi_gb300 import gen
     data = gen.c1_reads(scale=0.004)
