@@ -138,14 +138,14 @@ struct GraphSig {
   uint32_t passes = 0, slots = 0, fwords = 0;
   int threads = 0, cps = 0, chunk = 0, filter = 0;
   float fill = 0.f;
-  const void* ptrs[12] = {};
+  const void* ptrs[13] = {};
   bool operator==(const GraphSig& o) const {
     if (text_len != o.text_len || n_tiles != o.n_tiles || x != o.x || desc_cap != o.desc_cap || out_cap != o.out_cap ||
         n_inputs != o.n_inputs || k != o.k || m != o.m || mode != o.mode || passes != o.passes || slots != o.slots ||
         fwords != o.fwords || threads != o.threads || cps != o.cps || chunk != o.chunk || filter != o.filter ||
         fill != o.fill)
       return false;
-    for (int i = 0; i < 12; i++)
+    for (int i = 0; i < 13; i++)
       if (ptrs[i] != o.ptrs[i]) return false;
     return true;
   }
@@ -169,6 +169,7 @@ struct mczi_ctx {
   mczi::DevBuf out_lo, out_hi, out_cnt, out_mask;
   mczi::DevBuf cnt64;  // counts widened to u64 for direct copies to the caller
   mczi::DevBuf digest_acc;  // mczi_result_digest accumulators (3 u64)
+  mczi::DevBuf count_scratch;  // per-CTA window words of fast filtered counting rounds
   mczi::DevBuf kff_dev;          // KFF records formatted on the device
   mczi::HostPinned kff_host;     // their host copy, written to the file as is
   mczi::DevBuf sx_keys, sx_tab, sx_rank, sx_ext;  // simplitig writer: sorted keys, key->rank table, extensions

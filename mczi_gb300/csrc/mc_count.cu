@@ -91,6 +91,172 @@ __device__ __forceinline__ uint32_t popc_words(const unsigned long long* m, int 
   return c;
 }
 
+// Filtered rounds use two blocked Bloom filters in shared memory, each a key
+// sets two bits of one 32-bit word: the seen map (pass 1: a window whose two
+// bits were both set already is a repeat, or a collision) and the claimed map
+// (set for every key stored in the table; pass 2 looks up only windows whose
+// claimed bits are both set).  Two bits per key cut the collision rate to
+// about a third of one bit's at the densities the rounds run at.
+//   seen map   : word from hash bits 20..51, bits from 52..56 and 57..61
+//   claimed map: from hb31 = hash bits 20..50 (the value kept per window)
+__device__ __forceinline__ bool seen_test_set(uint32_t* bmap, uint32_t bwords, uint64_t hv) {
+  const uint32_t wi = (uint32_t)((((hv >> 20) & 0xffffffffull) * (uint64_t)bwords) >> 32);
+  const uint32_t m = (1u << ((uint32_t)(hv >> 52) & 31u)) | (1u << ((uint32_t)(hv >> 57) & 31u));
+  return (atomicOr(&bmap[wi], m) & m) == m;
+}
+__device__ __forceinline__ uint32_t hb31_of(uint64_t hv) { return (uint32_t)(hv >> 20) & 0x7fffffffu; }
+__device__ __forceinline__ void claimed_set(uint32_t* cmap, uint32_t cwords, uint32_t hb31) {
+  const uint32_t wi = (uint32_t)(((uint64_t)hb31 * (uint64_t)cwords) >> 31);
+  atomicOr(&cmap[wi], (1u << (hb31 & 31u)) | (1u << ((hb31 >> 5) & 31u)));
+}
+__device__ __forceinline__ bool claimed_test(const uint32_t* cmap, uint32_t cwords, uint32_t hb31) {
+  const uint32_t wi = (uint32_t)(((uint64_t)hb31 * (uint64_t)cwords) >> 31);
+  const uint32_t m = (1u << (hb31 & 31u)) | (1u << ((hb31 >> 5) & 31u));
+  return (cmap[wi] & m) == m;
+}
+
+// per-window word of the fast filtered rounds' scratch: hb31 of a window seen
+// for the first time in pass 1, or WIN_DONE (counted in pass 1, outside the
+// round's hash range, or past the end of its chunk)
+constexpr uint32_t WIN_DONE = 0xffffffffu;
+constexpr uint32_t WIN_REPEAT = 0xfffffffeu;  // a repeat of pass 1 (hb31 < 2^31 marks a first sight)
+
+// the k-mer starting at base `pos` of the packed stream
+template <class K, class R>
+__device__ __forceinline__ void roll_at(R& roll, const uint32_t* __restrict__ packed, uint64_t pos, int k) {
+  roll.init(k);
+  if constexpr (sizeof(K) == 8) {
+    roll.set(field64(packed, pos, k), k);
+  } else {
+    if (k > 32) roll.set(field64(packed, pos, k - 32), field64(packed, pos + (uint64_t)(k - 32), 32), k);
+    else roll.set(0ull, field64(packed, pos, k), k);
+  }
+}
+
+// Passes 2a (sub 0) and 2b (sub 1) of a fast filtered round over its nchunks
+// chunk records.  2a stores or counts every repeat (claim-or-count; the
+// claiming occurrence is implicit); 2b, once every key is stored, counts each
+// first sight whose claimed bits are set and whose key is in the table.  A
+// warp reads 32 consecutive records at a time and gathers the windows to look
+// up into a register queue (two entries per lane); whenever 32 are queued all
+// lanes look one up, so the rare lookups run with full warps instead of one
+// or two lanes each.  Only the queued windows' k-mers are re-extracted from
+// the packed stream.
+template <class K, class R, int MODE>
+__device__ __forceinline__ void lookup_window(int sub, uint64_t e, const uint32_t* __restrict__ packed, int k,
+                                              K* keys, uint32_t* cnt, unsigned long long* msk, int W, uint32_t S,
+                                              K EMPTY, uint32_t* s_over, uint32_t* claimed) {
+  const uint64_t pos = e & ((1ull << 48) - 1);
+  const uint32_t dset = (uint32_t)(e >> 48);
+  R roll;
+  roll_at<K, R>(roll, packed, pos, k);
+  const uint64_t hv = sym_hash(roll);
+  const K key = roll.canon();
+  uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
+  if (sub == 1) {
+    // 2b: keys are final: plain loads, stop at EMPTY
+    for (uint32_t probe = 0; probe < PROBE_LIMIT; probe++) {
+      const K cur = keys[s];
+      if (key_eq(cur, key)) {
+        if (MODE == 0) atomicAdd(&cnt[s], 1u);
+        else atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
+        return;
+      }
+      if (key_eq(cur, EMPTY)) return;
+      s = (s + 1 == S) ? 0u : s + 1;
+    }
+    return;
+  }
+  // 2a: claim-or-count, as the single pass (see k_count)
+  for (uint32_t probe = 0; probe < PROBE_LIMIT; probe++) {
+    K cur = keys[s];
+    if (KeyOps<K>::maybe_partial(cur)) {
+      const K prev = KeyOps<K>::cas(&keys[s], EMPTY, key);
+      if (key_eq(prev, EMPTY)) {
+        (*claimed)++;
+        if (MODE == 1) atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
+        return;
+      }
+      cur = prev;
+    }
+    if (key_eq(cur, key)) {
+      if (MODE == 0) atomicAdd(&cnt[s], 1u);
+      else atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
+      return;
+    }
+    s = (s + 1 == S) ? 0u : s + 1;
+  }
+  *s_over = 1;  // table far past its target fill: the round is split
+}
+
+template <class K, class R, int MODE>
+__device__ __forceinline__ void fast_pass2(int sub, const uint32_t* scr, const uint64_t* scr_pos, uint32_t nchunks,
+                                           const uint32_t* __restrict__ packed, int k, K* keys, uint32_t* cnt,
+                                           unsigned long long* msk, int W, uint32_t S, const uint32_t* cmap,
+                                           uint32_t cwords, K EMPTY, uint32_t* s_over, uint32_t* claimed) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  uint64_t q0 = 0, q1 = 0;  // queue entries lane and 32 + lane
+  uint32_t qn = 0;          // queued entries (warp-uniform)
+  for (uint32_t g = (uint32_t)wid * 32u; g < nchunks; g += (uint32_t)nw * 32u) {
+    if (*(volatile uint32_t*)s_over) break;  // uniform across the warp: read once below
+    const uint32_t c = g + (uint32_t)lane;
+    uint32_t m = 0;
+    uint64_t base = 0;
+    if (c < nchunks) {
+      const uint4 v = reinterpret_cast<const uint4*>(scr)[c];
+      const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const bool want = sub == 0 ? w[j] == WIN_REPEAT
+                                   : (w[j] < 0x80000000u && claimed_test(cmap, cwords, w[j]));
+        m |= want ? (1u << j) : 0u;
+      }
+      if (m) base = scr_pos[c];
+    }
+    // gather this group's windows into the queue, 32 at a time
+    const uint32_t n = __popc(m);
+    uint32_t incl = n;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    const uint32_t excl = incl - n;
+    for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+      const uint32_t t = b0 + (uint32_t)lane;
+      // source lane of candidate t: the first lane whose inclusive count exceeds t
+      int src = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const uint32_t v = __shfl_sync(0xffffffffu, incl, src + step - 1);
+        if (v <= t) src += step;
+      }
+      const uint32_t ms = __shfl_sync(0xffffffffu, m, src & 31);
+      const uint32_t es = __shfl_sync(0xffffffffu, excl, src & 31);
+      const uint64_t bs = __shfl_sync(0xffffffffu, base, src & 31);
+      const uint32_t gsz = min(32u, total - b0);
+      uint64_t e = 0;
+      if (t < total) e = bs + (uint64_t)(__fns(ms, 0, (int)(t - es) + 1));
+      // entry i of this gather goes to queue position qn + i
+      const uint64_t er = __shfl_sync(0xffffffffu, e, (lane - (int)qn) & 31);
+      const uint32_t i = (uint32_t)((lane - (int)qn) & 31);
+      if (i < gsz) {
+        if ((uint32_t)lane >= qn) q0 = er;
+        else q1 = er;
+      }
+      if (qn + gsz >= 32) {
+        lookup_window<K, R, MODE>(sub, q0, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
+        q0 = q1;
+        qn = qn + gsz - 32;
+      } else {
+        qn += gsz;
+      }
+    }
+  }
+  if ((uint32_t)lane < qn)
+    lookup_window<K, R, MODE>(sub, q0, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
+}
+
 }  // namespace
 
 size_t count_slot_bytes(int k, int mode, int n_datasets) {
@@ -120,7 +286,7 @@ size_t count_smem_bytes(int k, int mode, int n_datasets, uint32_t table_slots, u
 // KC > 0 compiles the kernel for one k (the shifts and masks of the rolling
 // k-mer become constants); KC == 0 takes k from the arguments
 template <class K, class R, int MODE, int KC>
-__global__ void k_count(CountArgs a) {
+__global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
   extern __shared__ __align__(16) uint8_t smem[];
   const uint32_t S = a.table_slots;
   const int W = MODE == 0 ? 1 : (a.n_datasets + 63) / 64;
@@ -136,9 +302,17 @@ __global__ void k_count(CountArgs a) {
   // claimed-key bitmap (1/8) that lets pass 2 skip the table for keys pass 1
   // never stored (both indexed by the same 32 hash bits)
   const uint32_t cwords = filtered ? ((fwords / 8) & ~31u) : 0u;
-  const uint64_t fbits = (uint64_t)(fwords - cwords) * 32, cbits = (uint64_t)cwords * 32;
+  const uint32_t bwords = fwords - cwords;
+  const uint64_t fbits = (uint64_t)bwords * 32;
   uint32_t* bmap = reinterpret_cast<uint32_t*>(smem + off);
-  uint32_t* cmap = bmap + (fwords - cwords);
+  uint32_t* cmap = bmap + bwords;
+  // this CTA's per-window scratch of fast filtered rounds (L2-resident: a
+  // round writes and re-reads only its own windows' words)
+  // layout per CTA: scr_chunks uint4 window words, then scr_chunks u64 chunk
+  // positions (base of the chunk's first window | dataset << 48)
+  uint32_t* scr = (filtered && a.win_scratch) ? a.win_scratch + (size_t)blockIdx.x * a.scratch_words : nullptr;
+  const uint32_t scr_chunks = (uint32_t)((a.scratch_words / 6) & ~3ull);
+  uint64_t* scr_pos = scr ? reinterpret_cast<uint64_t*>(scr + (size_t)scr_chunks * 4) : nullptr;
   off += (size_t)fwords * 4;
   off = (off + 15) & ~(size_t)15;
   uint32_t* occ = reinterpret_cast<uint32_t*>(smem + off);   // NP2 + 1, becomes occupancy prefix
@@ -158,6 +332,7 @@ __global__ void k_count(CountArgs a) {
   __shared__ uint32_t sh_cpre[MAX_THREADS + 1];
   __shared__ uint32_t sh_cpre32[MAX_THREADS / 32];
   __shared__ uint32_t s_step;
+  __shared__ uint32_t s_cbase;  // chunks of the round's earlier batches
   __shared__ uint64_t sh_desc[MAX_THREADS];
   __shared__ uint16_t sh_dset[MODE == 1 ? MAX_THREADS : 1];
   const uint32_t chunk = a.chunk;
@@ -337,21 +512,46 @@ __global__ void k_count(CountArgs a) {
         // keep every lane busy.  A chunk extracts its first k-mer from the
         // packed stream and rolls through the rest.
         //   single pass (ph 0): claim-or-count every window;
-        //   filtered (ph 1, 2): pass 1 sets one bitmap bit per window and claims
-        //   a slot only when the bit was already set (a repeat -- or a bitmap
-        //   collision, harmless); pass 2 counts every occurrence of the claimed
-        //   keys with plain-load lookups.  A k-mer seen once is never stored,
-        //   and a k-mer seen twice or more always is, so for x >= 1 the
-        //   emitted set and counts are the same as the single pass.
+        //   filtered (ph 1, 2): pass 1 sets a window's two seen bits and
+        //   claims a slot only when both were already set (a repeat -- or a
+        //   collision, harmless).  A k-mer seen once is never stored, one seen
+        //   twice or more always is, so for x >= 1 the emitted set and counts
+        //   equal the single pass'.  Two ways to count the claimed keys:
+        //   - fast (the round's windows fit the CTA's scratch): pass 1 also
+        //     counts every repeat it looks up and writes one word per window
+        //     to the scratch -- hb31 for a first sight, WIN_DONE otherwise; pass
+        //     2 reads those words (no rolling) and looks up only first sights
+        //     whose claimed bits are set, re-extracting just their k-mers.
+        //     Every occurrence is counted once: repeats in pass 1 (the claiming
+        //     one implicitly), the first sight in pass 2.
+        //   - otherwise pass 1 only claims and pass 2 re-rolls every window and
+        //     counts every occurrence of the claimed keys.
         // a round of one batch keeps that batch's descriptors and chunk
         // prefixes in shared memory from pass 1 to pass 2
         const bool one_batch = dhi - dlo <= (uint64_t)nth;
+        // chunks of the round <= (windows + descriptors * (chunk - 1)) / chunk
+        const uint64_t round_windows = (uint64_t)(occ[rr.bh] - occ[rr.bl]);
+        const bool fast = scr != nullptr && chunk == 4 &&
+                          (round_windows + (uint64_t)(dhi - dlo) * 3) / 4 <= scr_chunks;
         uint32_t total = 0;
         for (int ph = filtered ? 1 : 0; ph <= (filtered ? 2 : 0); ph++) {
-          if (ph == 2) {
-            if (one_batch && tid == 0) s_step = 0;
+          if (ph == 2 && fast) {
+            // ---- passes 2a and 2b of a fast round, over its chunk records
             __syncthreads();
+            const uint32_t nchunks = s_cbase;
+            for (int sub = 0; sub < 2; sub++) {
+              fast_pass2<K, R, MODE>(sub, scr, scr_pos, nchunks, a.packed, k, keys, cnt, msk, W, S, cmap, cwords,
+                                     EMPTY, &s_over, &claimed);
+              __syncthreads();
+              if (s_over) break;
+            }
+            break;
           }
+          if (tid == 0) {
+            s_cbase = 0;
+            if (ph == 2 && one_batch) s_step = 0;
+          }
+          __syncthreads();
           for (uint64_t bb = dlo; bb < dhi; bb += (uint64_t)nth) {
             if (!(ph == 2 && one_batch)) {
               const bool has = bb + (uint64_t)tid < dhi;
@@ -377,6 +577,7 @@ __global__ void k_count(CountArgs a) {
               __syncthreads();
             }
             const int nd = (int)min((uint64_t)nth, dhi - bb);
+            const uint32_t cbase = s_cbase;
             // Warps take steps of 32 chunks (one per lane) from a shared
             // counter, so a batch ends with at most one step of imbalance.  The
             // descriptor of the step's first chunk comes from a two-level
@@ -409,39 +610,32 @@ __global__ void k_count(CountArgs a) {
               const uint32_t dset = MODE == 1 ? (uint32_t)sh_dset[lo2] : 0u;
               const uint64_t s0 = bd_start(d2) + w0;
               R roll;
-              roll.init(k);
-              if constexpr (sizeof(K) == 8) {
-                roll.set(field64(a.packed, s0, k), k);
-              } else {
-                if (k > 32) roll.set(field64(a.packed, s0, k - 32), field64(a.packed, s0 + (uint64_t)(k - 32), 32), k);
-                else roll.set(0ull, field64(a.packed, s0, k), k);
-              }
+              roll_at<K, R>(roll, a.packed, s0, k);
               // next base: the top two bits of `word` (pre-shifted), q = its
               // index inside the packed word at wp
               const uint64_t p = s0 + (uint64_t)k;
               const uint32_t* wp = a.packed + (p >> 4);
               uint32_t q = (uint32_t)(p & 15);
               uint32_t word = *wp << (2 * q);
+              // pass 1 of a fast round: the chunk's words, stored at its end
+              uint32_t r0 = WIN_DONE, r1 = WIN_DONE, r2 = WIN_DONE, r3 = WIN_DONE;
               for (uint32_t j = w0; j < w1; j++) {
                 if (j > w0) {
                   roll.push(word >> 30);
                   word <<= 2;
                   if (++q == 16) { q = 0; word = *++wp; }
                 }
-                // slot, bitmap position and range come from the strand-symmetric
+                // slot, filter bits and range come from the strand-symmetric
                 // hash; the canonical key is formed only where the table is touched
                 const uint64_t hv = sym_hash(roll);
                 if (!full_range) {
                   const uint32_t hk = (uint32_t)(hv >> 32);
-                  if (hk < rr.hlo || hk > rr.hhi) continue;
+                  if (hk < rr.hlo || hk > rr.hhi) continue;  // its word stays WIN_DONE
                 }
-                // bitmap positions from hash bits 20..51 (the slot uses the low
-                // 32 bits, range splits bits 32..63)
-                const uint64_t hb = (hv >> 20) & 0xffffffffull;
+                const uint32_t hb = hb31_of(hv);
                 if (ph == 2) {
-                  // a key pass 1 never stored has its claimed bit clear
-                  const uint32_t cp = (uint32_t)((hb * cbits) >> 32);
-                  if (!((cmap[cp >> 5] >> (cp & 31)) & 1u)) continue;
+                  // slow pass 2: a key pass 1 never stored has its claimed bits clear
+                  if (!claimed_test(cmap, cwords, hb)) continue;
                   const K key = roll.canon();
                   uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
                   // keys are final during pass 2: plain loads, stop at EMPTY
@@ -458,37 +652,47 @@ __global__ void k_count(CountArgs a) {
                   continue;
                 }
                 if (ph == 1) {
-                  const uint32_t bp = (uint32_t)((hb * fbits) >> 32);
-                  const uint32_t bit = 1u << (bp & 31);
-                  if (!(atomicOr(&bmap[bp >> 5], bit) & bit)) continue;  // first sight: not stored
-                  const uint32_t cp = (uint32_t)((hb * cbits) >> 32);
-                  atomicOr(&cmap[cp >> 5], 1u << (cp & 31));  // stored (below) or already stored
+                  const bool repeat = seen_test_set(bmap, bwords, hv);
+                  if (repeat) claimed_set(cmap, cwords, hb);  // stored below, or in pass 2a
+                  if (fast) {
+                    // a fast round only records the window: hb31 for a first
+                    // sight, WIN_REPEAT for a repeat (stored by pass 2a)
+                    const uint32_t v = repeat ? WIN_REPEAT : hb;
+                    const uint32_t jj = j - w0;
+                    r0 = jj == 0 ? v : r0;
+                    r1 = jj == 1 ? v : r1;
+                    r2 = jj == 2 ? v : r2;
+                    r3 = jj == 3 ? v : r3;
+                    continue;
+                  }
+                  if (!repeat) continue;  // first sight: not stored
                 }
+                const bool count_here = ph == 0;
                 const K key = roll.canon();
                 uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
                 bool done = false;
                 // Probe with plain loads; CAS only on a slot that looks empty.
                 // A slot goes from EMPTY to a key exactly once, so a load that
                 // shows a complete key (no all-ones half) is final; anything
-                // else is resolved by the CAS's atomic snapshot.  In the single
-                // pass the claiming thread's own occurrence is implicit: a
-                // slot's stored count is (occurrences - 1).  A probe run longer
-                // than PROBE_LIMIT means the table is far past its target
-                // fill: the round is split.
+                // else is resolved by the CAS's atomic snapshot.  The claiming
+                // thread's own occurrence is implicit: a slot's stored count is
+                // (occurrences counted here - 1).  A probe run longer than
+                // PROBE_LIMIT means the table is far past its target fill: the
+                // round is split.
                 for (uint32_t probe = 0; probe < PROBE_LIMIT; probe++) {
                   K cur = keys[s];
                   if (KeyOps<K>::maybe_partial(cur)) {
                     const K prev = KeyOps<K>::cas(&keys[s], EMPTY, key);
                     if (key_eq(prev, EMPTY)) {
                       claimed++;
-                      if (MODE == 1 && ph == 0) atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
+                      if (MODE == 1 && count_here) atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
                       done = true;
                       break;
                     }
                     cur = prev;
                   }
                   if (key_eq(cur, key)) {
-                    if (ph == 0) {
+                    if (count_here) {
                       if (MODE == 0) atomicAdd(&cnt[s], 1u);
                       else atomicOr(&msk[(size_t)s * W + (dset >> 6)], 1ull << (dset & 63));
                     }
@@ -499,8 +703,14 @@ __global__ void k_count(CountArgs a) {
                 }
                 if (!done) { s_over = 1; break; }
               }
+              if (ph == 1 && fast) {
+                const uint32_t ci = cbase + c;
+                reinterpret_cast<uint4*>(scr)[ci] = make_uint4(r0, r1, r2, r3);
+                scr_pos[ci] = s0 | ((uint64_t)dset << 48);
+              }
             }
             __syncthreads();
+            if (tid == 0) s_cbase = cbase + total;
             if (s_over) break;
           }
           if (s_over) break;
@@ -543,7 +753,9 @@ __global__ void k_count(CountArgs a) {
           if (s < S) {
             key = keys[s];
             if (!key_eq(key, EMPTY)) {
-              c = MODE == 0 ? cnt[s] + (filtered ? 0u : 1u) : popc_words(&msk[(size_t)s * W], W);
+              // the claiming occurrence is implicit except in slow filtered
+              // rounds, whose pass 2 counts every occurrence
+              c = MODE == 0 ? cnt[s] + ((filtered && !fast) ? 0u : 1u) : popc_words(&msk[(size_t)s * W], W);
               emit = (uint64_t)c > a.threshold;
             }
           }

@@ -224,7 +224,8 @@ int32_t pipe_pack(mczi_ctx* ctx, Pipe& p) {
 
 // Superkmers one pass may hold: the partition addresses them with 32-bit
 // positions.
-constexpr uint64_t PASS_MAX_DESC = 4000000000ull;
+constexpr uint64_t PASS_MAX_DESC = 4000000000ull;  // < 2^32: the partition's 32-bit bucket counters hold a pass
+constexpr uint64_t COUNT_SCRATCH_WORDS = 1ull << 18;  // per counting CTA (1 MiB; a multiple of 4)
 
 uint32_t key_range_passes(mczi_ctx* ctx, int k, int m, uint64_t bases) {
   if (ctx->key_passes > 0) return (uint32_t)ctx->key_passes;
@@ -468,6 +469,15 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       ca.chunk = ctx->count_chunk > 0 ? (uint32_t)ctx->count_chunk : (wide ? 4u : 2u);
       ca.filter_words = fwords;
       ca.max_bucket_windows = ctx->max_bucket_windows ? ctx->max_bucket_windows : 0xffffffffull;
+      // filtered rounds whose windows fit COUNT_SCRATCH_WORDS per CTA take the
+      // fast path (pass 2 reads one word per window instead of re-rolling)
+      ca.win_scratch = nullptr;
+      ca.scratch_words = 0;
+      if (fwords > 0) {
+        CKA(ctx->count_scratch, (size_t)ca.ctas * COUNT_SCRATCH_WORDS * 4);
+        ca.win_scratch = ctx->count_scratch.as<uint32_t>();
+        ca.scratch_words = COUNT_SCRATCH_WORDS;
+      }
       launch_count(ca, s);
       p.launches += 1;
       CK(cudaGetLastError());
@@ -757,10 +767,10 @@ GraphSig make_sig(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint3
   g.chunk = ctx->count_chunk;
   g.filter = ctx->count_filter;
   g.fill = ctx->count_fill;
-  const void* ptrs[12] = {ctx->text.p, ctx->packed.p, ctx->fbits.p, ctx->desc.p, ctx->key.p, ctx->desc2.p,
+  const void* ptrs[13] = {ctx->text.p, ctx->packed.p, ctx->fbits.p, ctx->desc.p, ctx->key.p, ctx->desc2.p,
                           ctx->key2.p, ctx->out_lo.p, ctx->out_hi.p, ctx->out_cnt.p, ctx->scalars.p,
-                          ctx->part_hist.p};
-  for (int i = 0; i < 12; i++) g.ptrs[i] = ptrs[i];
+                          ctx->part_hist.p, ctx->count_scratch.p};
+  for (int i = 0; i < 13; i++) g.ptrs[i] = ptrs[i];
   return g;
 }
 

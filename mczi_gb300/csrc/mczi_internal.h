@@ -152,6 +152,10 @@ struct CountArgs {
   // the per-slot counts are 32-bit and each is bounded by the bucket's
   // windows; a bucket above this sets ST_COUNT_WIDTH and is not counted
   uint64_t max_bucket_windows;
+  // fast filtered rounds: one word per window of a round, scratch_words per
+  // CTA (a multiple of 4); nullptr keeps every filtered round on the slow path
+  uint32_t* win_scratch;
+  uint64_t scratch_words;
 };
 void launch_count(const CountArgs& a, cudaStream_t s);
 size_t count_smem_bytes(int k, int mode, int n_datasets, uint32_t table_slots, uint32_t filter_words);
