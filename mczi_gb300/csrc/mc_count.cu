@@ -133,15 +133,17 @@ __device__ __forceinline__ void roll_at(R& roll, const uint32_t* __restrict__ pa
   }
 }
 
-// Passes 2a (sub 0) and 2b (sub 1) of a fast filtered round over its nchunks
-// chunk records.  2a stores or counts every repeat (claim-or-count; the
-// claiming occurrence is implicit); 2b, once every key is stored, counts each
-// first sight whose claimed bits are set and whose key is in the table.  A
-// warp reads 32 consecutive records at a time and gathers the windows to look
-// up into a register queue (two entries per lane); whenever 32 are queued all
-// lanes look one up, so the rare lookups run with full warps instead of one
-// or two lanes each.  Only the queued windows' k-mers are re-extracted from
-// the packed stream.
+// Passes 2 and 3 of a fast filtered round, over the nchunks chunk records
+// pass 1 left.  Pass 2 stores or counts every repeat (claim-or-count; the
+// claiming occurrence is implicit) and lists the first sights whose claimed
+// bits are set; pass 3, once every key is stored, counts each listed first
+// sight whose key is in the table.  A warp reads 32 consecutive records at a
+// time (the next 32 already in flight) and gathers the repeats into a
+// register queue (two entries per lane); whenever 32 are queued all lanes
+// look one up, so the rare lookups run with full warps instead of one or two
+// lanes each.  Only the looked-up windows' k-mers are re-extracted from the
+// packed stream.  Each warp keeps its own list, so no shared counter is
+// touched.
 template <class K, class R, int MODE>
 __device__ __forceinline__ void lookup_window(int sub, uint64_t e, const uint32_t* __restrict__ packed, int k,
                                               K* keys, uint32_t* cnt, unsigned long long* msk, int W, uint32_t S,
@@ -190,30 +192,51 @@ __device__ __forceinline__ void lookup_window(int sub, uint64_t e, const uint32_
 }
 
 template <class K, class R, int MODE>
-__device__ __forceinline__ void fast_pass2(int sub, const uint32_t* scr, const uint64_t* scr_pos, uint32_t nchunks,
-                                           const uint32_t* __restrict__ packed, int k, K* keys, uint32_t* cnt,
-                                           unsigned long long* msk, int W, uint32_t S, const uint32_t* cmap,
-                                           uint32_t cwords, K EMPTY, uint32_t* s_over, uint32_t* claimed) {
+__device__ __forceinline__ uint32_t fast_pass2(const uint32_t* scr, const uint64_t* scr_pos, uint32_t* list,
+                                               uint32_t nchunks, const uint32_t* __restrict__ packed, int k, K* keys,
+                                               uint32_t* cnt, unsigned long long* msk, int W, uint32_t S,
+                                               const uint32_t* cmap, uint32_t cwords, K EMPTY, uint32_t* s_over,
+                                               uint32_t* claimed) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const uint32_t stride = (uint32_t)nw * 32u;
   uint64_t q0 = 0, q1 = 0;  // queue entries lane and 32 + lane
   uint32_t qn = 0;          // queued entries (warp-uniform)
-  for (uint32_t g = (uint32_t)wid * 32u; g < nchunks; g += (uint32_t)nw * 32u) {
-    if (*(volatile uint32_t*)s_over) break;  // uniform across the warp: read once below
-    const uint32_t c = g + (uint32_t)lane;
-    uint32_t m = 0;
-    uint64_t base = 0;
-    if (c < nchunks) {
-      const uint4 v = reinterpret_cast<const uint4*>(scr)[c];
-      const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const bool want = sub == 0 ? w[j] == WIN_REPEAT
-                                   : (w[j] < 0x80000000u && claimed_test(cmap, cwords, w[j]));
-        m |= want ? (1u << j) : 0u;
-      }
-      if (m) base = scr_pos[c];
+  uint32_t ln = 0;          // entries in this warp's first-sight list (warp-uniform)
+  uint32_t g = (uint32_t)wid * 32u;
+  uint4 v = make_uint4(WIN_DONE, WIN_DONE, WIN_DONE, WIN_DONE);
+  uint64_t base = 0;
+  if (g + (uint32_t)lane < nchunks) {
+    v = reinterpret_cast<const uint4*>(scr)[g + lane];
+    base = scr_pos[g + lane];
+  }
+  for (; g < nchunks; g += stride) {
+    // the next group's records, in flight while this one is processed
+    uint4 vn = make_uint4(WIN_DONE, WIN_DONE, WIN_DONE, WIN_DONE);
+    uint64_t bn = 0;
+    if (g + stride + (uint32_t)lane < nchunks) {
+      vn = reinterpret_cast<const uint4*>(scr)[g + stride + lane];
+      bn = scr_pos[g + stride + lane];
     }
-    // gather this group's windows into the queue, 32 at a time
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    uint32_t m = 0, f = 0;  // repeats; listed first sights
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      m |= (w[j] == WIN_REPEAT) ? (1u << j) : 0u;
+      f |= (w[j] < 0x80000000u && claimed_test(cmap, cwords, w[j])) ? (1u << j) : 0u;
+    }
+    // first sights to the warp's list (slots from a warp scan)
+    {
+      const uint32_t n = __popc(f);
+      uint32_t incl = n;
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      uint32_t at = ln + incl - n;
+      for (uint32_t ff = f; ff; ff &= ff - 1) list[at++] = ((g + (uint32_t)lane) << 2) | (uint32_t)(__ffs(ff) - 1);
+      ln += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    // repeats through the queue, 32 at a time
     const uint32_t n = __popc(m);
     uint32_t incl = n;
     for (int o = 1; o < 32; o <<= 1) {
@@ -228,8 +251,8 @@ __device__ __forceinline__ void fast_pass2(int sub, const uint32_t* scr, const u
       int src = 0;
 #pragma unroll
       for (int step = 16; step > 0; step >>= 1) {
-        const uint32_t v = __shfl_sync(0xffffffffu, incl, src + step - 1);
-        if (v <= t) src += step;
+        const uint32_t x = __shfl_sync(0xffffffffu, incl, src + step - 1);
+        if (x <= t) src += step;
       }
       const uint32_t ms = __shfl_sync(0xffffffffu, m, src & 31);
       const uint32_t es = __shfl_sync(0xffffffffu, excl, src & 31);
@@ -245,16 +268,32 @@ __device__ __forceinline__ void fast_pass2(int sub, const uint32_t* scr, const u
         else q1 = er;
       }
       if (qn + gsz >= 32) {
-        lookup_window<K, R, MODE>(sub, q0, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
+        lookup_window<K, R, MODE>(0, q0, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
         q0 = q1;
         qn = qn + gsz - 32;
       } else {
         qn += gsz;
       }
     }
+    v = vn;
+    base = bn;
   }
-  if ((uint32_t)lane < qn)
-    lookup_window<K, R, MODE>(sub, q0, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
+  if ((uint32_t)lane < qn) lookup_window<K, R, MODE>(0, q0, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
+  return ln;
+}
+
+// pass 3: this warp's listed first sights, 32 lookups at a time
+template <class K, class R, int MODE>
+__device__ __forceinline__ void fast_pass3(const uint64_t* scr_pos, const uint32_t* list, uint32_t ln,
+                                           const uint32_t* __restrict__ packed, int k, K* keys, uint32_t* cnt,
+                                           unsigned long long* msk, int W, uint32_t S, K EMPTY, uint32_t* s_over,
+                                           uint32_t* claimed) {
+  const int lane = threadIdx.x & 31;
+  for (uint32_t i = (uint32_t)lane; i < ln; i += 32) {
+    const uint32_t e = list[i];
+    const uint64_t pos = scr_pos[e >> 2] + (e & 3u);
+    lookup_window<K, R, MODE>(1, pos, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
+  }
 }
 
 }  // namespace
@@ -308,11 +347,15 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
   uint32_t* cmap = bmap + bwords;
   // this CTA's per-window scratch of fast filtered rounds (L2-resident: a
   // round writes and re-reads only its own windows' words)
-  // layout per CTA: scr_chunks uint4 window words, then scr_chunks u64 chunk
-  // positions (base of the chunk's first window | dataset << 48)
+  // layout per CTA: scr_chunks uint4 window words, scr_chunks u64 chunk
+  // positions (base of the chunk's first window | dataset << 48), then one
+  // first-sight list of scr_lcap u32 entries per warp (chunk << 2 | window)
   uint32_t* scr = (filtered && a.win_scratch) ? a.win_scratch + (size_t)blockIdx.x * a.scratch_words : nullptr;
-  const uint32_t scr_chunks = (uint32_t)((a.scratch_words / 6) & ~3ull);
+  const uint32_t scr_nw = blockDim.x >> 5;
+  const uint32_t scr_chunks = (uint32_t)(((a.scratch_words - 4096ull * scr_nw) / 10) & ~3ull);
+  const uint32_t scr_lcap = ((scr_chunks + 32u * scr_nw - 1) / (32u * scr_nw)) * 128u;
   uint64_t* scr_pos = scr ? reinterpret_cast<uint64_t*>(scr + (size_t)scr_chunks * 4) : nullptr;
+  uint32_t* scr_list = scr ? scr + (size_t)scr_chunks * 6 : nullptr;
   off += (size_t)fwords * 4;
   off = (off + 15) & ~(size_t)15;
   uint32_t* occ = reinterpret_cast<uint32_t*>(smem + off);   // NP2 + 1, becomes occupancy prefix
@@ -331,7 +374,6 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
   __shared__ float s_rho;
   __shared__ uint32_t sh_cpre[MAX_THREADS + 1];
   __shared__ uint32_t sh_cpre32[MAX_THREADS / 32];
-  __shared__ uint32_t s_step;
   __shared__ uint32_t s_cbase;  // chunks of the round's earlier batches
   __shared__ uint64_t sh_desc[MAX_THREADS];
   __shared__ uint16_t sh_dset[MODE == 1 ? MAX_THREADS : 1];
@@ -536,21 +578,18 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
         uint32_t total = 0;
         for (int ph = filtered ? 1 : 0; ph <= (filtered ? 2 : 0); ph++) {
           if (ph == 2 && fast) {
-            // ---- passes 2a and 2b of a fast round, over its chunk records
+            // ---- passes 2 and 3 of a fast round, over its chunk records
             __syncthreads();
             const uint32_t nchunks = s_cbase;
-            for (int sub = 0; sub < 2; sub++) {
-              fast_pass2<K, R, MODE>(sub, scr, scr_pos, nchunks, a.packed, k, keys, cnt, msk, W, S, cmap, cwords,
-                                     EMPTY, &s_over, &claimed);
-              __syncthreads();
-              if (s_over) break;
-            }
+            uint32_t* list = scr_list + (size_t)(tid >> 5) * scr_lcap;
+            const uint32_t ln = fast_pass2<K, R, MODE>(scr, scr_pos, list, nchunks, a.packed, k, keys, cnt, msk, W, S,
+                                                       cmap, cwords, EMPTY, &s_over, &claimed);
+            __syncthreads();
+            if (!s_over)
+              fast_pass3<K, R, MODE>(scr_pos, list, ln, a.packed, k, keys, cnt, msk, W, S, EMPTY, &s_over, &claimed);
             break;
           }
-          if (tid == 0) {
-            s_cbase = 0;
-            if (ph == 2 && one_batch) s_step = 0;
-          }
+          if (tid == 0) s_cbase = 0;
           __syncthreads();
           for (uint64_t bb = dlo; bb < dhi; bb += (uint64_t)nth) {
             if (!(ph == 2 && one_batch)) {
@@ -569,7 +608,6 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
                 }
               }
               sh_desc[tid] = dsc;
-              if (tid == 0) s_step = 0;  // the previous batch's steps all ended before its closing barrier
               const uint32_t cp = block_excl_scan_u32(nch, &total, warp_tmp);
               sh_cpre[tid] = cp;
               if (lane == 0) sh_cpre32[tid >> 5] = cp;
@@ -578,17 +616,16 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
             }
             const int nd = (int)min((uint64_t)nth, dhi - bb);
             const uint32_t cbase = s_cbase;
-            // Warps take steps of 32 chunks (one per lane) from a shared
-            // counter, so a batch ends with at most one step of imbalance.  The
+            // Warps take steps of 32 chunks (one per lane) round-robin: step
+            // t goes to warp t mod (warps), so a batch ends with at most one
+            // step of imbalance.  (Handing steps out from a shared counter
+            // serialised every step on one shared-memory address.)  The
             // descriptor of the step's first chunk comes from a two-level
             // 32-ary search (every 32nd prefix is kept apart, conflict-free);
             // every descriptor holds >= 1 chunk, so at most 32 descriptor
             // starts fall inside a step and a lane's descriptor is jw + (starts
             // at or before its chunk).
-            for (;;) {
-              uint32_t c0 = 0;
-              if (lane == 0) c0 = atomicAdd(&s_step, 32u);
-              c0 = __shfl_sync(0xffffffffu, c0, 0);
+            for (uint32_t c0 = (uint32_t)(tid >> 5) * 32u;; c0 += (uint32_t)nth) {
               if (c0 >= total || __any_sync(0xffffffffu, *(volatile uint32_t*)&s_over)) break;
               const int i1 = lane << 5;
               const unsigned b1 = __ballot_sync(0xffffffffu, i1 < nd && sh_cpre32[lane] <= c0);
