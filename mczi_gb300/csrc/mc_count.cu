@@ -91,35 +91,56 @@ __device__ __forceinline__ uint32_t popc_words(const unsigned long long* m, int 
   return c;
 }
 
-// Filtered rounds use two blocked Bloom filters in shared memory, each a key
-// sets two bits of one 32-bit word: the seen map (pass 1: a window whose two
-// bits were both set already is a repeat, or a collision) and the claimed map
-// (set for every key stored in the table; pass 2 looks up only windows whose
-// claimed bits are both set).  Two bits per key cut the collision rate to
-// about a third of one bit's at the densities the rounds run at.
+// Filtered rounds keep two bitmaps in shared memory.  The seen map is a
+// blocked Bloom filter: a key sets two bits of one 32-bit word, and a window
+// whose two bits were both set already is a repeat (or a collision).  Two
+// bits per key cut the collision rate to about a third of one bit's at the
+// densities the rounds run at.  The claimed map has one bit per 16-bit key
+// code and is set for every key stored in the table, so that a first sight
+// whose claimed bit is clear is known not to be stored.
 //   seen map   : word from hash bits 20..51, bits from 52..56 and 57..61
-//   claimed map: from hb31 = hash bits 20..50 (the value kept per window)
+//   key code   : hash bits 20..35, folded below 0xfffe (the per-window word
+//                of fast rounds; 0xfffe and 0xffff mark repeats and done)
 __device__ __forceinline__ bool seen_test_set(uint32_t* bmap, uint32_t bwords, uint64_t hv) {
   const uint32_t wi = (uint32_t)((((hv >> 20) & 0xffffffffull) * (uint64_t)bwords) >> 32);
   const uint32_t m = (1u << ((uint32_t)(hv >> 52) & 31u)) | (1u << ((uint32_t)(hv >> 57) & 31u));
   return (atomicOr(&bmap[wi], m) & m) == m;
 }
-__device__ __forceinline__ uint32_t hb31_of(uint64_t hv) { return (uint32_t)(hv >> 20) & 0x7fffffffu; }
-__device__ __forceinline__ void claimed_set(uint32_t* cmap, uint32_t cwords, uint32_t hb31) {
-  const uint32_t wi = (uint32_t)(((uint64_t)hb31 * (uint64_t)cwords) >> 31);
-  atomicOr(&cmap[wi], (1u << (hb31 & 31u)) | (1u << ((hb31 >> 5) & 31u)));
+__device__ __forceinline__ uint32_t key_code(uint64_t hv) {
+  const uint32_t c = (uint32_t)(hv >> 20) & 0xffffu;
+  return c >= 0xfffeu ? c - 2u : c;
 }
-__device__ __forceinline__ bool claimed_test(const uint32_t* cmap, uint32_t cwords, uint32_t hb31) {
-  const uint32_t wi = (uint32_t)(((uint64_t)hb31 * (uint64_t)cwords) >> 31);
-  const uint32_t m = (1u << (hb31 & 31u)) | (1u << ((hb31 >> 5) & 31u));
-  return (cmap[wi] & m) == m;
+__device__ __forceinline__ void claimed_set(uint32_t* cmap, uint32_t cbits, uint32_t code) {
+  const uint32_t b = (code * cbits) >> 16;
+  atomicOr(&cmap[b >> 5], 1u << (b & 31u));
+}
+__device__ __forceinline__ bool claimed_test(const uint32_t* cmap, uint32_t cbits, uint32_t code) {
+  const uint32_t b = (code * cbits) >> 16;
+  return (cmap[b >> 5] >> (b & 31u)) & 1u;
 }
 
-// per-window word of the fast filtered rounds' scratch: hb31 of a window seen
-// for the first time in pass 1, or WIN_DONE (counted in pass 1, outside the
-// round's hash range, or past the end of its chunk)
-constexpr uint32_t WIN_DONE = 0xffffffffu;
-constexpr uint32_t WIN_REPEAT = 0xfffffffeu;  // a repeat of pass 1 (hb31 < 2^31 marks a first sight)
+// per-window 16-bit word of the fast filtered rounds' scratch: the key code
+// of a window seen for the first time in pass 1, W16_REPEAT for a repeat, or
+// W16_DONE (outside the round's hash range, or past the end of its chunk)
+constexpr uint32_t W16_DONE = 0xffffu;
+constexpr uint32_t W16_REPEAT = 0xfffeu;
+
+// chunk reference of the scratch: round-relative descriptor index << 10 |
+// chunk within the descriptor (windows <= 4096, so < 1024 chunks of 4)
+__device__ __forceinline__ uint64_t chunk_pos(uint32_t ref, const uint64_t* __restrict__ rdesc) {
+  return bd_start(rdesc[ref >> 10]) + (uint64_t)(ref & 1023u) * 4u;
+}
+
+// dataset (input) of a base position: the largest i with dsbase[i] <= pos
+__device__ __forceinline__ uint32_t dataset_of(const uint64_t* dsbase, int n, uint64_t pos) {
+  int l = 0, h = n;
+  while (h - l > 1) {
+    const int mid = (l + h) >> 1;
+    if (dsbase[mid] <= pos) l = mid;
+    else h = mid;
+  }
+  return (uint32_t)l;
+}
 
 // the k-mer starting at base `pos` of the packed stream
 template <class K, class R>
@@ -145,11 +166,10 @@ __device__ __forceinline__ void roll_at(R& roll, const uint32_t* __restrict__ pa
 // packed stream.  Each warp keeps its own list, so no shared counter is
 // touched.
 template <class K, class R, int MODE>
-__device__ __forceinline__ void lookup_window(int sub, uint64_t e, const uint32_t* __restrict__ packed, int k,
-                                              K* keys, uint32_t* cnt, unsigned long long* msk, int W, uint32_t S,
-                                              K EMPTY, uint32_t* s_over, uint32_t* claimed) {
-  const uint64_t pos = e & ((1ull << 48) - 1);
-  const uint32_t dset = (uint32_t)(e >> 48);
+__device__ __forceinline__ void lookup_window(int sub, uint64_t pos, uint32_t dset,
+                                              const uint32_t* __restrict__ packed, int k, K* keys, uint32_t* cnt,
+                                              unsigned long long* msk, int W, uint32_t S, K EMPTY, uint32_t* s_over,
+                                              uint32_t* claimed) {
   R roll;
   roll_at<K, R>(roll, packed, pos, k);
   const uint64_t hv = sym_hash(roll);
@@ -192,37 +212,38 @@ __device__ __forceinline__ void lookup_window(int sub, uint64_t e, const uint32_
 }
 
 template <class K, class R, int MODE>
-__device__ __forceinline__ uint32_t fast_pass2(const uint32_t* scr, const uint64_t* scr_pos, uint32_t* list,
-                                               uint32_t nchunks, const uint32_t* __restrict__ packed, int k, K* keys,
-                                               uint32_t* cnt, unsigned long long* msk, int W, uint32_t S,
-                                               const uint32_t* cmap, uint32_t cwords, K EMPTY, uint32_t* s_over,
-                                               uint32_t* claimed) {
+__device__ __forceinline__ uint32_t fast_pass2(const uint2* words, const uint32_t* refs, uint32_t* list,
+                                               uint32_t nchunks, const uint64_t* __restrict__ rdesc,
+                                               const uint64_t* dsbase, int n_datasets,
+                                               const uint32_t* __restrict__ packed, int k, K* keys, uint32_t* cnt,
+                                               unsigned long long* msk, int W, uint32_t S, const uint32_t* cmap,
+                                               uint32_t cbits, K EMPTY, uint32_t* s_over, uint32_t* claimed) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const uint32_t stride = (uint32_t)nw * 32u;
-  uint64_t q0 = 0, q1 = 0;  // queue entries lane and 32 + lane
+  uint64_t q0 = 0, q1 = 0;  // queued window positions: entries lane and 32 + lane
   uint32_t qn = 0;          // queued entries (warp-uniform)
   uint32_t ln = 0;          // entries in this warp's first-sight list (warp-uniform)
   uint32_t g = (uint32_t)wid * 32u;
-  uint4 v = make_uint4(WIN_DONE, WIN_DONE, WIN_DONE, WIN_DONE);
-  uint64_t base = 0;
+  uint2 v = make_uint2(0xffffffffu, 0xffffffffu);
+  uint32_t ref = 0;
   if (g + (uint32_t)lane < nchunks) {
-    v = reinterpret_cast<const uint4*>(scr)[g + lane];
-    base = scr_pos[g + lane];
+    v = words[g + lane];
+    ref = refs[g + lane];
   }
   for (; g < nchunks; g += stride) {
     // the next group's records, in flight while this one is processed
-    uint4 vn = make_uint4(WIN_DONE, WIN_DONE, WIN_DONE, WIN_DONE);
-    uint64_t bn = 0;
+    uint2 vn = make_uint2(0xffffffffu, 0xffffffffu);
+    uint32_t rn = 0;
     if (g + stride + (uint32_t)lane < nchunks) {
-      vn = reinterpret_cast<const uint4*>(scr)[g + stride + lane];
-      bn = scr_pos[g + stride + lane];
+      vn = words[g + stride + lane];
+      rn = refs[g + stride + lane];
     }
-    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+    const uint32_t w[4] = {v.x & 0xffffu, v.x >> 16, v.y & 0xffffu, v.y >> 16};
     uint32_t m = 0, f = 0;  // repeats; listed first sights
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-      m |= (w[j] == WIN_REPEAT) ? (1u << j) : 0u;
-      f |= (w[j] < 0x80000000u && claimed_test(cmap, cwords, w[j])) ? (1u << j) : 0u;
+      m |= (w[j] == W16_REPEAT) ? (1u << j) : 0u;
+      f |= (w[j] < W16_REPEAT && claimed_test(cmap, cbits, w[j])) ? (1u << j) : 0u;
     }
     // first sights to the warp's list (slots from a warp scan)
     {
@@ -237,6 +258,7 @@ __device__ __forceinline__ uint32_t fast_pass2(const uint32_t* scr, const uint64
       ln += __shfl_sync(0xffffffffu, incl, 31);
     }
     // repeats through the queue, 32 at a time
+    const uint64_t base = m ? chunk_pos(ref, rdesc) : 0ull;
     const uint32_t n = __popc(m);
     uint32_t incl = n;
     for (int o = 1; o < 32; o <<= 1) {
@@ -268,7 +290,8 @@ __device__ __forceinline__ uint32_t fast_pass2(const uint32_t* scr, const uint64
         else q1 = er;
       }
       if (qn + gsz >= 32) {
-        lookup_window<K, R, MODE>(0, q0, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
+        const uint32_t ds = MODE == 1 ? dataset_of(dsbase, n_datasets, q0) : 0u;
+        lookup_window<K, R, MODE>(0, q0, ds, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
         q0 = q1;
         qn = qn + gsz - 32;
       } else {
@@ -276,23 +299,28 @@ __device__ __forceinline__ uint32_t fast_pass2(const uint32_t* scr, const uint64
       }
     }
     v = vn;
-    base = bn;
+    ref = rn;
   }
-  if ((uint32_t)lane < qn) lookup_window<K, R, MODE>(0, q0, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
+  if ((uint32_t)lane < qn) {
+    const uint32_t ds = MODE == 1 ? dataset_of(dsbase, n_datasets, q0) : 0u;
+    lookup_window<K, R, MODE>(0, q0, ds, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
+  }
   return ln;
 }
 
 // pass 3: this warp's listed first sights, 32 lookups at a time
 template <class K, class R, int MODE>
-__device__ __forceinline__ void fast_pass3(const uint64_t* scr_pos, const uint32_t* list, uint32_t ln,
-                                           const uint32_t* __restrict__ packed, int k, K* keys, uint32_t* cnt,
-                                           unsigned long long* msk, int W, uint32_t S, K EMPTY, uint32_t* s_over,
-                                           uint32_t* claimed) {
+__device__ __forceinline__ void fast_pass3(const uint32_t* refs, const uint32_t* list, uint32_t ln,
+                                           const uint64_t* __restrict__ rdesc, const uint64_t* dsbase,
+                                           int n_datasets, const uint32_t* __restrict__ packed, int k, K* keys,
+                                           uint32_t* cnt, unsigned long long* msk, int W, uint32_t S, K EMPTY,
+                                           uint32_t* s_over, uint32_t* claimed) {
   const int lane = threadIdx.x & 31;
   for (uint32_t i = (uint32_t)lane; i < ln; i += 32) {
     const uint32_t e = list[i];
-    const uint64_t pos = scr_pos[e >> 2] + (e & 3u);
-    lookup_window<K, R, MODE>(1, pos, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
+    const uint64_t pos = chunk_pos(refs[e >> 2], rdesc) + (e & 3u);
+    const uint32_t ds = MODE == 1 ? dataset_of(dsbase, n_datasets, pos) : 0u;
+    lookup_window<K, R, MODE>(1, pos, ds, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
   }
 }
 
@@ -340,22 +368,25 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
   // filtered rounds: the seen-once bitmap (7/8 of the words) and a coarser
   // claimed-key bitmap (1/8) that lets pass 2 skip the table for keys pass 1
   // never stored (both indexed by the same 32 hash bits)
-  const uint32_t cwords = filtered ? ((fwords / 8) & ~31u) : 0u;
+  const uint32_t cwords = filtered ? min(2048u, (fwords / 4) & ~31u) : 0u;
+  const uint32_t cbits = cwords * 32u;
   const uint32_t bwords = fwords - cwords;
   const uint64_t fbits = (uint64_t)bwords * 32;
   uint32_t* bmap = reinterpret_cast<uint32_t*>(smem + off);
   uint32_t* cmap = bmap + bwords;
   // this CTA's per-window scratch of fast filtered rounds (L2-resident: a
   // round writes and re-reads only its own windows' words)
-  // layout per CTA: scr_chunks uint4 window words, scr_chunks u64 chunk
-  // positions (base of the chunk's first window | dataset << 48), then one
-  // first-sight list of scr_lcap u32 entries per warp (chunk << 2 | window)
+  // layout per CTA (12 bytes per chunk of 4 windows, plus the lists):
+  // scr_chunks uint2 records of four 16-bit window words, scr_chunks u32
+  // chunk references (chunk_pos), then one first-sight list of scr_lcap u32
+  // entries per warp (chunk << 2 | window)
   uint32_t* scr = (filtered && a.win_scratch) ? a.win_scratch + (size_t)blockIdx.x * a.scratch_words : nullptr;
   const uint32_t scr_nw = blockDim.x >> 5;
-  const uint32_t scr_chunks = (uint32_t)(((a.scratch_words - 4096ull * scr_nw) / 10) & ~3ull);
+  const uint32_t scr_chunks = (uint32_t)(((a.scratch_words - 4096ull * scr_nw) / 7) & ~3ull);
   const uint32_t scr_lcap = ((scr_chunks + 32u * scr_nw - 1) / (32u * scr_nw)) * 128u;
-  uint64_t* scr_pos = scr ? reinterpret_cast<uint64_t*>(scr + (size_t)scr_chunks * 4) : nullptr;
-  uint32_t* scr_list = scr ? scr + (size_t)scr_chunks * 6 : nullptr;
+  uint2* scr_words = reinterpret_cast<uint2*>(scr);
+  uint32_t* scr_refs = scr ? scr + (size_t)scr_chunks * 2 : nullptr;
+  uint32_t* scr_list = scr ? scr + (size_t)scr_chunks * 3 : nullptr;
   off += (size_t)fwords * 4;
   off = (off + 15) & ~(size_t)15;
   uint32_t* occ = reinterpret_cast<uint32_t*>(smem + off);   // NP2 + 1, becomes occupancy prefix
@@ -559,22 +590,26 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
         //   collision, harmless).  A k-mer seen once is never stored, one seen
         //   twice or more always is, so for x >= 1 the emitted set and counts
         //   equal the single pass'.  Two ways to count the claimed keys:
-        //   - fast (the round's windows fit the CTA's scratch): pass 1 also
-        //     counts every repeat it looks up and writes one word per window
-        //     to the scratch -- hb31 for a first sight, WIN_DONE otherwise; pass
-        //     2 reads those words (no rolling) and looks up only first sights
-        //     whose claimed bits are set, re-extracting just their k-mers.
-        //     Every occurrence is counted once: repeats in pass 1 (the claiming
-        //     one implicitly), the first sight in pass 2.
-        //   - otherwise pass 1 only claims and pass 2 re-rolls every window and
-        //     counts every occurrence of the claimed keys.
+        //   - fast (the round's chunks fit the CTA's scratch): pass 1 touches
+        //     no table; it writes a 16-bit word per window (the key code of a
+        //     first sight, W16_REPEAT for a repeat) and a reference per chunk
+        //     to the scratch.  Pass 2 reads those records (no rolling), stores
+        //     or counts every repeat and lists the first sights whose claimed
+        //     bit is set; pass 3 counts the listed first sights whose key is
+        //     stored.  Only the looked-up windows' k-mers are re-extracted,
+        //     and the lookups run in full warps (fast_pass2).  Every
+        //     occurrence of a stored key is counted once: its claiming repeat
+        //     implicitly, the other repeats in pass 2, the first sight in 3.
+        //   - otherwise pass 1 claims the repeats and pass 2 re-rolls every
+        //     window and counts every occurrence of the claimed keys.
         // a round of one batch keeps that batch's descriptors and chunk
         // prefixes in shared memory from pass 1 to pass 2
         const bool one_batch = dhi - dlo <= (uint64_t)nth;
         // chunks of the round <= (windows + descriptors * (chunk - 1)) / chunk
         const uint64_t round_windows = (uint64_t)(occ[rr.bh] - occ[rr.bl]);
         const bool fast = scr != nullptr && chunk == 4 &&
-                          (round_windows + (uint64_t)(dhi - dlo) * 3) / 4 <= scr_chunks;
+                          (round_windows + (uint64_t)(dhi - dlo) * 3) / 4 <= scr_chunks &&
+                          dhi - dlo < (1u << 22);  // chunk references: 22-bit descriptor index
         uint32_t total = 0;
         for (int ph = filtered ? 1 : 0; ph <= (filtered ? 2 : 0); ph++) {
           if (ph == 2 && fast) {
@@ -582,11 +617,14 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
             __syncthreads();
             const uint32_t nchunks = s_cbase;
             uint32_t* list = scr_list + (size_t)(tid >> 5) * scr_lcap;
-            const uint32_t ln = fast_pass2<K, R, MODE>(scr, scr_pos, list, nchunks, a.packed, k, keys, cnt, msk, W, S,
-                                                       cmap, cwords, EMPTY, &s_over, &claimed);
+            const uint64_t* rdesc = a.desc + lo + dlo;
+            const uint32_t ln = fast_pass2<K, R, MODE>(scr_words, scr_refs, list, nchunks, rdesc, dsbase,
+                                                       a.n_datasets, a.packed, k, keys, cnt, msk, W, S, cmap, cbits,
+                                                       EMPTY, &s_over, &claimed);
             __syncthreads();
             if (!s_over)
-              fast_pass3<K, R, MODE>(scr_pos, list, ln, a.packed, k, keys, cnt, msk, W, S, EMPTY, &s_over, &claimed);
+              fast_pass3<K, R, MODE>(scr_refs, list, ln, rdesc, dsbase, a.n_datasets, a.packed, k, keys, cnt, msk, W,
+                                     S, EMPTY, &s_over, &claimed);
             break;
           }
           if (tid == 0) s_cbase = 0;
@@ -655,7 +693,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
               uint32_t q = (uint32_t)(p & 15);
               uint32_t word = *wp << (2 * q);
               // pass 1 of a fast round: the chunk's words, stored at its end
-              uint32_t r0 = WIN_DONE, r1 = WIN_DONE, r2 = WIN_DONE, r3 = WIN_DONE;
+              uint32_t r0 = W16_DONE, r1 = W16_DONE, r2 = W16_DONE, r3 = W16_DONE;
               for (uint32_t j = w0; j < w1; j++) {
                 if (j > w0) {
                   roll.push(word >> 30);
@@ -667,12 +705,12 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
                 const uint64_t hv = sym_hash(roll);
                 if (!full_range) {
                   const uint32_t hk = (uint32_t)(hv >> 32);
-                  if (hk < rr.hlo || hk > rr.hhi) continue;  // its word stays WIN_DONE
+                  if (hk < rr.hlo || hk > rr.hhi) continue;  // its word stays W16_DONE
                 }
-                const uint32_t hb = hb31_of(hv);
+                const uint32_t hb = key_code(hv);
                 if (ph == 2) {
                   // slow pass 2: a key pass 1 never stored has its claimed bits clear
-                  if (!claimed_test(cmap, cwords, hb)) continue;
+                  if (!claimed_test(cmap, cbits, hb)) continue;
                   const K key = roll.canon();
                   uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
                   // keys are final during pass 2: plain loads, stop at EMPTY
@@ -690,11 +728,11 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
                 }
                 if (ph == 1) {
                   const bool repeat = seen_test_set(bmap, bwords, hv);
-                  if (repeat) claimed_set(cmap, cwords, hb);  // stored below, or in pass 2a
+                  if (repeat) claimed_set(cmap, cbits, hb);  // stored below, or in pass 2
                   if (fast) {
-                    // a fast round only records the window: hb31 for a first
-                    // sight, WIN_REPEAT for a repeat (stored by pass 2a)
-                    const uint32_t v = repeat ? WIN_REPEAT : hb;
+                    // a fast round only records the window: its key code for a
+                    // first sight, W16_REPEAT for a repeat (stored by pass 2)
+                    const uint32_t v = repeat ? W16_REPEAT : hb;
                     const uint32_t jj = j - w0;
                     r0 = jj == 0 ? v : r0;
                     r1 = jj == 1 ? v : r1;
@@ -742,8 +780,8 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
               }
               if (ph == 1 && fast) {
                 const uint32_t ci = cbase + c;
-                reinterpret_cast<uint4*>(scr)[ci] = make_uint4(r0, r1, r2, r3);
-                scr_pos[ci] = s0 | ((uint64_t)dset << 48);
+                scr_words[ci] = make_uint2(r0 | (r1 << 16), r2 | (r3 << 16));
+                scr_refs[ci] = ((uint32_t)(bb - dlo + (uint64_t)lo2) << 10) | (w0 >> 2);
               }
             }
             __syncthreads();
