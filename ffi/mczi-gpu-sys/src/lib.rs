@@ -120,6 +120,7 @@ extern "C" {
                            n_kmers: *mut u64, latency_ms: *mut f64, queue_ms: *mut f64) -> i32;
     pub fn mczi_serve_result(srv: *mut mczi_server, request_id: u64, key_lo: *mut u64, key_hi: *mut u64, cap: u64,
                              n: *mut u64) -> i32;
+    pub fn mczi_serve_release(srv: *mut mczi_server, request_id: u64) -> i32;
     pub fn mczi_serve_error(srv: *mut mczi_server, request_id: u64) -> *const c_char;
     pub fn mczi_serve_stats(srv: *mut mczi_server, out: *mut f64, cap: i32) -> i32;
     pub fn mczi_serve_close(srv: *mut mczi_server) -> i32;

@@ -302,6 +302,9 @@ int32_t mczi_serve_next(mczi_server* srv, int32_t timeout_ms, uint64_t* request_
  * mczi_serve_error gives its message until then. */
 int32_t mczi_serve_result(mczi_server* srv, uint64_t request_id, uint64_t* key_lo, uint64_t* key_hi, uint64_t cap,
                           uint64_t* n);
+/* Releases a reported request without copying its absent set (a client that
+ * needs only the size from mczi_serve_next); returns the request's status. */
+int32_t mczi_serve_release(mczi_server* srv, uint64_t request_id);
 /* mczi_serve_error(NULL, 0) gives the message of this thread's last failed
  * mczi_serve_open. */
 const char* mczi_serve_error(mczi_server* srv, uint64_t request_id);

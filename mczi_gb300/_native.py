@@ -108,6 +108,7 @@ SIGNATURES = [
                                     C.POINTER(C.c_uint64), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("mczi_serve_result", C.c_int32, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_uint64,
                                       C.POINTER(C.c_uint64)]),
+    ("mczi_serve_release", C.c_int32, [C.c_void_p, C.c_uint64]),
     ("mczi_serve_error", C.c_char_p, [C.c_void_p, C.c_uint64]),
     ("mczi_serve_stats", C.c_int32, [C.c_void_p, C.POINTER(C.c_double), C.c_int32]),
     ("mczi_serve_close", C.c_int32, [C.c_void_p]),

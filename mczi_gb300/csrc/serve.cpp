@@ -28,10 +28,72 @@ using Clock = std::chrono::steady_clock;
 // bits, superkmer descriptors (double-buffered) and keys, absent runs
 constexpr double HBM_BYTES_PER_QUERY_BYTE = 8.0;
 
+// Pinned host blocks for batch results, reused across batches: the absent
+// sets of a batch (hundreds of MB at full load) reach the host at the link's
+// speed only in pinned memory, and a fresh pageable allocation per batch
+// costs a page fault per 4 KiB on first touch.  A block returns to the pool
+// when the last request of its batch has been copied out; the pool keeps at
+// most POOL_MAX_BYTES of free blocks.
+class PinnedPool {
+ public:
+  static constexpr size_t POOL_MAX_BYTES = 16ull << 30;
+  ~PinnedPool() {
+    for (auto& b : free_) cudaFreeHost(b.first);
+  }
+  // a block of at least `bytes`, or nullptr when pinned memory is exhausted
+  void* get(size_t bytes, size_t* cap) {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      size_t best = free_.size();
+      for (size_t i = 0; i < free_.size(); i++)
+        if (free_[i].second >= bytes && (best == free_.size() || free_[i].second < free_[best].second)) best = i;
+      if (best < free_.size()) {
+        void* p = free_[best].first;
+        *cap = free_[best].second;
+        cached_ -= *cap;
+        free_.erase(free_.begin() + (long)best);
+        return p;
+      }
+    }
+    const size_t want = bytes + bytes / 4;  // room for a slightly larger batch next time
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, want, cudaHostAllocPortable) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    *cap = want;
+    return p;
+  }
+  void put(void* p, size_t cap) {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (cached_ + cap <= POOL_MAX_BYTES) {
+        free_.emplace_back(p, cap);
+        cached_ += cap;
+        return;
+      }
+    }
+    cudaFreeHost(p);
+  }
+
+ private:
+  std::mutex mu_;
+  std::vector<std::pair<void*, size_t>> free_;
+  size_t cached_ = 0;
+};
+
 // one batch's absent sets, split per request on the device and copied to
-// the host once (left uninitialised until then); requests keep a range
+// the host once into a pinned block; requests keep a range of it
 struct BatchResult {
-  std::unique_ptr<uint64_t[]> lo, hi;
+  std::shared_ptr<PinnedPool> pool;
+  void* block = nullptr;
+  size_t cap = 0;
+  uint64_t* lo = nullptr;
+  uint64_t* hi = nullptr;
+  std::unique_ptr<uint64_t[]> heap;  // when pinned memory ran out
+  ~BatchResult() {
+    if (block) pool->put(block, cap);
+  }
 };
 
 struct ServeRequest {
@@ -69,6 +131,7 @@ struct mczi_server {
   bool stop = false;
   uint64_t batches = 0, answered = 0, largest = 0;
   double t_query = 0.0, t_results = 0.0;
+  std::shared_ptr<PinnedPool> pool = std::make_shared<PinnedPool>();
 };
 
 namespace {
@@ -96,13 +159,21 @@ void answer(mczi_server* S, mczi_ctx* ctx, const std::vector<ServeRequest*>& bat
   uint64_t records = 0, total = 0;
   std::vector<uint64_t> offs(n + 1, 0);
   auto br = std::make_shared<BatchResult>();
+  br->pool = S->pool;
   int32_t rc = mczi_zi_query_per_input(ctx, in.data(), n, &records);
   const Clock::time_point tq = Clock::now();
   if (rc == MCZI_OK) rc = mczi_zi_batch_split(ctx, nullptr, nullptr, offs.data(), 0, &total);
   if (rc == MCZI_OK && total > 0) {
-    br->lo.reset(new uint64_t[total]);
-    if (S->k > 32) br->hi.reset(new uint64_t[total]);
-    rc = mczi_zi_batch_split(ctx, br->lo.get(), br->hi.get(), offs.data(), total, &total);
+    const size_t words = (size_t)total * (S->k > 32 ? 2 : 1);
+    br->block = S->pool->get(words * 8, &br->cap);
+    if (br->block) {
+      br->lo = static_cast<uint64_t*>(br->block);
+    } else {
+      br->heap.reset(new uint64_t[words]);
+      br->lo = br->heap.get();
+    }
+    if (S->k > 32) br->hi = br->lo + total;
+    rc = mczi_zi_batch_split(ctx, br->lo, br->hi, offs.data(), total, &total);
   }
   const std::string err = rc == MCZI_OK ? std::string() : std::string(mczi_last_error(ctx));
   for (size_t i = 0; i < n; i++) {
@@ -266,12 +337,24 @@ int32_t mczi_serve_result(mczi_server* S, uint64_t request_id, uint64_t* key_lo,
     S->reqs.erase(it);
   }
   const uint64_t cnt = r->cnt;
-  if (cnt) std::memcpy(key_lo, r->res->lo.get() + r->off, cnt * 8);
+  if (cnt) std::memcpy(key_lo, r->res->lo + r->off, cnt * 8);
   if (key_hi && cnt) {
     if (!r->res->hi) std::memset(key_hi, 0, cnt * 8);
-    else std::memcpy(key_hi, r->res->hi.get() + r->off, cnt * 8);
+    else std::memcpy(key_hi, r->res->hi + r->off, cnt * 8);
   }
   return MCZI_OK;  // the batch's buffer goes with its last request
+}
+
+int32_t mczi_serve_release(mczi_server* S, uint64_t request_id) {
+  if (!S) return MCZI_ERR_STATE;
+  std::unique_ptr<ServeRequest> r;  // destroyed after the lock is dropped
+  std::lock_guard<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(request_id);
+  if (it == S->reqs.end() || it->second->finished == Clock::time_point()) return MCZI_ERR_STATE;
+  const int32_t st = it->second->status;
+  r = std::move(it->second);
+  S->reqs.erase(it);
+  return st;
 }
 
 const char* mczi_serve_error(mczi_server* S, uint64_t request_id) {

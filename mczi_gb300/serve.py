@@ -12,8 +12,9 @@ result it gets alone.  Batches of different workers overlap on the device.
 
 This module wraps the native server in futures: ``submit`` returns a
 ``concurrent.futures.Future`` whose result is the request's absent set (k <=
-32: a uint64 array; k > 32: an (n, 2) array of (lo, hi)); the future carries
-``latency_ms`` and ``queue_ms`` once done.
+32: a uint64 array; k > 32: an (n, 2) array of (lo, hi)), or only its size
+with ``keep_results=False``; the future carries ``latency_ms`` and
+``queue_ms`` once done.
 
 No counterpart exists in the reference (ZI is a one-shot CLI, src/zi.rs:64-101).
 """
@@ -32,12 +33,15 @@ from .mc import _as_bytes
 
 class ZIServer:
     def __init__(self, index, k: int, m: int | None = None, workers: int = 2, device: int = 0,
-                 max_batch: int = 64, hbm_budget: int | None = None, hbm_free_fn=None):
+                 max_batch: int = 64, hbm_budget: int | None = None, hbm_free_fn=None, keep_results: bool = True):
         zi.validate_k(k)
         m = zi.default_minimizer_size(k) if m is None else m
         if not 0 < m < k:
             raise N.MCZIError(N.MCZI_ERR_INVALID_CONFIG, "minimizer size must be > 0 and < k")
         self.k = k
+        # keep_results=False: futures give only the absent-set size and the
+        # native server releases each request without copying its k-mers
+        self.keep_results = keep_results
         self._lib = N.load()
         if hbm_budget is None:
             hbm_budget = int(0.6 * hbm_free_fn()) if hbm_free_fn else 0  # 0: the library asks the device
@@ -118,6 +122,10 @@ class ZIServer:
                 err = N.MCZIError(st.value, msg.decode() if msg else "")
                 self._lib.mczi_serve_result(self._h, rid.value, _EMPTY.ctypes.data, None, 0, None)  # release
                 fut.set_exception(err)
+                continue
+            if not self.keep_results:
+                self._lib.mczi_serve_release(self._h, rid.value)
+                fut.set_result(int(n.value))
                 continue
             lo = np.empty(n.value, dtype=np.uint64)
             hi = np.empty(n.value, dtype=np.uint64) if self.k > 32 else None

@@ -66,6 +66,10 @@ class FakeServeLib:
             C.memmove(lo, r.ctypes.data, r.nbytes)
         return N.MCZI_OK
 
+    def mczi_serve_release(self, h, i):
+        self.results.pop(i, None)
+        return N.MCZI_ERR_DEVICE if i in self.errors else N.MCZI_OK
+
     def mczi_serve_error(self, h, i):
         return self.errors.get(i, b"")
 
@@ -94,3 +98,16 @@ def test_futures_results_errors_and_close(monkeypatch):
     srv.close()
     assert fake.closed and late.done() and list(late.result()) == sorted(set(b"late"))
     assert not srv._pending
+
+
+def test_sizes_only_client(monkeypatch):
+    """keep_results=False: futures give the absent-set size and the requests
+    are released without copying their k-mers."""
+    fake = FakeServeLib()
+    monkeypatch.setattr(N, "load", lambda required=True: fake)
+    from mczi_gb300.serve import ZIServer
+    with ZIServer(b">i\nACGTACGT\n", 5, 3, workers=1, keep_results=False) as srv:
+        reqs = [bytes([65 + (i % 5)]) * (i + 1) + b"q" for i in range(20)]
+        futs = [srv.submit(r) for r in reqs]
+        assert [f.result(timeout=10) for f in futs] == [len(set(r)) for r in reqs]
+    assert not fake.results

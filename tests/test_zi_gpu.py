@@ -186,6 +186,10 @@ def test_serving_results_match_alone(gpu_ctx, oracle):
     for i in range(len(reqs)):
         assert sorted(int(v) for v in got[i]) == alone[i], i
         assert futs[i].latency_ms >= futs[i].queue_ms >= 0.0
+    # a client that needs only the sizes releases requests without copying
+    with ZIServer(index, 31, 19, workers=2, max_batch=16, keep_results=False) as srv:
+        sizes = [f.result(timeout=120) for f in [srv.submit(r) for r in reqs]]
+    assert sizes == [len(a) for a in alone]
 
 
 def test_serving_wide_keys_and_empty_requests(gpu_ctx, oracle):
