@@ -176,25 +176,6 @@ struct ProbeArgs {
   const uint32_t* bucket_key;
 };
 
-// one pair of atomics per group of lanes emitting together (the run counter
-// and the absent-window total are single addresses every thread hits)
-__device__ __forceinline__ void emit_run(const ProbeArgs& a, uint64_t start, uint32_t len, uint32_t key) {
-  namespace cg = cooperative_groups;
-  cg::coalesced_group g = cg::coalesced_threads();
-  const unsigned long long w = cg::reduce(g, (unsigned long long)len, cg::plus<unsigned long long>());
-  unsigned long long base = 0;
-  if (g.thread_rank() == 0) {
-    base = atomicAdd(a.n_runs, (unsigned long long)g.size());
-    atomicAdd(a.n_absent_windows, w);
-  }
-  base = g.shfl(base, 0);
-  const unsigned long long idx = base + g.thread_rank();
-  if (idx < a.cap) {
-    a.out_desc[idx] = (start << 24) | (uint64_t)(len - 1);
-    a.out_key[idx] = key;
-  }
-}
-
 template <class K, class R>
 __device__ __forceinline__ void roll_set(R& r, const uint32_t* packed, uint64_t s0, int k) {
   r.init(k);
@@ -206,65 +187,146 @@ __device__ __forceinline__ void roll_set(R& r, const uint32_t* packed, uint64_t 
   }
 }
 
+// The probe works in tiles of PROBE_TILE query superkmers per CTA.
+//   A. every thread classifies a share of the tile: a minimizer the index
+//      does not hold maps to an arbitrary bucket whose stored key differs, so
+//      every k-mer of that superkmer is absent (equal canonical k-mers have
+//      equal minimizers) and the whole superkmer is one absent run, emitted
+//      without rolling it; the others go to the tile's list with their bucket;
+//   B. the threads compare the listed superkmers with their buckets, so all
+//      lanes do comparison work (foreign reads, about half of a query, no
+//      longer leave most lanes idle behind a few comparing ones).
+// Absent runs collect in shared memory and leave with one pair of global
+// atomics per tile (single-address global atomics per warp had become the
+// probe's bottleneck); a tile whose runs overflow the buffer appends the rest
+// directly.
+constexpr int PROBE_TILE = 1024;
+constexpr int PROBE_RUNS = 3072;
+
+struct ProbeSmem {
+  uint64_t run_d[PROBE_RUNS];
+  uint32_t run_k[PROBE_RUNS];
+  uint32_t list_i[PROBE_TILE];
+  uint32_t list_b[PROBE_TILE];
+  uint32_t n_run, n_list;
+  unsigned long long w;  // windows of the buffered runs
+  unsigned long long base;
+};
+
+__device__ __forceinline__ void tile_run(const ProbeArgs& a, ProbeSmem& sm, uint64_t start, uint32_t len,
+                                         uint32_t key) {
+  const uint32_t idx = atomicAdd(&sm.n_run, 1u);
+  if (idx < (uint32_t)PROBE_RUNS) {
+    sm.run_d[idx] = (start << 24) | (uint64_t)(len - 1);
+    sm.run_k[idx] = key;
+    atomicAdd(&sm.w, (unsigned long long)len);
+    return;
+  }
+  // buffer full: straight to the output
+  const unsigned long long g = atomicAdd(a.n_runs, 1ull);
+  atomicAdd(a.n_absent_windows, (unsigned long long)len);
+  if (g < a.cap) {
+    a.out_desc[g] = (start << 24) | (uint64_t)(len - 1);
+    a.out_key[g] = key;
+  }
+}
+
 template <class K, class R>
 __global__ void __launch_bounds__(ZI_THREADS) k_zi_probe(ProbeArgs a) {
+  __shared__ ProbeSmem sm;
   const uint64_t n = *a.n_q;
   const int k = a.k;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t d = a.qdesc[i];
-    const uint64_t s0 = d >> 24;
-    const uint32_t nw = (uint32_t)(d & 0xffffffu) + 1u;
-    const uint32_t key = a.qkey[i];
-    const uint64_t b = mphf_lookup(a.v, key);
-    uint32_t blo = 0, bhi = 0;
-    // a minimizer the index does not hold maps to an arbitrary bucket: its
-    // k-mers are all absent (equal canonical k-mers have equal minimizers)
-    if (b < a.n_keys && a.bucket_key[b] == key) { blo = a.bucket_off[b]; bhi = a.bucket_off[b + 1]; }
-    int64_t run = -1;
-    for (uint32_t c0 = 0; c0 < nw; c0 += Q_CHUNK) {
-      const uint32_t cn = min((uint32_t)Q_CHUNK, nw - c0);
-      K q[Q_CHUNK];
-      {
-        R r;
-        roll_set<K, R>(r, a.qpacked, s0 + c0, k);
-        uint64_t p = s0 + c0 + (uint64_t)k;
+  for (uint64_t t0 = (uint64_t)blockIdx.x * PROBE_TILE; t0 < n; t0 += (uint64_t)gridDim.x * PROBE_TILE) {
+    if (threadIdx.x == 0) { sm.n_run = 0; sm.n_list = 0; sm.w = 0; }
+    __syncthreads();
+    // A. classify
+    for (int t = threadIdx.x; t < PROBE_TILE; t += blockDim.x) {
+      const uint64_t i = t0 + (uint64_t)t;
+      if (i >= n) break;
+      const uint64_t d = a.qdesc[i];
+      const uint32_t key = a.qkey[i];
+      const uint64_t b = mphf_lookup(a.v, key);
+      if (b < a.n_keys && a.bucket_key[b] == key) {
+        const uint32_t l = atomicAdd(&sm.n_list, 1u);
+        sm.list_i[l] = (uint32_t)t;
+        sm.list_b[l] = (uint32_t)b;
+      } else {
+        tile_run(a, sm, d >> 24, (uint32_t)(d & 0xffffffu) + 1u, key);
+      }
+    }
+    __syncthreads();
+    // B. compare the listed superkmers with their buckets
+    const uint32_t nl = sm.n_list;
+    for (uint32_t l = threadIdx.x; l < nl; l += blockDim.x) {
+      const uint64_t i = t0 + sm.list_i[l];
+      const uint32_t b = sm.list_b[l];
+      const uint64_t d = a.qdesc[i];
+      const uint64_t s0 = d >> 24;
+      const uint32_t nw = (uint32_t)(d & 0xffffffu) + 1u;
+      const uint32_t key = a.qkey[i];
+      const uint32_t blo = a.bucket_off[b], bhi = a.bucket_off[b + 1];
+      int64_t run = -1;
+      for (uint32_t c0 = 0; c0 < nw; c0 += Q_CHUNK) {
+        const uint32_t cn = min((uint32_t)Q_CHUNK, nw - c0);
+        K q[Q_CHUNK];
+        {
+          R r;
+          roll_set<K, R>(r, a.qpacked, s0 + c0, k);
+          uint64_t p = s0 + c0 + (uint64_t)k;
 #pragma unroll
-        for (int t = 0; t < Q_CHUNK; t++) {
-          if (t < (int)cn) {
-            if (t > 0) { r.push(base_at(a.qpacked, p)); p++; }
-            q[t] = r.canon();
+          for (int t = 0; t < Q_CHUNK; t++) {
+            if (t < (int)cn) {
+              if (t > 0) { r.push(base_at(a.qpacked, p)); p++; }
+              q[t] = r.canon();
+            }
+          }
+        }
+        const uint32_t full = (cn == 32) ? 0xffffffffu : ((1u << cn) - 1u);
+        uint32_t found = 0;
+        for (uint32_t j = blo; j < bhi && found != full; j++) {
+          const uint64_t e = a.sk[j];
+          const uint64_t e0 = e >> 24;
+          const uint32_t en = (uint32_t)(e & 0xffffffu) + 1u;
+          R r;
+          roll_set<K, R>(r, a.ipacked, e0, k);
+          uint64_t p = e0 + (uint64_t)k;
+          for (uint32_t u = 0; u < en; u++) {
+            if (u > 0) { r.push(base_at(a.ipacked, p)); p++; }
+            const K ek = r.canon();
+#pragma unroll
+            for (int t = 0; t < Q_CHUNK; t++)
+              if (t < (int)cn && key_eq(q[t], ek)) found |= 1u << t;
+            if (found == full) break;
+          }
+        }
+        for (uint32_t t = 0; t < cn; t++) {
+          const bool absent = !((found >> t) & 1u);
+          if (absent) {
+            if (run < 0) run = (int64_t)(c0 + t);
+          } else if (run >= 0) {
+            tile_run(a, sm, s0 + (uint64_t)run, c0 + t - (uint32_t)run, key);
+            run = -1;
           }
         }
       }
-      const uint32_t full = (cn == 32) ? 0xffffffffu : ((1u << cn) - 1u);
-      uint32_t found = 0;
-      for (uint32_t j = blo; j < bhi && found != full; j++) {
-        const uint64_t e = a.sk[j];
-        const uint64_t e0 = e >> 24;
-        const uint32_t en = (uint32_t)(e & 0xffffffu) + 1u;
-        R r;
-        roll_set<K, R>(r, a.ipacked, e0, k);
-        uint64_t p = e0 + (uint64_t)k;
-        for (uint32_t u = 0; u < en; u++) {
-          if (u > 0) { r.push(base_at(a.ipacked, p)); p++; }
-          const K ek = r.canon();
-#pragma unroll
-          for (int t = 0; t < Q_CHUNK; t++)
-            if (t < (int)cn && key_eq(q[t], ek)) found |= 1u << t;
-          if (found == full) break;
-        }
-      }
-      for (uint32_t t = 0; t < cn; t++) {
-        const bool absent = !((found >> t) & 1u);
-        if (absent) {
-          if (run < 0) run = (int64_t)(c0 + t);
-        } else if (run >= 0) {
-          emit_run(a, s0 + (uint64_t)run, c0 + t - (uint32_t)run, key);
-          run = -1;
-        }
+      if (run >= 0) tile_run(a, sm, s0 + (uint64_t)run, nw - (uint32_t)run, key);
+    }
+    __syncthreads();
+    // C. the tile's buffered runs, in one piece
+    const uint32_t nr = min(sm.n_run, (uint32_t)PROBE_RUNS);
+    if (threadIdx.x == 0) {
+      sm.base = nr ? atomicAdd(a.n_runs, (unsigned long long)nr) : 0ull;
+      if (sm.w) atomicAdd(a.n_absent_windows, sm.w);
+    }
+    __syncthreads();
+    for (uint32_t r = threadIdx.x; r < nr; r += blockDim.x) {
+      const unsigned long long g = sm.base + r;
+      if (g < a.cap) {
+        a.out_desc[g] = sm.run_d[r];
+        a.out_key[g] = sm.run_k[r];
       }
     }
-    if (run >= 0) emit_run(a, s0 + (uint64_t)run, nw - (uint32_t)run, key);
+    __syncthreads();
   }
 }
 
@@ -1234,7 +1296,7 @@ int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, u
     pa.out_key = ctx->key2.as<uint32_t>();
     pa.n_runs = reinterpret_cast<unsigned long long*>(sc + SC_NRUNS);
     pa.cap = cap;
-    const int grid = grid_for(ctx, p.n_desc);
+    const int grid = std::max<int>(1, std::min<int>(ctx->sm_count * 4, (int)((p.n_desc + PROBE_TILE - 1) / PROBE_TILE)));
     if (z.k <= 32) k_zi_probe<K64, Roll64><<<grid, ZI_THREADS, 0, s>>>(pa);
     else k_zi_probe<K128, Roll128><<<grid, ZI_THREADS, 0, s>>>(pa);
     p.launches += 1;
