@@ -124,6 +124,8 @@ struct ZiIndex {
   DevBuf bucket_off;     // n_keys + 1 offsets into sk (u32)
   DevBuf bucket_key;     // the superkmer key (minimizer) of each bucket (u32)
   DevBuf bits, rank;     // MPHF bit vector (u64 words) and per-word rank (u32)
+  DevBuf mfilter;        // blocked Bloom filter of the minimizer keys (u64 words)
+  uint64_t mf_mask = 0;  // its words - 1 (a power of two)
   uint64_t n_keys = 0, n_sk = 0, n_words = 0;
   int levels = 0;
   uint64_t lvl_off[MPHF_MAX_LEVELS + 1] = {};

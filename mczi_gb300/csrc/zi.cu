@@ -47,6 +47,28 @@ constexpr int ZI_THREADS = 256;
 constexpr uint64_t MPHF_NOT_FOUND = ~0ull;
 constexpr int Q_CHUNK = 8;
 
+// Blocked Bloom filter over the index's minimizer keys: three bits of one
+// 64-bit word per key, about 32 bits per key.  Most minimizers of foreign
+// reads fail it with one load (usually from L2) instead of walking the MPHF
+// levels and the bucket's stored key, all random accesses.
+__host__ __device__ __forceinline__ uint64_t mfilter_hash(uint32_t key) {
+  uint64_t x = (uint64_t)key * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+  x ^= x >> 31;
+  x *= 0xBF58476D1CE4E5B9ull;
+  return x ^ (x >> 29);
+}
+__device__ __forceinline__ unsigned long long mfilter_bits(uint64_t h) {
+  return (1ull << (h & 63)) | (1ull << ((h >> 6) & 63)) | (1ull << ((h >> 12) & 63));
+}
+
+__global__ void k_zi_mfilter_set(const uint32_t* __restrict__ keys, uint64_t n, unsigned long long* filter,
+                                 uint64_t mask) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t h = mfilter_hash(keys[i]);
+    atomicOr(&filter[(h >> 32) & mask], mfilter_bits(h));
+  }
+}
+
 struct MphfView {
   const unsigned long long* bits;
   const uint32_t* rank;
@@ -174,6 +196,8 @@ struct ProbeArgs {
   unsigned long long* n_absent_windows;
   uint64_t cap;
   const uint32_t* bucket_key;
+  const unsigned long long* mfilter;
+  uint64_t mf_mask;
 };
 
 template <class K, class R>
@@ -189,8 +213,9 @@ __device__ __forceinline__ void roll_set(R& r, const uint32_t* packed, uint64_t 
 
 // The probe works in tiles of PROBE_TILE query superkmers per CTA.
 //   A. every thread classifies a share of the tile: a minimizer the index
-//      does not hold maps to an arbitrary bucket whose stored key differs, so
-//      every k-mer of that superkmer is absent (equal canonical k-mers have
+//      does not hold fails the minimizer filter (one load) or maps to an
+//      arbitrary bucket whose stored key differs, so every k-mer of that
+//      superkmer is absent (equal canonical k-mers have
 //      equal minimizers) and the whole superkmer is one absent run, emitted
 //      without rolling it; the others go to the tile's list with their bucket;
 //   B. the threads compare the listed superkmers with their buckets, so all
@@ -245,7 +270,9 @@ __global__ void __launch_bounds__(ZI_THREADS) k_zi_probe(ProbeArgs a) {
       if (i >= n) break;
       const uint64_t d = a.qdesc[i];
       const uint32_t key = a.qkey[i];
-      const uint64_t b = mphf_lookup(a.v, key);
+      const uint64_t h = mfilter_hash(key);
+      const unsigned long long fb = mfilter_bits(h);
+      const uint64_t b = (a.mfilter[(h >> 32) & a.mf_mask] & fb) == fb ? mphf_lookup(a.v, key) : MPHF_NOT_FOUND;
       if (b < a.n_keys && a.bucket_key[b] == key) {
         const uint32_t l = atomicAdd(&sm.n_list, 1u);
         sm.list_i[l] = (uint32_t)t;
@@ -1014,6 +1041,18 @@ int32_t zi_build(mczi_ctx* ctx, const uint8_t* fasta, uint64_t len, uint32_t k, 
   if (h[1]) return fail(ctx, MCZI_ERR_DEVICE, "ZI key set overflow");
   const uint64_t n_keys = h[0];
   z.n_keys = n_keys;
+  // the minimizer filter: a power of two of 64-bit words, >= n_keys / 2
+  {
+    uint64_t words = 1024;
+    while (words * 2 < n_keys) words <<= 1;
+    CKA(z.mfilter, words * 8);
+    CK(cudaMemsetAsync(z.mfilter.p, 0, words * 8, s));
+    z.mf_mask = words - 1;
+    if (n_keys)
+      k_zi_mfilter_set<<<grid_for(ctx, n_keys), ZI_THREADS, 0, s>>>(keys_a, n_keys,
+                                                                     z.mfilter.as<unsigned long long>(), z.mf_mask);
+    CK(cudaGetLastError());
+  }
   // BBHash levels, gamma = 2
   const uint64_t max_bits = 4 * n_keys + 128ull * MPHF_MAX_LEVELS + 64;
   const uint64_t max_words = max_bits / 64 + 1;
@@ -1288,6 +1327,8 @@ int32_t zi_query(mczi_ctx* ctx, const mczi_input* q, size_t n, bool per_input, u
     pa.sk = z.sk.as<uint64_t>();
     pa.bucket_off = z.bucket_off.as<uint32_t>();
     pa.bucket_key = z.bucket_key.as<uint32_t>();
+    pa.mfilter = z.mfilter.as<unsigned long long>();
+    pa.mf_mask = z.mf_mask;
     pa.n_absent_windows = reinterpret_cast<unsigned long long*>(sc + SC_NABSW);
     pa.n_keys = z.n_keys;
     pa.v = view_of(z);
