@@ -77,6 +77,9 @@ extern "C" {
                                            cfg: *const mczi_counter_config, output_path: *const c_char) -> i32;
     pub fn mczi_count_datasets_to_fasta_path(ctx: *mut mczi_ctx, inputs: *const *const c_char, n_inputs: usize,
                                              cfg: *const mczi_counter_config, output_path: *const c_char) -> i32;
+    pub fn mczi_route_superkmers(ctx: *mut mczi_ctx, cfg: *const mczi_counter_config, inputs: *const mczi_input,
+                                 n_inputs: usize, n_dest: u32, dest_bytes: *mut u64) -> i32;
+    pub fn mczi_route_copy(ctx: *mut mczi_ctx, dest: u32, out: *mut u8, cap: u64) -> i32;
     pub fn mczi_phase_times(ctx: *mut mczi_ctx, ms: *mut f32, cap: i32) -> i32;
     pub fn mczi_run_stats(ctx: *mut mczi_ctx, out: *mut u64, cap: i32) -> i32;
     pub fn mczi_set_count_tuning(ctx: *mut mczi_ctx, threads: i32, table_slots: i32, ctas_per_sm: i32) -> i32;

@@ -126,6 +126,21 @@ int32_t mczi_count_datasets_to_kff_path(mczi_ctx* ctx, const char* const* inputs
 int32_t mczi_count_datasets_to_fasta_path(mczi_ctx* ctx, const char* const* inputs, size_t n_inputs,
                                           const mczi_counter_config* cfg, const char* output_path);
 
+/* The local step of counting on several GPUs (the reference's counterpart
+ * is its partition files: src/lib.rs:4821-4925 writes each superkmer to
+ * partition_NNNN.skm by minimizer, src/lib.rs:2803-2845).  Packs and scans
+ * this GPU's share of the reads and groups every superkmer by destination
+ * GPU d = (minimizer bucket) mod n_dest, n_dest <= 1024, as one-line FASTA
+ * records of its windows + k - 1 bases; dest_bytes[d] receives each group's
+ * size.  The groups stay in the context until the next routing and are
+ * copied out with mczi_route_copy.  Each GPU then counts the records it
+ * received (mczi_count): every k-mer occurrence lies in exactly one
+ * superkmer and a canonical k-mer's superkmers share one minimizer, so the
+ * union of the GPUs' results equals one GPU's result on all the reads. */
+int32_t mczi_route_superkmers(mczi_ctx* ctx, const mczi_counter_config* cfg, const mczi_input* inputs,
+                              size_t n_inputs, uint32_t n_dest, uint64_t* dest_bytes);
+int32_t mczi_route_copy(mczi_ctx* ctx, uint32_t dest, uint8_t* out, uint64_t cap);
+
 /* Per-phase device times (ms) of the last run, measured with CUDA events on
  * the context's stream: [0] pack, [1] minimizer scan, [2] partition,
  * [3] k-mer counting, [4] minimizer pre-count (0 when not run).  After a

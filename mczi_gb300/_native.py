@@ -65,6 +65,9 @@ SIGNATURES = [
     ("mczi_result_digest", C.c_int32, [C.c_void_p, C.c_int32, C.POINTER(C.c_uint64)]),
     ("mczi_result_write_kff", C.c_int32, [C.c_void_p, C.c_char_p]),
     ("mczi_result_write_fasta", C.c_int32, [C.c_void_p, C.c_char_p]),
+    ("mczi_route_superkmers", C.c_int32, [C.c_void_p, C.POINTER(CounterConfigC), C.POINTER(InputC), C.c_size_t,
+                                          C.c_uint32, C.POINTER(C.c_uint64)]),
+    ("mczi_route_copy", C.c_int32, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64]),
     ("mczi_count_inputs_to_kff_path", C.c_int32, [C.c_void_p, C.POINTER(C.c_char_p), C.c_size_t,
                                                   C.POINTER(CounterConfigC), C.c_char_p]),
     ("mczi_count_inputs_to_fasta_path", C.c_int32, [C.c_void_p, C.POINTER(C.c_char_p), C.c_size_t,

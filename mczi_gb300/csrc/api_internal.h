@@ -172,6 +172,7 @@ struct mczi_ctx {
   mczi::DevBuf cnt64;  // counts widened to u64 for direct copies to the caller
   mczi::DevBuf digest_acc;  // mczi_result_digest accumulators (3 u64)
   mczi::DevBuf count_scratch;  // per-CTA window words of fast filtered counting rounds
+  std::vector<std::vector<uint8_t>> route;  // mczi_route_superkmers: FASTA records per destination GPU
   mczi::DevBuf kff_dev;          // KFF records formatted on the device
   mczi::HostPinned kff_host;     // their host copy, written to the file as is
   mczi::DevBuf sx_keys, sx_tab, sx_rank, sx_ext;  // simplitig writer: sorted keys, key->rank table, extensions

@@ -1,0 +1,110 @@
+"""MC counting on several GPUs (mczi_gb300/exchange.py): the exchange plan
+on two gloo ranks on the CPU, and the record split.
+
+The GPU routing step (mczi_route_superkmers) is replaced here by a CPU
+stand-in with the property the plan relies on: every window goes to the rank
+chosen by a function of its canonical k-mer (the GPU routes whole superkmers
+by their minimizer bucket, which is such a function).  The per-rank count is
+the oracle's.  The union of the ranks' records must equal the oracle's
+single-rank result.  The real routing step is checked on one GPU in
+tests/test_mc_gpu.py::test_route_superkmers_union_equals_single.
+"""
+import os
+import socket
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+K, X = 15, 1
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _reads(seed=4, n=300):
+    rng = np.random.default_rng(seed)
+    g = rng.choice(np.frombuffer(b"ACGT", dtype=np.uint8), size=3000)
+    out = []
+    for i in range(n):
+        a = int(rng.integers(0, 2800))
+        s = g[a:a + int(rng.integers(20, 200))].copy()
+        if rng.random() < 0.5:
+            s = np.frombuffer(bytes(s)[::-1].translate(bytes.maketrans(b"ACGT", b"TGCA")), dtype=np.uint8).copy()
+        if rng.random() < 0.2:
+            s[int(rng.integers(0, s.size))] = ord("N")
+        out.append(b">r%d\n" % i + s.tobytes() + b"\n")
+    return b"".join(out)
+
+
+def cpu_route(share, world, k=K):
+    """Every window of the share as its own FASTA record, sent to the rank
+    hash(canonical k-mer) mod world."""
+    import oracle_ref
+    groups = [[] for _ in range(world)]
+    comp = {0: 3, 1: 2, 2: 1, 3: 0}
+    for buf in share:
+        codes, offs, _ = oracle_ref.fragments(bytes(buf), k)
+        for f in range(len(offs) - 1):
+            seq = codes[int(offs[f]):int(offs[f + 1])]
+            for i in range(seq.size - k + 1):
+                w = seq[i:i + k]
+                fwd = int("".join("%d" % c for c in w), 4)
+                rev = int("".join("%d" % comp[int(c)] for c in w[::-1]), 4)
+                dest = (min(fwd, rev) * 0x9E3779B97F4A7C15 >> 17) % world
+                groups[dest].append(b">\n" + bytes(b"ACGT"[int(c)] for c in w) + b"\n")
+    return [np.frombuffer(b"".join(g), dtype=np.uint8) for g in groups]
+
+
+def _rank_main(rank: int, world: int, port: int, out_dir: str) -> None:
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    sys.path.insert(0, str(ROOT))
+    sys.path.insert(0, str(ROOT / "tests"))
+    import torch.distributed as dist
+    import oracle_ref
+    from mczi_gb300 import exchange
+    from mczi_gb300.mc import CounterConfig
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    data = _reads()
+    share = [exchange.split_records(data, world)[rank]]
+    lo, hi, cnt = exchange.count_sharded(
+        share, CounterConfig(K, 7, X), route=cpu_route,
+        count=lambda received: (lambda r: (r[0], None, r[2]))(oracle_ref.count(received, K, X)))
+    got = exchange.gather_records(lo, hi, cnt)
+    if rank == 0:
+        np.save(Path(out_dir, "lo.npy"), got[0])
+        np.save(Path(out_dir, "cnt.npy"), got[2])
+    Path(out_dir, f"n{rank}").write_text(str(lo.size))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_exchange_plan_two_gloo_ranks(tmp_path, oracle):
+    torch = pytest.importorskip("torch")
+    world, port = 2, _free_port()
+    torch.multiprocessing.start_processes(_rank_main, args=(world, port, str(tmp_path)), nprocs=world,
+                                          start_method="spawn")
+    lo, hi, cnt = oracle.count([_reads()], K, X)
+    assert np.array_equal(np.load(tmp_path / "lo.npy"), lo)
+    assert np.array_equal(np.load(tmp_path / "cnt.npy"), cnt)
+    # both ranks counted a share of the k-mers (a disjoint split)
+    n = [int((tmp_path / f"n{r}").read_text()) for r in range(world)]
+    assert all(v > 0 for v in n) and sum(n) == lo.size
+
+
+def test_split_records_cuts_at_record_starts():
+    from mczi_gb300 import exchange
+    fa = _reads(7, 50)
+    for parts in (1, 2, 3, 7, 60):
+        sl = exchange.split_records(fa, parts)
+        assert len(sl) == parts and b"".join(bytes(s) for s in sl) == fa
+        assert all(s.size == 0 or s[0] == ord(">") for s in sl)
+    fq = b"".join(b"@q%d\nACGTACGT\n+\nIIIIIIII\n" % i for i in range(40))
+    sl = exchange.split_records(fq, 4)
+    assert b"".join(bytes(s) for s in sl) == fq
+    assert all(s.size == 0 or (s[0] == ord("@") and bytes(s).count(b"\n") % 4 == 0) for s in sl)

@@ -462,3 +462,34 @@ def test_simplitig_fasta_byte_identical(gpu_ctx, oracle, tmp_path, k, m, x):
     q = tmp_path / "o.fa"
     oracle.write_simplitigs(q, lo, hi, k)
     assert p.read_bytes() == q.read_bytes()
+
+
+def test_route_superkmers_union_equals_single(gpu_ctx, oracle):
+    """The multi-GPU plan's local step (mczi_route_superkmers) on one GPU: the
+    reads split in three shares, each share routed to three destinations,
+    every destination counts what it received; the union of the three
+    results equals the single count and the oracle, record for record."""
+    from mczi_gb300 import exchange, gen
+    from mczi_gb300.mc import CounterConfig
+    for k, m, x, buf in ((31, 21, 1, gen.c1_reads(scale=0.004)), (63, 21, 2, gen.c2_reads(0.001))):
+        world = 3
+        cfg = CounterConfig(k, m, x)
+        received = [[] for _ in range(world)]
+        for share in exchange.split_records(buf, world):
+            for d, g in enumerate(exchange.route_superkmers(gpu_ctx, [share], cfg, world)):
+                if g.size:
+                    received[d].append(g)
+        parts = []
+        for d in range(world):
+            assert received[d], d  # every destination gets superkmers
+            n = gpu_ctx.count(received[d], cfg)
+            r = gpu_ctx.records(n, sorted=True)
+            parts.append((r.lo, r.hi if r.hi is not None else np.zeros_like(r.lo), r.count))
+        lo = np.concatenate([p[0] for p in parts])
+        hi = np.concatenate([p[1] for p in parts])
+        cnt = np.concatenate([p[2] for p in parts])
+        order = np.lexsort((lo, hi))
+        olo, ohi, ocnt = oracle.count([buf], k, x)
+        assert np.array_equal(lo[order], olo) and np.array_equal(cnt[order], ocnt), k
+        if k > 32:
+            assert np.array_equal(hi[order], ohi)
