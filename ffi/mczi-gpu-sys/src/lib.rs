@@ -96,6 +96,7 @@ extern "C" {
     // ---------------------------------------------------------------- ZI
     pub fn mczi_zi_build(ctx: *mut mczi_ctx, index_fasta: *const u8, len: u64, k: u32, m: u32) -> i32;
     pub fn mczi_zi_query(ctx: *mut mczi_ctx, queries: *const mczi_input, n: usize, n_absent: *mut u64) -> i32;
+    pub fn mczi_zi_build_from_result(ctx: *mut mczi_ctx, m: u32) -> i32;
     pub fn mczi_zi_build_path(ctx: *mut mczi_ctx, index_path: *const c_char, k: u32, m: u32) -> i32;
     pub fn mczi_zi_query_paths(ctx: *mut mczi_ctx, query_paths: *const *const c_char, n: usize,
                                n_absent: *mut u64) -> i32;

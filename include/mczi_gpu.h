@@ -234,6 +234,14 @@ int32_t mczi_zi_build(mczi_ctx* ctx, const uint8_t* index_fasta, uint64_t len, u
  * writes them as simplitigs like write_novel_simplitigs (src/zi.rs:177-189). */
 int32_t mczi_zi_query(mczi_ctx* ctx, const mczi_input* queries, size_t n, uint64_t* n_absent);
 
+/* The dictionary of the last count's kept k-mers, built on the device
+ * without leaving it (MCZI's orchestration, src/mczi.rs:340-360, writes MC's
+ * k-mers to FASTA, compacts them with GGCAT and indexes the simplitigs; the
+ * k-mer set is the same).  Each kept k-mer becomes its own index sequence;
+ * k is the count's, odd in [3, 63], and 0 < m < k (validate_k,
+ * src/zi.rs:103-107).  The count's result and staged inputs are consumed. */
+int32_t mczi_zi_build_from_result(mczi_ctx* ctx, uint32_t m);
+
 /* Path-based forms of the two ZI seams (build_dictionary src/zi.rs:114 and
  * collect_query_kmers_absent_from_index src/zi.rs:152, whose callers pass
  * paths, src/zi.rs:85-96): the files are plain or gzip / xz / zstd

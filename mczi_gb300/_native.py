@@ -90,6 +90,7 @@ SIGNATURES = [
     ("mczi_debug_set_bucket_window_limit", C.c_int32, [C.c_void_p, C.c_uint64]),
     ("mczi_zi_build", C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32]),
     ("mczi_zi_query", C.c_int32, [C.c_void_p, C.POINTER(InputC), C.c_size_t, C.POINTER(C.c_uint64)]),
+    ("mczi_zi_build_from_result", C.c_int32, [C.c_void_p, C.c_uint32]),
     ("mczi_zi_build_path", C.c_int32, [C.c_void_p, C.c_char_p, C.c_uint32, C.c_uint32]),
     ("mczi_zi_query_paths", C.c_int32, [C.c_void_p, C.POINTER(C.c_char_p), C.c_size_t, C.POINTER(C.c_uint64)]),
     ("mczi_read_input_file", C.c_int32, [C.c_char_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_char_p,

@@ -987,6 +987,38 @@ int32_t zi_validate(mczi_ctx* ctx, uint32_t k, uint32_t m) {
   return MCZI_OK;
 }
 
+int32_t zi_build_stream(mczi_ctx* ctx, Pipe& p, uint64_t nb, uint32_t k, uint32_t m, cudaEvent_t e0,
+                        cudaEvent_t e1);
+
+// k-mer records -> a 2-bit stream in which each k-mer is its own fragment
+// (base b of the stream is base b mod k of k-mer b / k): one thread per
+// packed word and per fragment-bit word, no atomics
+__global__ void k_kmers_to_stream(const uint64_t* __restrict__ lo, const uint64_t* __restrict__ hi, uint64_t n,
+                                  int k, uint32_t* __restrict__ packed, uint64_t pwords, uint32_t* __restrict__ fbits,
+                                  uint64_t fwords) {
+  const uint64_t nb = n * (uint64_t)k;
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < pwords; w += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t word = 0;
+    for (uint32_t q = 0; q < 16; q++) {
+      const uint64_t b = w * 16 + q;
+      if (b >= nb) break;
+      const uint64_t i = b / (uint64_t)k;
+      const int sh = 2 * (k - 1 - (int)(b - i * (uint64_t)k));  // bit offset of the base in the k-mer value
+      const uint64_t code = sh >= 64 ? (hi[i] >> (sh - 64)) & 3u : (lo[i] >> sh) & 3u;
+      word |= (uint32_t)code << (30 - 2 * q);
+    }
+    packed[w] = word;
+  }
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < fwords; w += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t word = 0;
+    const uint64_t b0 = w * 32;
+    // the first fragment start at or after b0
+    uint64_t b = ((b0 + (uint64_t)k - 1) / (uint64_t)k) * (uint64_t)k;
+    for (; b < b0 + 32 && b < nb; b += (uint64_t)k) word |= 1u << (b - b0);
+    fbits[w] = word;
+  }
+}
+
 int32_t zi_build(mczi_ctx* ctx, const uint8_t* fasta, uint64_t len, uint32_t k, uint32_t m) {
   int32_t rc = zi_validate(ctx, k, m);
   if (rc) return rc;
@@ -1007,6 +1039,17 @@ int32_t zi_build(mczi_ctx* ctx, const uint8_t* fasta, uint64_t len, uint32_t k, 
   CK(cudaStreamSynchronize(s));
   if (nb == 0)  // src/zi.rs:116-120
     return fail(ctx, MCZI_ERR_INVALID_CONFIG, "index FASTA did not contain any sequence of length >= k");
+  return zi_build_stream(ctx, p, nb, k, m, e0, e1);
+}
+
+// The dictionary of the 2-bit stream in ctx->packed / ctx->fbits (nb bases;
+// p.d_nbases on the device): superkmers, minimizer keys and filter, MPHF,
+// buckets.  e0 was recorded at the start of the build.
+int32_t zi_build_stream(mczi_ctx* ctx, Pipe& p, uint64_t nb, uint32_t k, uint32_t m, cudaEvent_t e0,
+                        cudaEvent_t e1) {
+  ZiIndex& z = ctx->zi;
+  cudaStream_t s = ctx->stream;
+  int32_t rc;
   if ((rc = pipe_scan(ctx, p, (int)k, (int)m))) return rc;
   const uint64_t n_desc = p.n_desc;
   uint64_t* sc = ctx->scalars.as<uint64_t>();
@@ -1392,6 +1435,46 @@ int32_t mczi_zi_query(mczi_ctx* ctx, const mczi_input* queries, size_t n, uint64
   if (!ctx) return MCZI_ERR_STATE;
   cudaSetDevice(ctx->device);
   return zi_query(ctx, queries, n, false, n_absent);
+}
+
+int32_t mczi_zi_build_from_result(mczi_ctx* ctx, uint32_t m) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (!ctx->have_result) return fail(ctx, MCZI_ERR_STATE, "no result");
+  const uint32_t k = (uint32_t)ctx->k;
+  int32_t rc = zi_validate(ctx, k, m);
+  if (rc) return rc;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  const uint64_t n = ctx->n_out, nb = n * (uint64_t)k;
+  if (n == 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "index FASTA did not contain any sequence of length >= k");
+  ZiIndex& z = ctx->zi;
+  z.built = false;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, s));
+  // the result's k-mers become the stream the dictionary is built from (the
+  // staged inputs are replaced)
+  const uint64_t pwords = nb / 16 + 8, fwords = nb / 32 + 8;
+  CKA(ctx->packed, pwords * 4);
+  CKA(ctx->fbits, fwords * 4);
+  CKA(ctx->input_base, 16);
+  const unsigned grid = (unsigned)std::min<uint64_t>((pwords + ZI_THREADS - 1) / ZI_THREADS, (uint64_t)ctx->sm_count * 16);
+  k_kmers_to_stream<<<grid, ZI_THREADS, 0, s>>>(ctx->out_lo.as<uint64_t>(), k > 32 ? ctx->out_hi.as<uint64_t>() : nullptr,
+                                                n, (int)k, ctx->packed.as<uint32_t>(), pwords, ctx->fbits.as<uint32_t>(),
+                                                fwords);
+  CK(cudaGetLastError());
+  uint64_t* d_nb = ctx->input_base.as<uint64_t>();
+  CK(cudaMemcpyAsync(d_nb, &nb, 8, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  ctx->staged = false;
+  ctx->text_len = nb;
+  ctx->have_result = false;
+  Pipe p;
+  p.d_nbases = d_nb;
+  p.n_bases_host = nb;
+  p.pwords = pwords;
+  return zi_build_stream(ctx, p, nb, k, m, e0, e1);
 }
 
 int32_t mczi_zi_build_path(mczi_ctx* ctx, const char* index_path, uint32_t k, uint32_t m) {

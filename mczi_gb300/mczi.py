@@ -14,7 +14,6 @@ tiling into simplitigs differs), the R reformer and the "regular" output mode.
 from __future__ import annotations
 
 import os
-import tempfile
 from dataclasses import dataclass
 from pathlib import Path
 from typing import Sequence
@@ -105,11 +104,10 @@ def run(index_inputs: Sequence, query_inputs: Sequence, k: int, m: int, x: int =
     ctx.validate(cfg)
     data = [mc.read_input(p) if not isinstance(p, (bytes, bytearray, memoryview)) else p for p in index_inputs]
     n_index = ctx.count(data, cfg)
-    # 2. the kept k-mers as simplitigs -> the dictionary (resident on the device)
-    with tempfile.TemporaryDirectory(prefix="mczi-") as tmp:
-        fa = Path(tmp) / "index_simplitigs.fa"
-        ctx.write_fasta(fa)
-        zi.build_dictionary(fa.read_bytes(), k, m, ctx)
+    # 2. the kept k-mers -> the dictionary, built where they are (on the device)
+    if n_index == 0:
+        raise N.MCZIError(N.MCZI_ERR_INVALID_CONFIG, "index FASTA did not contain any sequence of length >= k")
+    zi.build_dictionary_from_result(ctx, m)
     # 3. the subtraction, per output job
     absent = []
     for job in jobs:

@@ -52,6 +52,18 @@ def build_dictionary(index, k: int, m: int | None = None, ctx: Context | None = 
     return ctx
 
 
+def build_dictionary_from_result(ctx: Context, m: int | None = None) -> Context:
+    """Builds the device dictionary from the context's last count (its kept
+    k-mers), without moving them off the device."""
+    k = ctx.k
+    validate_k(k)
+    m = default_minimizer_size(k) if m is None else m
+    if not 0 < m < k:
+        raise N.MCZIError(N.MCZI_ERR_INVALID_CONFIG, "minimizer size must be > 0 and < k")
+    ctx._ck(ctx._lib.mczi_zi_build_from_result(ctx.handle, m))
+    return ctx
+
+
 def query(ctx: Context, queries: Sequence) -> int:
     """Runs the subtraction; the absent set stays on the device as the
     context's result.  Returns its size."""

@@ -207,3 +207,23 @@ def test_serving_wide_keys_and_empty_requests(gpu_ctx, oracle):
     for r, x in zip(reqs, got):
         want = oracle_absent(oracle, index, [r], 45) if r.startswith(b">") else []
         assert sorted((int(h) << 64) | int(l) for l, h in x) == want
+
+
+def test_dictionary_from_count_result(gpu_ctx, oracle):
+    """The MCZI index built on the device from a count's kept k-mers answers
+    as ZI over those k-mers (each kept k-mer an index sequence), for k <= 32
+    and k > 32."""
+    from mczi_gb300 import zi
+    from mczi_gb300.mc import CounterConfig, decode_kmer
+    rng = np.random.default_rng(8)
+    g = rand_seq(rng, 30000)
+    idx_reads = reads(rng, g, 600, 150, 0.005)
+    q = reads(rng, g, 200, 150, 0.01) + reads(rng, rand_seq(rng, 5000), 50, 150, 0.0)
+    for k, m in ((31, 19), (45, 21)):
+        n = gpu_ctx.count([idx_reads], CounterConfig(k, m, 1))
+        r = gpu_ctx.records(n, sorted=True)
+        hi = r.hi if r.hi is not None else np.zeros_like(r.lo)
+        kept = b"".join(b">\n" + decode_kmer((int(h) << 64) | int(l), k) + b"\n" for l, h in zip(r.lo, hi))
+        zi.build_dictionary_from_result(gpu_ctx, m)
+        got = zi.collect_query_kmers_absent_from_index(gpu_ctx, [q]).encoded()
+        assert got == oracle_absent(oracle, kept, [q], k), k
