@@ -10,8 +10,12 @@ MCZI_TUNE_CACHE).
 
 Knobs: threads per counting CTA and CTAs per SM (block size and table size
 follow), target table fill, windows per work item, two-pass filtered rounds,
-and the pass-1 minimizer pre-count.  The scan tile (4096 windows) and the
-partition digits (12 + 11 bits) are compile-time constants.
+and the pass-1 minimizer pre-count.  The pack tile (8 KiB), the scan tile
+(4096 windows) and the partition digits (12 + 11 bits) size shared-memory
+arrays and unrolled loops, so they are compile-time constants; builds with
+other tiles measured no faster on GB300 (4 Gbp, k = 63: scan 12.04 ms at 4096
+windows, 12.84 at 2048; pack 7.41 ms at 8 KiB, 7.30 at 4 KiB, 7.92 at 16 KiB;
+identical results).
 """
 from __future__ import annotations
 
@@ -62,8 +66,8 @@ def cache_key(k: int, mode: int, threshold: int) -> str:
 
 def candidates(k: int, threshold: int) -> list[Tuning]:
     wide = k > 32
-    shapes = [(1024, 1), (512, 2), (768, 1)] if wide else [(512, 2), (1024, 1), (256, 4)]
-    fills = [0.4, 0.6]
+    shapes = [(512, 2), (1024, 1), (384, 2)] if wide else [(512, 2), (1024, 1), (256, 4)]
+    fills = [0.5, 0.6, 0.7]
     chunks = [4, 2] if wide else [2, 4]
     filters = [1, 0] if threshold >= 1 else [0]
     out = [DEFAULT]

@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   }
   const Cnt2 c{(uint32_t)__popc(starts | terms), (uint32_t)__popc(emitm)};
   Cnt2 tot;
-  const Cnt2 pre = block_exclusive_scan<Cnt2, Cnt2Op>(c, &tot, shc);
+  const Cnt2 pre = block_exclusive_scan<Cnt2, Cnt2Op, SCANK_THREADS>(c, &tot, shc);
   // sh_h is free from here on (all reads of it finished before the scan's barriers)
   {
     uint32_t e = pre.ev;

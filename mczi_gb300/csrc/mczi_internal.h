@@ -7,8 +7,19 @@
 namespace mczi {
 
 // ---------------------------------------------------------------- K1 packer
-constexpr int PACK_TILE = 8192;     // text bytes per CTA
-constexpr int PACK_THREADS = 256;  // 32 bytes per thread (128 x 64 measured no faster)
+// The tile sizes are compile-time constants (shared-memory arrays and unrolled
+// per-thread loops are sized by them); a build may override them with
+// -DMCZI_PACK_THREADS=n (32 text bytes per thread) and -DMCZI_SCAN_TILE=n
+// (<= 8192 windows, 16 per thread) to measure other sizes.  The defaults are the fastest of
+// those measured on GB300.
+#ifndef MCZI_PACK_THREADS
+#define MCZI_PACK_THREADS 256
+#endif
+#ifndef MCZI_SCAN_TILE
+#define MCZI_SCAN_TILE 4096
+#endif
+constexpr int PACK_THREADS = MCZI_PACK_THREADS;  // 32 bytes per thread
+constexpr int PACK_TILE = 32 * PACK_THREADS;      // text bytes per CTA
 constexpr int PACK_PER_THREAD = PACK_TILE / PACK_THREADS;
 
 struct LineSum {
@@ -49,8 +60,8 @@ constexpr int NP1 = 1 << P1_BITS;
 constexpr int NP2 = 1 << P2_BITS;
 
 // ---------------------------------------------------------------- K2 scan
-constexpr int SCAN_TILE = 4096;     // windows per CTA
-constexpr int SCANK_THREADS = 256;
+constexpr int SCAN_TILE = MCZI_SCAN_TILE;  // windows per CTA
+constexpr int SCANK_THREADS = SCAN_TILE / 16;  // one thread owns 16 windows
 
 struct ScanArgs {
   const uint32_t* packed;
