@@ -123,6 +123,7 @@ __device__ __forceinline__ bool claimed_test(const uint32_t* cmap, uint32_t cbit
 // of a window seen for the first time in pass 1, W16_REPEAT for a repeat, or
 // W16_DONE (outside the round's hash range, or past the end of its chunk)
 constexpr uint32_t W16_DONE = 0xffffu;
+constexpr uint32_t REP_LIST = 512;  // repeats a warp lists per round (more go through the records)
 constexpr uint32_t W16_REPEAT = 0xfffeu;
 
 // chunk reference of the scratch: round-relative descriptor index << 10 |
@@ -154,27 +155,12 @@ __device__ __forceinline__ void roll_at(R& roll, const uint32_t* __restrict__ pa
   }
 }
 
-// Passes 2 and 3 of a fast filtered round, over the nchunks chunk records
-// pass 1 left.  Pass 2 stores or counts every repeat (claim-or-count; the
-// claiming occurrence is implicit) and lists the first sights whose claimed
-// bits are set; pass 3, once every key is stored, counts each listed first
-// sight whose key is in the table.  A warp reads 32 consecutive records at a
-// time (the next 32 already in flight) and gathers the repeats into a
-// register queue (two entries per lane); whenever 32 are queued all lanes
-// look one up, so the rare lookups run with full warps instead of one or two
-// lanes each.  Only the looked-up windows' k-mers are re-extracted from the
-// packed stream.  Each warp keeps its own list, so no shared counter is
-// touched.
-template <class K, class R, int MODE>
-__device__ __forceinline__ void lookup_window(int sub, uint64_t pos, uint32_t dset,
-                                              const uint32_t* __restrict__ packed, int k, K* keys, uint32_t* cnt,
-                                              unsigned long long* msk, int W, uint32_t S, K EMPTY, uint32_t* s_over,
-                                              uint32_t* claimed) {
-  R roll;
-  roll_at<K, R>(roll, packed, pos, k);
-  const uint64_t hv = sym_hash(roll);
-  const K key = roll.canon();
-  uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
+// looks key up from its home slot s: sub 1 counts it when stored (keys are
+// final), sub 0 claims or counts it
+template <class K, int MODE>
+__device__ __forceinline__ void lookup_key(int sub, const K key, uint32_t s, uint32_t dset, K* keys, uint32_t* cnt,
+                                           unsigned long long* msk, int W, uint32_t S, K EMPTY, uint32_t* s_over,
+                                           uint32_t* claimed) {
   if (sub == 1) {
     // 2b: keys are final: plain loads, stop at EMPTY
     for (uint32_t probe = 0; probe < PROBE_LIMIT; probe++) {
@@ -211,14 +197,45 @@ __device__ __forceinline__ void lookup_window(int sub, uint64_t pos, uint32_t ds
   *s_over = 1;  // table far past its target fill: the round is split
 }
 
+// the window whose k-mer starts at base `pos`, re-extracted from the stream
+template <class K, class R, int MODE>
+__device__ __forceinline__ void lookup_window(int sub, uint64_t pos, uint32_t dset,
+                                              const uint32_t* __restrict__ packed, int k, K* keys, uint32_t* cnt,
+                                              unsigned long long* msk, int W, uint32_t S, K EMPTY, uint32_t* s_over,
+                                              uint32_t* claimed) {
+  R roll;
+  roll_at<K, R>(roll, packed, pos, k);
+  const uint64_t hv = sym_hash(roll);
+  const uint32_t s = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
+  lookup_key<K, MODE>(sub, roll.canon(), s, dset, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
+}
+
+// Passes 2 and 3 of a fast filtered round.  Pass 2 stores or counts every
+// repeat (claim-or-count; the claiming occurrence is implicit): first the
+// warp's own list of repeats that pass 1 appended with their keys (no
+// re-extraction), then the repeats whose list was full, found in the chunk
+// records; the same scan lists the first sights whose claimed bit is set.
+// Pass 3, once every key is stored, counts each listed first sight whose key
+// is in the table.  The scan reads 32 consecutive records at a time (the next
+// 32 already in flight) and gathers the record repeats into a register queue
+// (two entries per lane); whenever 32 are queued all lanes look one up, so
+// the rare lookups run with full warps instead of one or two lanes each.
+// Only windows looked up from the records are re-extracted from the packed
+// stream.  Each warp keeps its own lists, so no shared counter is touched.
 template <class K, class R, int MODE>
 __device__ __forceinline__ uint32_t fast_pass2(const uint2* words, const uint32_t* refs, uint32_t* list,
                                                uint32_t nchunks, const uint64_t* __restrict__ rdesc,
                                                const uint64_t* dsbase, int n_datasets,
+                                               const K* rl_keys, const uint32_t* rl_info, uint32_t nrep,
                                                const uint32_t* __restrict__ packed, int k, K* keys, uint32_t* cnt,
                                                unsigned long long* msk, int W, uint32_t S, const uint32_t* cmap,
                                                uint32_t cbits, K EMPTY, uint32_t* s_over, uint32_t* claimed) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  // the repeats pass 1 listed with their keys (slot | dataset << 16)
+  for (uint32_t i = (uint32_t)lane; i < nrep; i += 32) {
+    const uint32_t inf = rl_info[i];
+    lookup_key<K, MODE>(0, rl_keys[i], inf & 0xffffu, inf >> 16, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
+  }
   const uint32_t stride = (uint32_t)nw * 32u;
   uint64_t q0 = 0, q1 = 0;  // queued window positions: entries lane and 32 + lane
   uint32_t qn = 0;          // queued entries (warp-uniform)
@@ -376,13 +393,19 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
   uint32_t* cmap = bmap + bwords;
   // this CTA's per-window scratch of fast filtered rounds (L2-resident: a
   // round writes and re-reads only its own windows' words)
-  // layout per CTA (12 bytes per chunk of 4 windows, plus the lists):
-  // scr_chunks uint2 records of four 16-bit window words, scr_chunks u32
-  // chunk references (chunk_pos), then one first-sight list of scr_lcap u32
+  // layout per CTA: per warp a list of REP_LIST repeats (keys, then u32
+  // slot | dataset << 16), then 12 bytes per chunk of 4 windows (scr_chunks
+  // uint2 records of four 16-bit window words and scr_chunks u32 chunk
+  // references, see chunk_pos), then one first-sight list of scr_lcap u32
   // entries per warp (chunk << 2 | window)
-  uint32_t* scr = (filtered && a.win_scratch) ? a.win_scratch + (size_t)blockIdx.x * a.scratch_words : nullptr;
+  uint32_t* scr0 = (filtered && a.win_scratch) ? a.win_scratch + (size_t)blockIdx.x * a.scratch_words : nullptr;
   const uint32_t scr_nw = blockDim.x >> 5;
-  const uint32_t scr_chunks = (uint32_t)(((a.scratch_words - 4096ull * scr_nw) / 7) & ~3ull);
+  const uint64_t rl_words = (uint64_t)scr_nw * REP_LIST * (sizeof(K) / 4 + 1);
+  K* rl_keys = scr0 ? reinterpret_cast<K*>(scr0) + (size_t)(threadIdx.x >> 5) * REP_LIST : nullptr;
+  uint32_t* rl_info =
+      scr0 ? scr0 + (size_t)scr_nw * REP_LIST * (sizeof(K) / 4) + (size_t)(threadIdx.x >> 5) * REP_LIST : nullptr;
+  uint32_t* scr = scr0 && a.scratch_words > rl_words + 4096ull * scr_nw + 64 ? scr0 + rl_words : nullptr;
+  const uint32_t scr_chunks = scr ? (uint32_t)(((a.scratch_words - rl_words - 4096ull * scr_nw) / 7) & ~3ull) : 0u;
   const uint32_t scr_lcap = ((scr_chunks + 32u * scr_nw - 1) / (32u * scr_nw)) * 128u;
   uint2* scr_words = reinterpret_cast<uint2*>(scr);
   uint32_t* scr_refs = scr ? scr + (size_t)scr_chunks * 2 : nullptr;
@@ -611,6 +634,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
                           (round_windows + (uint64_t)(dhi - dlo) * 3) / 4 <= scr_chunks &&
                           dhi - dlo < (1u << 22);  // chunk references: 22-bit descriptor index
         uint32_t total = 0;
+        uint32_t rl_n = 0;  // repeats this warp appended to its list in pass 1 (warp-uniform)
         for (int ph = filtered ? 1 : 0; ph <= (filtered ? 2 : 0); ph++) {
           if (ph == 2 && fast) {
             // ---- passes 2 and 3 of a fast round, over its chunk records
@@ -619,8 +643,8 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
             uint32_t* list = scr_list + (size_t)(tid >> 5) * scr_lcap;
             const uint64_t* rdesc = a.desc + lo + dlo;
             const uint32_t ln = fast_pass2<K, R, MODE>(scr_words, scr_refs, list, nchunks, rdesc, dsbase,
-                                                       a.n_datasets, a.packed, k, keys, cnt, msk, W, S, cmap, cbits,
-                                                       EMPTY, &s_over, &claimed);
+                                                       a.n_datasets, rl_keys, rl_info, min(rl_n, REP_LIST), a.packed,
+                                                       k, keys, cnt, msk, W, S, cmap, cbits, EMPTY, &s_over, &claimed);
             __syncthreads();
             if (!s_over)
               fast_pass3<K, R, MODE>(scr_refs, list, ln, rdesc, dsbase, a.n_datasets, a.packed, k, keys, cnt, msk, W,
@@ -677,6 +701,76 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
               const int lo2 = jw + __popc(starts & (0xffffffffu >> (31 - lane)));
               const uint32_t cend = total;
               const uint32_t c = c0 + (uint32_t)lane;
+              if (ph == 1 && fast) {
+                // pass 1 of a fast round, in step for the whole warp (the
+                // repeats are appended to the warp's list with one ballot per
+                // window position): the windows' seen bits, a 16-bit word
+                // per window and a reference per chunk in the scratch
+                const bool has = c < cend;
+                uint32_t nwin = 0, w0 = 0, dset = 0, q = 0, word = 0;
+                uint64_t s0 = 0;
+                const uint32_t* wp = a.packed;
+                R roll;
+                if (has) {
+                  const uint64_t d2 = sh_desc[lo2];
+                  w0 = (c - sh_cpre[lo2]) * 4u;
+                  nwin = min(4u, bd_windows(d2) - w0);
+                  dset = MODE == 1 ? (uint32_t)sh_dset[lo2] : 0u;
+                  s0 = bd_start(d2) + w0;
+                  roll_at<K, R>(roll, a.packed, s0, k);
+                  const uint64_t p = s0 + (uint64_t)k;
+                  wp = a.packed + (p >> 4);
+                  q = (uint32_t)(p & 15);
+                  word = *wp << (2 * q);
+                }
+                uint32_t r0 = W16_DONE, r1 = W16_DONE, r2 = W16_DONE, r3 = W16_DONE;
+#pragma unroll
+                for (uint32_t jj = 0; jj < 4; jj++) {
+                  bool repeat = false;
+                  uint32_t v = W16_DONE, slot = 0;
+                  K key = EMPTY;
+                  if (jj < nwin) {
+                    if (jj > 0) {
+                      roll.push(word >> 30);
+                      word <<= 2;
+                      if (++q == 16) { q = 0; word = *++wp; }
+                    }
+                    const uint64_t hv = sym_hash(roll);
+                    const uint32_t hk = (uint32_t)(hv >> 32);
+                    if (full_range || (hk >= rr.hlo && hk <= rr.hhi)) {
+                      const uint32_t hb = key_code(hv);
+                      repeat = seen_test_set(bmap, bwords, hv);
+                      v = hb;
+                      if (repeat) {
+                        claimed_set(cmap, cbits, hb);
+                        key = roll.canon();
+                        slot = (uint32_t)(((hv & 0xffffffffull) * (uint64_t)S) >> 32);
+                        v = W16_REPEAT;
+                      }
+                    }
+                  }
+                  const unsigned bal = __ballot_sync(0xffffffffu, repeat);
+                  if (bal) {
+                    const uint32_t idx = rl_n + (uint32_t)__popc(bal & ((1u << lane) - 1u));
+                    if (repeat && idx < REP_LIST) {
+                      rl_keys[idx] = key;
+                      rl_info[idx] = slot | (dset << 16);
+                      v = W16_DONE;  // counted from the list in pass 2
+                    }
+                    rl_n += (uint32_t)__popc(bal);
+                  }
+                  if (jj == 0) r0 = v;
+                  else if (jj == 1) r1 = v;
+                  else if (jj == 2) r2 = v;
+                  else r3 = v;
+                }
+                if (has) {
+                  const uint32_t ci = cbase + c;
+                  scr_words[ci] = make_uint2(r0 | (r1 << 16), r2 | (r3 << 16));
+                  scr_refs[ci] = ((uint32_t)(bb - dlo + (uint64_t)lo2) << 10) | (w0 >> 2);
+                }
+                continue;
+              }
               if (c >= cend) continue;
               const uint64_t d2 = sh_desc[lo2];
               const uint32_t len = bd_windows(d2);
@@ -692,8 +786,6 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
               const uint32_t* wp = a.packed + (p >> 4);
               uint32_t q = (uint32_t)(p & 15);
               uint32_t word = *wp << (2 * q);
-              // pass 1 of a fast round: the chunk's words, stored at its end
-              uint32_t r0 = W16_DONE, r1 = W16_DONE, r2 = W16_DONE, r3 = W16_DONE;
               for (uint32_t j = w0; j < w1; j++) {
                 if (j > w0) {
                   roll.push(word >> 30);
@@ -729,17 +821,6 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
                 if (ph == 1) {
                   const bool repeat = seen_test_set(bmap, bwords, hv);
                   if (repeat) claimed_set(cmap, cbits, hb);  // stored below, or in pass 2
-                  if (fast) {
-                    // a fast round only records the window: its key code for a
-                    // first sight, W16_REPEAT for a repeat (stored by pass 2)
-                    const uint32_t v = repeat ? W16_REPEAT : hb;
-                    const uint32_t jj = j - w0;
-                    r0 = jj == 0 ? v : r0;
-                    r1 = jj == 1 ? v : r1;
-                    r2 = jj == 2 ? v : r2;
-                    r3 = jj == 3 ? v : r3;
-                    continue;
-                  }
                   if (!repeat) continue;  // first sight: not stored
                 }
                 const bool count_here = ph == 0;
@@ -777,11 +858,6 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
                   s = (s + 1 == S) ? 0u : s + 1;
                 }
                 if (!done) { s_over = 1; break; }
-              }
-              if (ph == 1 && fast) {
-                const uint32_t ci = cbase + c;
-                scr_words[ci] = make_uint2(r0 | (r1 << 16), r2 | (r3 << 16));
-                scr_refs[ci] = ((uint32_t)(bb - dlo + (uint64_t)lo2) << 10) | (w0 >> 2);
               }
             }
             __syncthreads();

@@ -225,7 +225,7 @@ int32_t pipe_pack(mczi_ctx* ctx, Pipe& p) {
 // Superkmers one pass may hold: the partition addresses them with 32-bit
 // positions.
 constexpr uint64_t PASS_MAX_DESC = 4000000000ull;  // < 2^32: the partition's 32-bit bucket counters hold a pass
-constexpr uint64_t COUNT_SCRATCH_WORDS = 1ull << 18;  // per counting CTA (1 MiB; a multiple of 4)
+constexpr uint64_t COUNT_SCRATCH_WORDS = 1ull << 19;  // per counting CTA (2 MiB; a multiple of 4)
 
 uint32_t key_range_passes(mczi_ctx* ctx, int k, int m, uint64_t bases) {
   if (ctx->key_passes > 0) return (uint32_t)ctx->key_passes;
