@@ -126,10 +126,17 @@ constexpr uint32_t W16_DONE = 0xffffu;
 constexpr uint32_t REP_LIST = 512;  // repeats a warp lists per round (more go through the records)
 constexpr uint32_t W16_REPEAT = 0xfffeu;
 
+// fast rounds' chunks: FAST_CH windows, one 16-bit word each in a record
+constexpr uint32_t FAST_CH = COUNT_FAST_CHUNK;
+constexpr uint32_t FAST_LOG = FAST_CH == 8 ? 3u : 2u;
+struct __align__(2 * FAST_CH) ChunkWords {
+  uint32_t w[FAST_CH / 2];
+};
+
 // chunk reference of the scratch: round-relative descriptor index << 10 |
-// chunk within the descriptor (windows <= 4096, so < 1024 chunks of 4)
+// chunk within the descriptor (windows <= 4096, so < 1024 chunks)
 __device__ __forceinline__ uint64_t chunk_pos(uint32_t ref, const uint64_t* __restrict__ rdesc) {
-  return bd_start(rdesc[ref >> 10]) + (uint64_t)(ref & 1023u) * 4u;
+  return bd_start(rdesc[ref >> 10]) + (uint64_t)(ref & 1023u) * FAST_CH;
 }
 
 // dataset (input) of a base position: the largest i with dsbase[i] <= pos
@@ -210,6 +217,22 @@ __device__ __forceinline__ void lookup_window(int sub, uint64_t pos, uint32_t ds
   lookup_key<K, MODE>(sub, roll.canon(), s, dset, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
 }
 
+// exclusive prefix over the warp of a per-lane n < 2^NB, and the warp's
+// total, from one ballot per bit of n (no chain of shuffles)
+template <int NB>
+__device__ __forceinline__ uint32_t warp_prefix_small(uint32_t n, uint32_t* total) {
+  const uint32_t lt = (1u << (threadIdx.x & 31)) - 1u;
+  uint32_t ex = 0, tot = 0;
+#pragma unroll
+  for (int b = 0; b < NB; b++) {
+    const uint32_t bal = __ballot_sync(0xffffffffu, (n >> b) & 1u);
+    ex += (uint32_t)__popc(bal & lt) << b;
+    tot += (uint32_t)__popc(bal) << b;
+  }
+  *total = tot;
+  return ex;
+}
+
 // Passes 2 and 3 of a fast filtered round.  Pass 2 stores or counts every
 // repeat (claim-or-count; the claiming occurrence is implicit): first the
 // warp's own list of repeats that pass 1 appended with their keys (no
@@ -223,7 +246,7 @@ __device__ __forceinline__ void lookup_window(int sub, uint64_t pos, uint32_t ds
 // Only windows looked up from the records are re-extracted from the packed
 // stream.  Each warp keeps its own lists, so no shared counter is touched.
 template <class K, class R, int MODE>
-__device__ __forceinline__ uint32_t fast_pass2(const uint2* words, const uint32_t* refs, uint32_t* list,
+__device__ __forceinline__ uint32_t fast_pass2(const ChunkWords* words, const uint32_t* refs, uint32_t* list,
                                                uint32_t nchunks, const uint64_t* __restrict__ rdesc,
                                                const uint64_t* dsbase, int n_datasets,
                                                const K* rl_keys, const uint32_t* rl_info, uint32_t nrep,
@@ -241,7 +264,9 @@ __device__ __forceinline__ uint32_t fast_pass2(const uint2* words, const uint32_
   uint32_t qn = 0;          // queued entries (warp-uniform)
   uint32_t ln = 0;          // entries in this warp's first-sight list (warp-uniform)
   uint32_t g = (uint32_t)wid * 32u;
-  uint2 v = make_uint2(0xffffffffu, 0xffffffffu);
+  ChunkWords v;
+#pragma unroll
+  for (int i = 0; i < (int)FAST_CH / 2; i++) v.w[i] = 0xffffffffu;
   uint32_t ref = 0;
   if (g + (uint32_t)lane < nchunks) {
     v = words[g + lane];
@@ -249,41 +274,37 @@ __device__ __forceinline__ uint32_t fast_pass2(const uint2* words, const uint32_
   }
   for (; g < nchunks; g += stride) {
     // the next group's records, in flight while this one is processed
-    uint2 vn = make_uint2(0xffffffffu, 0xffffffffu);
+    ChunkWords vn;
+#pragma unroll
+    for (int i = 0; i < (int)FAST_CH / 2; i++) vn.w[i] = 0xffffffffu;
     uint32_t rn = 0;
     if (g + stride + (uint32_t)lane < nchunks) {
       vn = words[g + stride + lane];
       rn = refs[g + stride + lane];
     }
-    const uint32_t w[4] = {v.x & 0xffffu, v.x >> 16, v.y & 0xffffu, v.y >> 16};
     uint32_t m = 0, f = 0;  // repeats; listed first sights
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
-      m |= (w[j] == W16_REPEAT) ? (1u << j) : 0u;
-      f |= (w[j] < W16_REPEAT && claimed_test(cmap, cbits, w[j])) ? (1u << j) : 0u;
+    for (int j = 0; j < (int)FAST_CH; j++) {
+      const uint32_t wj = (v.w[j >> 1] >> (16 * (j & 1))) & 0xffffu;
+      m |= (wj == W16_REPEAT) ? (1u << j) : 0u;
+      f |= (wj < W16_REPEAT && claimed_test(cmap, cbits, wj)) ? (1u << j) : 0u;
     }
-    // first sights to the warp's list (slots from a warp scan)
+    // first sights to the warp's list
     {
-      const uint32_t n = __popc(f);
-      uint32_t incl = n;
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-      }
-      uint32_t at = ln + incl - n;
-      for (uint32_t ff = f; ff; ff &= ff - 1) list[at++] = ((g + (uint32_t)lane) << 2) | (uint32_t)(__ffs(ff) - 1);
-      ln += __shfl_sync(0xffffffffu, incl, 31);
+      uint32_t nf;
+      uint32_t at = ln + warp_prefix_small<FAST_LOG + 1>(__popc(f), &nf);
+      for (uint32_t ff = f; ff; ff &= ff - 1) list[at++] = ((g + (uint32_t)lane) << FAST_LOG) | (uint32_t)(__ffs(ff) - 1);
+      ln += nf;
     }
-    // repeats through the queue, 32 at a time
-    const uint64_t base = m ? chunk_pos(ref, rdesc) : 0ull;
-    const uint32_t n = __popc(m);
-    uint32_t incl = n;
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += y;
+    // repeats that found their warp's list full, through the queue 32 at a
+    // time (rare: most rounds have none)
+    uint32_t total = 0, excl = 0, incl = 0;
+    uint64_t base = 0;
+    if (__any_sync(0xffffffffu, m != 0)) {
+      base = m ? chunk_pos(ref, rdesc) : 0ull;
+      excl = warp_prefix_small<FAST_LOG + 1>(__popc(m), &total);
+      incl = excl + __popc(m);
     }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    const uint32_t excl = incl - n;
     for (uint32_t b0 = 0; b0 < total; b0 += 32) {
       const uint32_t t = b0 + (uint32_t)lane;
       // source lane of candidate t: the first lane whose inclusive count exceeds t
@@ -335,7 +356,7 @@ __device__ __forceinline__ void fast_pass3(const uint32_t* refs, const uint32_t*
   const int lane = threadIdx.x & 31;
   for (uint32_t i = (uint32_t)lane; i < ln; i += 32) {
     const uint32_t e = list[i];
-    const uint64_t pos = chunk_pos(refs[e >> 2], rdesc) + (e & 3u);
+    const uint64_t pos = chunk_pos(refs[e >> FAST_LOG], rdesc) + (e & (FAST_CH - 1));
     const uint32_t ds = MODE == 1 ? dataset_of(dsbase, n_datasets, pos) : 0u;
     lookup_window<K, R, MODE>(1, pos, ds, packed, k, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
   }
@@ -394,10 +415,10 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
   // this CTA's per-window scratch of fast filtered rounds (L2-resident: a
   // round writes and re-reads only its own windows' words)
   // layout per CTA: per warp a list of REP_LIST repeats (keys, then u32
-  // slot | dataset << 16), then 12 bytes per chunk of 4 windows (scr_chunks
-  // uint2 records of four 16-bit window words and scr_chunks u32 chunk
-  // references, see chunk_pos), then one first-sight list of scr_lcap u32
-  // entries per warp (chunk << 2 | window)
+  // slot | dataset << 16), then per chunk of FAST_CH windows a record of
+  // 16-bit window words (scr_chunks ChunkWords) and a u32 chunk reference
+  // (scr_chunks of them, see chunk_pos), then one first-sight list of
+  // scr_lcap u32 entries per warp (chunk << FAST_LOG | window)
   uint32_t* scr0 = (filtered && a.win_scratch) ? a.win_scratch + (size_t)blockIdx.x * a.scratch_words : nullptr;
   const uint32_t scr_nw = blockDim.x >> 5;
   const uint64_t rl_words = (uint64_t)scr_nw * REP_LIST * (sizeof(K) / 4 + 1);
@@ -405,11 +426,16 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
   uint32_t* rl_info =
       scr0 ? scr0 + (size_t)scr_nw * REP_LIST * (sizeof(K) / 4) + (size_t)(threadIdx.x >> 5) * REP_LIST : nullptr;
   uint32_t* scr = scr0 && a.scratch_words > rl_words + 4096ull * scr_nw + 64 ? scr0 + rl_words : nullptr;
-  const uint32_t scr_chunks = scr ? (uint32_t)(((a.scratch_words - rl_words - 4096ull * scr_nw) / 7) & ~3ull) : 0u;
-  const uint32_t scr_lcap = ((scr_chunks + 32u * scr_nw - 1) / (32u * scr_nw)) * 128u;
-  uint2* scr_words = reinterpret_cast<uint2*>(scr);
-  uint32_t* scr_refs = scr ? scr + (size_t)scr_chunks * 2 : nullptr;
-  uint32_t* scr_list = scr ? scr + (size_t)scr_chunks * 3 : nullptr;
+  // words per chunk: its record, its reference and FAST_CH list entries (the
+  // lists' rounding up to whole groups of 32 chunks per warp stays inside
+  // the 4096 words per warp kept apart)
+  constexpr uint32_t chunk_words = FAST_CH / 2 + 1 + FAST_CH;
+  const uint32_t scr_chunks =
+      scr ? (uint32_t)(((a.scratch_words - rl_words - 4096ull * scr_nw) / chunk_words) & ~3ull) : 0u;
+  const uint32_t scr_lcap = ((scr_chunks + 32u * scr_nw - 1) / (32u * scr_nw)) * 32u * FAST_CH;
+  ChunkWords* scr_words = reinterpret_cast<ChunkWords*>(scr);
+  uint32_t* scr_refs = scr ? scr + (size_t)scr_chunks * (FAST_CH / 2) : nullptr;
+  uint32_t* scr_list = scr ? scr + (size_t)scr_chunks * (FAST_CH / 2 + 1) : nullptr;
   off += (size_t)fwords * 4;
   off = (off + 15) & ~(size_t)15;
   uint32_t* occ = reinterpret_cast<uint32_t*>(smem + off);   // NP2 + 1, becomes occupancy prefix
@@ -630,8 +656,8 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
         const bool one_batch = dhi - dlo <= (uint64_t)nth;
         // chunks of the round <= (windows + descriptors * (chunk - 1)) / chunk
         const uint64_t round_windows = (uint64_t)(occ[rr.bh] - occ[rr.bl]);
-        const bool fast = scr != nullptr && chunk == 4 &&
-                          (round_windows + (uint64_t)(dhi - dlo) * 3) / 4 <= scr_chunks &&
+        const bool fast = scr != nullptr && chunk == FAST_CH &&
+                          (round_windows + (uint64_t)(dhi - dlo) * (FAST_CH - 1)) / FAST_CH <= scr_chunks &&
                           dhi - dlo < (1u << 22);  // chunk references: 22-bit descriptor index
         uint32_t total = 0;
         uint32_t rl_n = 0;  // repeats this warp appended to its list in pass 1 (warp-uniform)
@@ -713,8 +739,8 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
                 R roll;
                 if (has) {
                   const uint64_t d2 = sh_desc[lo2];
-                  w0 = (c - sh_cpre[lo2]) * 4u;
-                  nwin = min(4u, bd_windows(d2) - w0);
+                  w0 = (c - sh_cpre[lo2]) * FAST_CH;
+                  nwin = min(FAST_CH, bd_windows(d2) - w0);
                   dset = MODE == 1 ? (uint32_t)sh_dset[lo2] : 0u;
                   s0 = bd_start(d2) + w0;
                   roll_at<K, R>(roll, a.packed, s0, k);
@@ -723,9 +749,9 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
                   q = (uint32_t)(p & 15);
                   word = *wp << (2 * q);
                 }
-                uint32_t r0 = W16_DONE, r1 = W16_DONE, r2 = W16_DONE, r3 = W16_DONE;
+                uint32_t rw[FAST_CH / 2];  // the record's words, two windows each
 #pragma unroll
-                for (uint32_t jj = 0; jj < 4; jj++) {
+                for (uint32_t jj = 0; jj < FAST_CH; jj++) {
                   bool repeat = false;
                   uint32_t v = W16_DONE, slot = 0;
                   K key = EMPTY;
@@ -759,15 +785,16 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
                     }
                     rl_n += (uint32_t)__popc(bal);
                   }
-                  if (jj == 0) r0 = v;
-                  else if (jj == 1) r1 = v;
-                  else if (jj == 2) r2 = v;
-                  else r3 = v;
+                  if (jj & 1) rw[jj >> 1] |= v << 16;
+                  else rw[jj >> 1] = v;
                 }
                 if (has) {
                   const uint32_t ci = cbase + c;
-                  scr_words[ci] = make_uint2(r0 | (r1 << 16), r2 | (r3 << 16));
-                  scr_refs[ci] = ((uint32_t)(bb - dlo + (uint64_t)lo2) << 10) | (w0 >> 2);
+                  ChunkWords rec;
+#pragma unroll
+                  for (int i = 0; i < (int)FAST_CH / 2; i++) rec.w[i] = rw[i];
+                  scr_words[ci] = rec;
+                  scr_refs[ci] = ((uint32_t)(bb - dlo + (uint64_t)lo2) << 10) | (w0 >> FAST_LOG);
                 }
                 continue;
               }

@@ -468,7 +468,10 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       ca.ctas = ctx->sm_count * cps;
       ca.work_counter = reinterpret_cast<unsigned int*>(sc + SC_WORK);
       ca.fill = ctx->count_fill > 0.f ? ctx->count_fill : 0.6f;
-      ca.chunk = ctx->count_chunk > 0 ? (uint32_t)ctx->count_chunk : (wide ? 4u : 2u);
+      // default: the fast rounds' chunk for filtered k > 32 counts, else 4
+      // (k > 32) or 2 windows per work item
+      ca.chunk = ctx->count_chunk > 0 ? (uint32_t)ctx->count_chunk
+                                      : (wide ? (fwords > 0 ? COUNT_FAST_CHUNK : 4u) : 2u);
       ca.filter_words = fwords;
       ca.max_bucket_windows = ctx->max_bucket_windows ? ctx->max_bucket_windows : 0xffffffffull;
       // filtered rounds whose windows fit COUNT_SCRATCH_WORDS per CTA take the

@@ -157,7 +157,7 @@ struct CountArgs {
   int ctas;
   unsigned int* work_counter;
   float fill;                 // target fill of a round's table
-  uint32_t chunk;             // windows per work item in the insert phase
+  uint32_t chunk;             // windows per work item in the insert phase (COUNT_FAST_CHUNK for fast filtered rounds)
   uint32_t filter_words;      // > 0: two-pass rounds with a bitmap of this many u32 words (needs x >= 1)
   // k-mer windows one bucket may hold: the bin occupancies, their prefix and
   // the per-slot counts are 32-bit and each is bounded by the bucket's
@@ -168,6 +168,14 @@ struct CountArgs {
   uint32_t* win_scratch;
   uint64_t scratch_words;
 };
+// Windows per chunk of the counting kernel's fast filtered rounds (4 or 8;
+// a filtered count takes the fast rounds only with chunk equal to it).  A
+// build may override it with -DMCZI_COUNT_FAST_CHUNK=n to measure the other.
+#ifndef MCZI_COUNT_FAST_CHUNK
+#define MCZI_COUNT_FAST_CHUNK 4
+#endif
+constexpr uint32_t COUNT_FAST_CHUNK = MCZI_COUNT_FAST_CHUNK;
+static_assert(COUNT_FAST_CHUNK == 4 || COUNT_FAST_CHUNK == 8, "fast chunks hold 4 or 8 windows");
 void launch_count(const CountArgs& a, cudaStream_t s);
 size_t count_smem_bytes(int k, int mode, int n_datasets, uint32_t table_slots, uint32_t filter_words);
 size_t count_fixed_smem_bytes(int mode, int n_datasets);
