@@ -135,7 +135,7 @@ struct __align__(2 * FAST_CH) ChunkWords {
 
 // chunk reference of the scratch: round-relative descriptor index << 10 |
 // chunk within the descriptor (windows <= 4096, so < 1024 chunks)
-__device__ __forceinline__ uint64_t chunk_pos(uint32_t ref, const uint64_t* __restrict__ rdesc) {
+__device__ __forceinline__ uint64_t chunk_pos(uint32_t ref, const uint64_t* rdesc) {
   return bd_start(rdesc[ref >> 10]) + (uint64_t)(ref & 1023u) * FAST_CH;
 }
 
@@ -236,29 +236,38 @@ __device__ __forceinline__ uint32_t warp_prefix_small(uint32_t n, uint32_t* tota
 // Passes 2 and 3 of a fast filtered round.  Pass 2 stores or counts every
 // repeat (claim-or-count; the claiming occurrence is implicit): first the
 // warp's own list of repeats that pass 1 appended with their keys (no
-// re-extraction), then the repeats whose list was full, found in the chunk
-// records; the same scan lists the first sights whose claimed bit is set.
-// Pass 3, once every key is stored, counts each listed first sight whose key
-// is in the table.  The scan reads 32 consecutive records at a time (the next
-// 32 already in flight) and gathers the record repeats into a register queue
-// (two entries per lane); whenever 32 are queued all lanes look one up, so
-// the rare lookups run with full warps instead of one or two lanes each.
-// Only windows looked up from the records are re-extracted from the packed
-// stream.  Each warp keeps its own lists, so no shared counter is touched.
-template <class K, class R, int MODE>
-__device__ __forceinline__ uint32_t fast_pass2(const ChunkWords* words, const uint32_t* refs, uint32_t* list,
-                                               uint32_t nchunks, const uint64_t* __restrict__ rdesc,
-                                               const uint64_t* dsbase, int n_datasets,
-                                               const K* rl_keys, const uint32_t* rl_info, uint32_t nrep,
-                                               const uint32_t* __restrict__ packed, int k, K* keys, uint32_t* cnt,
-                                               unsigned long long* msk, int W, uint32_t S, const uint32_t* cmap,
-                                               uint32_t cbits, K EMPTY, uint32_t* s_over, uint32_t* claimed) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+// re-extraction, fast_claims), then the repeats whose list was full, found in
+// the chunk records (fast_scan); the same scan lists the first sights whose
+// claimed bit is set.  Pass 3 (fast_pass3), once every key is stored, counts
+// each listed first sight whose key is in the table.  The scan reads 32
+// consecutive records at a time (the next 32 already in flight) and gathers
+// the record repeats into a register queue (two entries per lane); whenever
+// 32 are queued all lanes look one up, so the rare lookups run with full
+// warps instead of one or two lanes each.  Only windows looked up from the
+// records are re-extracted from the packed stream.  Each warp keeps its own
+// lists, so no shared counter is touched.  (Looking the first sights up
+// inside the scan, when no list was full, measured slower: the lookups'
+// dependent loads stall the scan.  So did taking two list entries per lane
+// at a time.)
+template <class K, int MODE>
+__device__ __forceinline__ void fast_claims(const K* rl_keys, const uint32_t* rl_info, uint32_t nrep, K* keys,
+                                            uint32_t* cnt, unsigned long long* msk, int W, uint32_t S, K EMPTY,
+                                            uint32_t* s_over, uint32_t* claimed) {
   // the repeats pass 1 listed with their keys (slot | dataset << 16)
-  for (uint32_t i = (uint32_t)lane; i < nrep; i += 32) {
+  for (uint32_t i = (uint32_t)(threadIdx.x & 31); i < nrep; i += 32) {
     const uint32_t inf = rl_info[i];
     lookup_key<K, MODE>(0, rl_keys[i], inf & 0xffffu, inf >> 16, keys, cnt, msk, W, S, EMPTY, s_over, claimed);
   }
+}
+
+template <class K, class R, int MODE>
+__device__ __forceinline__ uint32_t fast_scan(const ChunkWords* words, const uint32_t* refs, uint32_t* list,
+                                              uint32_t nchunks, const uint64_t* rdesc, const uint64_t* dsbase,
+                                              int n_datasets, const uint32_t* __restrict__ packed, int k, K* keys,
+                                              uint32_t* cnt, unsigned long long* msk, int W, uint32_t S,
+                                              const uint32_t* cmap, uint32_t cbits, K EMPTY, uint32_t* s_over,
+                                              uint32_t* claimed) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const uint32_t stride = (uint32_t)nw * 32u;
   uint64_t q0 = 0, q1 = 0;  // queued window positions: entries lane and 32 + lane
   uint32_t qn = 0;          // queued entries (warp-uniform)
@@ -282,14 +291,14 @@ __device__ __forceinline__ uint32_t fast_pass2(const ChunkWords* words, const ui
       vn = words[g + stride + lane];
       rn = refs[g + stride + lane];
     }
-    uint32_t m = 0, f = 0;  // repeats; listed first sights
+    uint32_t m = 0, f = 0;  // record repeats; first sights whose claimed bit is set
 #pragma unroll
     for (int j = 0; j < (int)FAST_CH; j++) {
       const uint32_t wj = (v.w[j >> 1] >> (16 * (j & 1))) & 0xffffu;
       m |= (wj == W16_REPEAT) ? (1u << j) : 0u;
       f |= (wj < W16_REPEAT && claimed_test(cmap, cbits, wj)) ? (1u << j) : 0u;
     }
-    // first sights to the warp's list
+    // the first sights to the warp's list
     {
       uint32_t nf;
       uint32_t at = ln + warp_prefix_small<FAST_LOG + 1>(__popc(f), &nf);
@@ -349,7 +358,7 @@ __device__ __forceinline__ uint32_t fast_pass2(const ChunkWords* words, const ui
 // pass 3: this warp's listed first sights, 32 lookups at a time
 template <class K, class R, int MODE>
 __device__ __forceinline__ void fast_pass3(const uint32_t* refs, const uint32_t* list, uint32_t ln,
-                                           const uint64_t* __restrict__ rdesc, const uint64_t* dsbase,
+                                           const uint64_t* rdesc, const uint64_t* dsbase,
                                            int n_datasets, const uint32_t* __restrict__ packed, int k, K* keys,
                                            uint32_t* cnt, unsigned long long* msk, int W, uint32_t S, K EMPTY,
                                            uint32_t* s_over, uint32_t* claimed) {
@@ -646,7 +655,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
         //     or counts every repeat and lists the first sights whose claimed
         //     bit is set; pass 3 counts the listed first sights whose key is
         //     stored.  Only the looked-up windows' k-mers are re-extracted,
-        //     and the lookups run in full warps (fast_pass2).  Every
+        //     and the lookups run in full warps (fast_claims, fast_scan).  Every
         //     occurrence of a stored key is counted once: its claiming repeat
         //     implicitly, the other repeats in pass 2, the first sight in 3.
         //   - otherwise pass 1 claims the repeats and pass 2 re-rolls every
@@ -667,10 +676,13 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
             __syncthreads();
             const uint32_t nchunks = s_cbase;
             uint32_t* list = scr_list + (size_t)(tid >> 5) * scr_lcap;
-            const uint64_t* rdesc = a.desc + lo + dlo;
-            const uint32_t ln = fast_pass2<K, R, MODE>(scr_words, scr_refs, list, nchunks, rdesc, dsbase,
-                                                       a.n_datasets, rl_keys, rl_info, min(rl_n, REP_LIST), a.packed,
-                                                       k, keys, cnt, msk, W, S, cmap, cbits, EMPTY, &s_over, &claimed);
+            // a round of one batch still has its descriptors in shared memory
+            const uint64_t* rdesc = one_batch ? sh_desc : a.desc + lo + dlo;
+            fast_claims<K, MODE>(rl_keys, rl_info, min(rl_n, REP_LIST), keys, cnt, msk, W, S, EMPTY, &s_over,
+                                 &claimed);
+            const uint32_t ln = fast_scan<K, R, MODE>(scr_words, scr_refs, list, nchunks, rdesc, dsbase, a.n_datasets,
+                                                      a.packed, k, keys, cnt, msk, W, S, cmap, cbits, EMPTY, &s_over,
+                                                      &claimed);
             __syncthreads();
             if (!s_over)
               fast_pass3<K, R, MODE>(scr_refs, list, ln, rdesc, dsbase, a.n_datasets, a.packed, k, keys, cnt, msk, W,
@@ -922,42 +934,54 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
           __syncthreads();
           continue;
         }
-        // ---- emit slots with count > threshold
-        for (uint32_t base = 0; base < S; base += nth) {
-          const uint32_t s = base + tid;
-          bool emit = false;
-          uint32_t c = 0;
-          K key = EMPTY;
-          if (s < S) {
+        // ---- emit slots with count > threshold.  Each warp counts the
+        // emissions of its slots, reserves them with one atomic (whose
+        // latency is paid once per warp and round, not once per 32 slots),
+        // then writes them.
+        {
+          // the claiming occurrence is implicit except in slow filtered
+          // rounds, whose pass 2 counts every occurrence
+          const uint32_t implicit = (filtered && !fast) ? 0u : 1u;
+          auto slot_count = [&](uint32_t s, K& key, uint32_t& c) -> bool {
+            if (s >= S) return false;
             key = keys[s];
-            if (!key_eq(key, EMPTY)) {
-              // the claiming occurrence is implicit except in slow filtered
-              // rounds, whose pass 2 counts every occurrence
-              c = MODE == 0 ? cnt[s] + ((filtered && !fast) ? 0u : 1u) : popc_words(&msk[(size_t)s * W], W);
-              emit = (uint64_t)c > a.threshold;
-            }
+            if (key_eq(key, EMPTY)) return false;
+            c = MODE == 0 ? cnt[s] + implicit : popc_words(&msk[(size_t)s * W], W);
+            return (uint64_t)c > a.threshold;
+          };
+          uint32_t mine = 0;  // this warp's emissions (warp-uniform)
+          for (uint32_t base = 0; base < S; base += nth) {
+            K key;
+            uint32_t c;
+            mine += __popc(__ballot_sync(0xffffffffu, slot_count(base + tid, key, c)));
           }
-          const unsigned bal = __ballot_sync(0xffffffffu, emit);
-          if (bal) {
+          if (mine) {
             unsigned long long ob = 0;
-            const int leader = __ffs(bal) - 1;
-            if (lane == leader) ob = atomicAdd(a.n_out, (unsigned long long)__popc(bal));
-            ob = __shfl_sync(0xffffffffu, ob, leader);
-            if (emit) {
-              const unsigned long long idx = ob + __popc(bal & ((1u << lane) - 1u));
-              if (idx < a.out_cap) {
-                if constexpr (sizeof(K) == 8) {
-                  a.out_lo[idx] = reinterpret_cast<const K64&>(key).v;
+            if (lane == 0) ob = atomicAdd(a.n_out, (unsigned long long)mine);
+            ob = __shfl_sync(0xffffffffu, ob, 0);
+            for (uint32_t base = 0; base < S; base += nth) {
+              const uint32_t s = base + tid;
+              K key = EMPTY;
+              uint32_t c = 0;
+              const bool emit = slot_count(s, key, c);
+              const unsigned bal = __ballot_sync(0xffffffffu, emit);
+              if (emit) {
+                const unsigned long long idx = ob + __popc(bal & ((1u << lane) - 1u));
+                if (idx < a.out_cap) {
+                  if constexpr (sizeof(K) == 8) {
+                    a.out_lo[idx] = reinterpret_cast<const K64&>(key).v;
+                  } else {
+                    a.out_lo[idx] = reinterpret_cast<const K128&>(key).lo;
+                    a.out_hi[idx] = reinterpret_cast<const K128&>(key).hi;
+                  }
+                  a.out_count[idx] = c;
+                  if (MODE == 1 && a.out_mask)
+                    for (int q = 0; q < W; q++) a.out_mask[idx * W + q] = msk[(size_t)s * W + q];
                 } else {
-                  a.out_lo[idx] = reinterpret_cast<const K128&>(key).lo;
-                  a.out_hi[idx] = reinterpret_cast<const K128&>(key).hi;
+                  set_status(a.status, ST_OUT_OVERFLOW);
                 }
-                a.out_count[idx] = c;
-                if (MODE == 1 && a.out_mask)
-                  for (int q = 0; q < W; q++) a.out_mask[idx * W + q] = msk[(size_t)s * W + q];
-              } else {
-                set_status(a.status, ST_OUT_OVERFLOW);
               }
+              ob += __popc(bal);
             }
           }
         }
