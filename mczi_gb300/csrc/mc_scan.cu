@@ -23,6 +23,7 @@
 #include "mczi_internal.h"
 #include "mczi_common.cuh"
 #include "scan.cuh"
+#include "bulk.cuh"
 
 namespace mczi {
 
@@ -35,6 +36,7 @@ constexpr int PKW = (SCAN_TILE + 128) / 16 + 4;      // packed words staged
 constexpr int FBW = (SCAN_TILE + 128) / 32 + 4;      // fragment-bit words staged
 constexpr int WPT = SCAN_TILE / SCANK_THREADS;       // windows per thread
 static_assert(SCAN_TILE <= 8192, "event encoding holds 13-bit positions");
+static_assert(SCAN_TILE % 512 == 0, "a tile's packed words and fragment bits start on 16-byte boundaries");
 
 struct Cnt2 {
   uint32_t ev, st;
@@ -95,14 +97,6 @@ __device__ __forceinline__ bool in_range(uint32_t mval, uint32_t lo, uint32_t hi
   return p1 >= lo && p1 < hi;
 }
 
-// 64 fragment-start bits beginning at relative bit q
-__device__ __forceinline__ uint64_t bits64(const uint32_t* sfb, uint32_t q) {
-  const uint32_t i = q >> 5, o = q & 31;
-  const uint64_t a = (uint64_t)sfb[i] | ((uint64_t)sfb[i + 1] << 32);
-  const uint64_t b = (uint64_t)sfb[i + 2];
-  return o ? ((a >> o) | (b << (64 - o))) : a;
-}
-
 }  // namespace
 
 constexpr int MVL = SCAN_TILE + SCAN_TILE / 16 + 2;  // minimizer values, padded like hp()
@@ -122,6 +116,7 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   uint32_t* ev = sh_h;  // reused once the minima are known: pos | start << 13 | rank << 14
   __shared__ Cnt2 shc[SCAN_THREADS + 1];
   __shared__ unsigned long long s_base;
+  __shared__ __align__(8) uint64_t s_bar;  // completion of the staging copies
 
   const uint64_t nb = *a.n_bases;
   uint64_t tile = blockIdx.x;
@@ -134,18 +129,39 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   if (t0 + (uint64_t)k > nb) return;  // no valid window in this tile (uniform per CTA)
   const int tid = threadIdx.x;
 
-  // stage packed words and fragment bits (t0 is a multiple of 32)
-  const uint64_t pw0 = t0 >> 4, fw0 = t0 >> 5;
-  for (int i = tid; i < PKW; i += SCANK_THREADS) {
+  // stage packed words and fragment bits.  The tile's words start on a 1 KiB
+  // (packed) and 512-byte (bits) boundary, so their in-range body goes by
+  // two bulk copies (whole 16-byte groups) on one mbarrier; the words past
+  // the streams' ends (the last tile) are zeros written by the threads.
+  const uint64_t pw0 = t0 >> 4, fw0 = t0 >> 5;  // pw0 < packed_words: the tile holds a window
+  const uint64_t fwords = (a.packed_words + 1) >> 1;
+  const uint32_t npk = (uint32_t)(a.packed_words - pw0 < (uint64_t)PKW ? a.packed_words - pw0 : (uint64_t)PKW) & ~3u;
+  const uint32_t nfb = (uint32_t)(fwords - fw0 < (uint64_t)FBW ? fwords - fw0 : (uint64_t)FBW) & ~3u;
+  if (tid == 0) mbar_init(&s_bar, 1);
+  __syncthreads();
+  if (tid == 0) {
+    mbar_arrive_expect_tx(&s_bar, (npk + nfb) * 4u);
+    if (npk) bulk_load(spk, a.packed + pw0, npk * 4u, &s_bar);
+    if (nfb) bulk_load(sfb, a.fbits + fw0, nfb * 4u, &s_bar);
+  }
+  for (int i = (int)npk + tid; i < PKW; i += SCANK_THREADS) {
     const uint64_t wi = pw0 + (uint64_t)i;
     spk[i] = wi < a.packed_words ? a.packed[wi] : 0u;
   }
-  const uint64_t fwords = (a.packed_words + 1) >> 1;
-  for (int i = tid; i < FBW; i += SCANK_THREADS) {
+  for (int i = (int)nfb + tid; i < FBW; i += SCANK_THREADS) {
     const uint64_t wi = fw0 + (uint64_t)i;
     sfb[i] = wi < fwords ? a.fbits[wi] : 0u;
   }
-  __syncthreads();
+  const bool staged = mbar_wait(&s_bar, 0, 1u << 20);
+  if (__syncthreads_or(!staged)) {
+    // the copies did not complete: record it, wait once more (bounded) so
+    // nothing lands after the block exits, and leave the tile
+    if (tid == 0) {
+      set_status(a.status, ST_SPIN_TIMEOUT);
+      mbar_wait(&s_bar, 0, 1u << 20);
+    }
+    return;
+  }
 
   // m-mer hashes for positions [t0, t0 + SCAN_TILE + w - 1): 16 per thread,
   // then the tail of w - 1 positions in runs of 16

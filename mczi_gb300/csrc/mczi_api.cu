@@ -284,6 +284,7 @@ int32_t pipe_scan(mczi_ctx* ctx, Pipe& p, int k, int m, uint32_t p1_lo, uint32_t
     CK(cudaMemcpyAsync(h, sc + SC_NDESC, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(h + 1, sc + SC_STATUS, 8, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (h[1] & ST_SPIN_TIMEOUT) return fail(ctx, MCZI_ERR_DEVICE, "a scan tile's staging copy did not complete");
     if (!(h[1] & ST_DESC_OVERFLOW)) {
       p.n_desc = h[0];
       p.desc_cap = desc_cap;
@@ -705,6 +706,7 @@ int32_t stream_pack_scan(mczi_ctx* ctx, const mczi_input* inputs, size_t n, cons
   CK(cudaMemcpyAsync(h, sc + SC_NDESC, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(h + 1, sc + SC_STATUS, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  if (h[1] & ST_SPIN_TIMEOUT) return fail(ctx, MCZI_ERR_DEVICE, "a scan tile's staging copy did not complete");
   if (h[1] & ST_DESC_OVERFLOW) {
     *overflow = true;
     return MCZI_OK;
@@ -850,6 +852,7 @@ int32_t run_count_graph(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode,
     CK(cudaMemcpyAsync(h, ctx->scalars.p, sizeof h, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     const uint32_t st = (uint32_t)(h[SC_STATUS] | h[SC_SCANST]);
+    if (st & ST_SPIN_TIMEOUT) return fail(ctx, MCZI_ERR_DEVICE, "a scan tile's staging copy did not complete");
     if (st & (ST_DESC_OVERFLOW | ST_OUT_OVERFLOW | ST_TABLE_STUCK | ST_COUNT_WIDTH)) {
       drop_graph(ctx);  // these inputs outgrew the captured sizes (or fail on the plain path)
       rc = run_count(ctx, cfg, mode, n_records);
