@@ -106,6 +106,9 @@ static_assert(HLP >= SCAN_TILE + 2, "events reuse the hash array");
 
 size_t scan_smem_bytes() { return (size_t)(PKW + FBW + HLP + MVL + VBW) * sizeof(uint32_t); }
 
+// KC, MC > 0 compile the kernel for one (k, m): the minima loops then have
+// constant trip counts and unroll; 0 takes both from the arguments
+template <int KC, int MC>
 __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   extern __shared__ __align__(16) uint32_t dyn[];
   uint32_t* spk = dyn;
@@ -125,7 +128,7 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
     if (tile >= a.tile_range[1]) return;
   }
   const uint64_t t0 = tile * SCAN_TILE;
-  const int k = a.k, m = a.m, w = k - m + 1;
+  const int k = KC > 0 ? KC : a.k, m = MC > 0 ? MC : a.m, w = k - m + 1;
   if (t0 + (uint64_t)k > nb) return;  // no valid window in this tile (uniform per CTA)
   const int tid = threadIdx.x;
 
@@ -183,6 +186,7 @@ __global__ void __launch_bounds__(SCANK_THREADS) k_scan(ScanArgs a) {
   {
     const int nb_end = ((WPT - 1) / w + 1) * w;  // end of the block holding position 15
     uint32_t run = 0xffffffffu;
+#pragma unroll
     for (int j = nb_end - 1; j >= WPT; j--) run = min(run, sh_h[hp(r0 + j)]);
     int rem = (WPT - 1) % w;  // position within its block, counting down
 #pragma unroll
@@ -311,17 +315,28 @@ __global__ void k_scan_window(const uint64_t* __restrict__ avail, uint64_t* __re
   range[1] = hi;
 }
 
+// the (k, m) pairs of the benchmark workloads get their own kernels
+using ScanKernel = void (*)(ScanArgs);
+static ScanKernel scan_kernel(int k, int m) {
+  if (k == 63 && m == 21) return k_scan<63, 21>;
+  if (k == 31 && m == 21) return k_scan<31, 21>;
+  if (k == 31 && m == 19) return k_scan<31, 19>;
+  return k_scan<0, 0>;
+}
+
 // the attribute is per device: set before every launch (a host-side call of
 // microseconds, allowed during stream capture)
-static void scan_attr() {
-  cudaFuncSetAttribute(k_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scan_smem_bytes());
+static ScanKernel scan_attr(const ScanArgs& a) {
+  const ScanKernel f = scan_kernel(a.k, a.m);
+  cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)scan_smem_bytes());
+  return f;
 }
 
 void launch_scan(const ScanArgs& a, cudaStream_t s) {
   const uint64_t ntiles = (a.max_bases + SCAN_TILE - 1) / SCAN_TILE;
   if (ntiles == 0) return;
-  scan_attr();
-  k_scan<<<(unsigned)ntiles, SCANK_THREADS, scan_smem_bytes(), s>>>(a);
+  const ScanKernel f = scan_attr(a);
+  f<<<(unsigned)ntiles, SCANK_THREADS, scan_smem_bytes(), s>>>(a);
 }
 
 void launch_scan_window(const uint64_t* avail, uint64_t* range, bool final, uint64_t max_tiles, uint32_t* status,
@@ -331,8 +346,8 @@ void launch_scan_window(const uint64_t* avail, uint64_t* range, bool final, uint
 
 void launch_scan_range(const ScanArgs& a, uint64_t max_tiles, cudaStream_t s) {
   if (max_tiles == 0) return;
-  scan_attr();
-  k_scan<<<(unsigned)max_tiles, SCANK_THREADS, scan_smem_bytes(), s>>>(a);
+  const ScanKernel f = scan_attr(a);
+  f<<<(unsigned)max_tiles, SCANK_THREADS, scan_smem_bytes(), s>>>(a);
 }
 
 }  // namespace mczi

@@ -188,12 +188,12 @@ __host__ __device__ __forceinline__ uint64_t bd_start(uint64_t bd) { return bd >
 __host__ __device__ __forceinline__ uint32_t bd_windows(uint64_t bd) { return (uint32_t)((bd >> 11) & 0xfffu) + 1u; }
 __host__ __device__ __forceinline__ uint32_t bd_p2(uint64_t bd) { return (uint32_t)(bd & 0x7ffu); }
 
-// canonical m-mer hash: the minimizer order (strand-symmetric by construction)
+// canonical m-mer hash: the minimizer order (strand-symmetric by
+// construction).  Multiplicative hashing (Knuth): the top half of the 64-bit
+// product with an odd constant, one multiply and no shifts of the integer
+// pipe, which bounds the scan.
 __device__ __forceinline__ uint32_t mmer_hash64(uint64_t canon) {
-  uint64_t x = canon * 0x9E3779B97F4A7C15ull;
-  x ^= x >> 29;
-  x *= 0xBF58476D1CE4E5B9ull;
-  return (uint32_t)(x >> 32);
+  return (uint32_t)((canon * 0x9E3779B97F4A7C15ull) >> 32);
 }
 
 }  // namespace mczi
