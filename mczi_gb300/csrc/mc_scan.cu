@@ -46,11 +46,19 @@ struct Cnt2Op {
   static __device__ Cnt2 combine(const Cnt2& a, const Cnt2& b) { return Cnt2{a.ev + b.ev, a.st + b.st}; }
 };
 
+// order of an m-mer (m <= 32) from both strands' values: the smaller of the
+// two strands' hashes, a function of the canonical m-mer.  The multiplies run
+// on the FMA pipe; the compare and select of the canonical value would load
+// the integer pipe, which bounds the scan.
+__device__ __forceinline__ uint32_t mmer_order(uint64_t f, uint64_t r) {
+  return min(mmer_hash64(f), mmer_hash64(r));
+}
+
 __device__ __forceinline__ uint32_t mmer_hash_at(const uint32_t* spk, uint32_t rel, int m) {
   if (m <= 32) {
     const uint64_t f = field64_s(spk, rel, m);
     const uint64_t r = rc64_full(f) >> (64 - 2 * m);
-    return mmer_hash64(f < r ? f : r);
+    return mmer_order(f, r);
   }
   // 32 < m <= 64: hi = first m - 32 bases, lo = last 32 bases
   const int mh = m - 32;
@@ -82,13 +90,13 @@ __device__ __forceinline__ void hash_run(const uint32_t* spk, uint32_t* sh_h, in
   uint64_t f = field64_s(spk, (uint32_t)j0, m);
   uint64_t r = rc64_full(f) >> (64 - 2 * m);
   uint64_t nxt = field64_s(spk, (uint32_t)(j0 + m), 32);  // bases j0 + m .., MSB-first
-  sh_h[hp(j0)] = mmer_hash64(f < r ? f : r);
+  sh_h[hp(j0)] = mmer_order(f, r);
   for (int i = 1; i < n; i++) {
     const uint32_t b = (uint32_t)(nxt >> 62);
     nxt <<= 2;
     f = ((f << 2) | b) & mask;
     r = (r >> 2) | ((uint64_t)(b ^ 3u) << hs);
-    sh_h[hp(j0 + i)] = mmer_hash64(f < r ? f : r);
+    sh_h[hp(j0 + i)] = mmer_order(f, r);
   }
 }
 
