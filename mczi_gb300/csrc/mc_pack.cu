@@ -69,7 +69,7 @@ __device__ __forceinline__ void load_tile(const uint8_t* __restrict__ text, uint
 // FASTA: returns LS/HDR/SEQ.  FASTQ: returns the line index mod 4.
 __device__ __forceinline__ uint32_t thread_state(const uint8_t* sb, bool fastq, uint32_t tile_state,
                                                  uint32_t tile_line4, int first) {
-  __shared__ NlSum sh[SCAN_THREADS + 1];
+  __shared__ NlSum sh[PACK_THREADS / 32 + 1];
   NlSum mine{-1, 0};
 #pragma unroll
   for (int q = 0; q < PACK_PER_THREAD / 16; q++) {
@@ -114,26 +114,30 @@ __device__ __forceinline__ uint32_t step_fastq(uint32_t c, uint32_t& line) {
 
 // Fast path for 32 bytes that are all A/C/G/T (either case): returns true and
 // the 32 MC codes MSB-first in *codes.  One u32 holds 4 bytes, first byte in
-// the low bits.
+// the low bits.  Bits 1-2 of A, C, T, G (either case) are t = 0, 1, 2, 3: a
+// byte is one of the eight letters iff it equals, up to the case bit, the
+// upper-case letter t names ('A' + {0, 2, 0x13, 6}[t], computed for four
+// bytes at once), and MC's code (A0 C1 G2 T3) is t ^ (t >> 1).  One multiply
+// gathers a word's four 2-bit codes into its top byte, first byte's highest.
 __device__ __forceinline__ bool acgt32(const uint8_t* src, uint64_t* codes) {
   const uint4 v0 = *reinterpret_cast<const uint4*>(src);
   const uint4 v1 = *reinterpret_cast<const uint4*>(src + 16);
   const uint32_t w[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
-  uint32_t ok = 0x80808080u;
-  uint64_t c = 0;
+  bool ok = true;
+  uint32_t p[8];
 #pragma unroll
   for (int j = 0; j < 8; j++) {
-    const uint32_t l = w[j] | 0x20202020u;
-    ok &= zero_bytes(l ^ 0x61616161u) | zero_bytes(l ^ 0x63636363u) | zero_bytes(l ^ 0x67676767u) |
-          zero_bytes(l ^ 0x74747474u);
-    // a0 c1 g3 t2 from bits 1-2, then MC's A0 C1 G2 T3 by x ^ (x >> 1)
     const uint32_t t = (w[j] >> 1) & 0x03030303u;
-    const uint32_t mc = t ^ ((t >> 1) & 0x01010101u);
-    const uint32_t v8 = ((mc & 3u) << 6) | (((mc >> 8) & 3u) << 4) | (((mc >> 16) & 3u) << 2) | ((mc >> 24) & 3u);
-    c |= (uint64_t)v8 << (56 - 8 * j);
+    const uint32_t t1 = (t >> 1) & 0x01010101u;
+    const uint32_t expect = 0x41414141u + 2u * t + 15u * (t1 & ~t);  // + 0x13 where t == 2
+    ok &= (w[j] | 0x20202020u) == (expect | 0x20202020u);
+    p[j] = (t ^ t1) * 0x40100401u;  // bits 24-31: codes of bytes 0, 1, 2, 3 from the top
   }
-  *codes = c;
-  return ok == 0x80808080u;
+  // the eight top bytes in order: byte 0 of the chunk at the top of *codes
+  const uint32_t hi = __byte_perm(__byte_perm(p[3], p[2], 0x0073), __byte_perm(p[1], p[0], 0x7300), 0x7610);
+  const uint32_t lo = __byte_perm(__byte_perm(p[7], p[6], 0x0073), __byte_perm(p[5], p[4], 0x7300), 0x7610);
+  *codes = ((uint64_t)hi << 32) | lo;
+  return ok;
 }
 
 // a chunk's base count and breaks as one BaseSum term
@@ -238,7 +242,7 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_count(const uint8_t* __re
                                                              const LineSum* __restrict__ line_pre, uint64_t tile_lo,
                                                              uint64_t tile_hi, BaseSum* __restrict__ out) {
   __shared__ __align__(16) uint8_t sb[PACK_TILE];
-  __shared__ BaseSum shs[SCAN_THREADS + 1];
+  __shared__ BaseSum shs[PACK_THREADS / 32 + 1];
   const uint64_t tile = tile_lo + blockIdx.x;
   if (tile >= tile_hi) return;
   load_tile(text, tile, sb);
@@ -286,11 +290,14 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __re
                                                              uint32_t* __restrict__ fbits,
                                                              uint64_t* __restrict__ input_base) {
   __shared__ __align__(16) uint8_t sb[PACK_TILE];
-  __shared__ BaseSum shs[SCAN_THREADS + 1];
+  __shared__ BaseSum shs[PACK_THREADS / 32 + 1];
   __shared__ uint32_t spk[PACK_TILE / 16 + 3];
   __shared__ uint32_t sfb[PACK_TILE / 32 + 2];
   const uint64_t tile = tile_lo + blockIdx.x;
   if (tile >= tile_hi) return;
+  // the tile's base prefix is needed after pass A: its load is issued first,
+  // so its latency overlaps the tile load and pass A
+  const BaseSum tile_pre = base_pre[tile];
   load_tile(text, tile, sb);
   for (int i = threadIdx.x; i < PACK_TILE / 16 + 2; i += PACK_THREADS) spk[i] = 0;
   for (int i = threadIdx.x; i < PACK_TILE / 32 + 2; i += PACK_THREADS) sfb[i] = 0;
@@ -329,7 +336,6 @@ __global__ void __launch_bounds__(PACK_THREADS) k_pack_write(const uint8_t* __re
     s = BaseOp::combine(s, c);
   }
   BaseSum tot;
-  const BaseSum tile_pre = base_pre[tile];
   BaseSum excl =
       BaseOp::combine(tile_pre, block_exclusive_scan<BaseSum, BaseOp, PACK_THREADS>(s, &tot, shs));
   if (threadIdx.x == 0 && (tile_info[tile] & 1u)) input_base[tile_info[tile] >> 2] = tile_pre.nb;

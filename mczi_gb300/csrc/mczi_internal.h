@@ -8,19 +8,21 @@ namespace mczi {
 
 // ---------------------------------------------------------------- K1 packer
 // The tile sizes are compile-time constants (shared-memory arrays and unrolled
-// per-thread loops are sized by them); a build may override them with
-// -DMCZI_PACK_THREADS=n (32 text bytes per thread) and -DMCZI_SCAN_TILE=n
-// (<= 8192 windows, 16 per thread) to measure other sizes.  The defaults are the fastest of
-// those measured on GB300.
+// per-thread loops are sized by them); a build may override the packer's
+// threads per 8 KiB tile with -DMCZI_PACK_THREADS=n (64, 128 or 256: 128, 64
+// or 32 text bytes per thread) and the scan tile with -DMCZI_SCAN_TILE=n
+// (<= 8192 windows, 16 per thread) to measure other sizes.  The defaults are
+// the fastest of those measured on GB300.
 #ifndef MCZI_PACK_THREADS
-#define MCZI_PACK_THREADS 256
+#define MCZI_PACK_THREADS 128
 #endif
 #ifndef MCZI_SCAN_TILE
 #define MCZI_SCAN_TILE 4096
 #endif
-constexpr int PACK_THREADS = MCZI_PACK_THREADS;  // 32 bytes per thread
-constexpr int PACK_TILE = 32 * PACK_THREADS;      // text bytes per CTA
+constexpr int PACK_THREADS = MCZI_PACK_THREADS;
+constexpr int PACK_TILE = 8192;  // text bytes per CTA (inputs are laid out in whole tiles)
 constexpr int PACK_PER_THREAD = PACK_TILE / PACK_THREADS;
+static_assert(PACK_PER_THREAD % 32 == 0 && PACK_THREADS % 32 == 0, "whole 32-byte chunks, whole warps per tile");
 
 struct LineSum {
   int64_t last;   // absolute position of the last '\n' (or -1)
