@@ -289,6 +289,19 @@ int32_t mczi_set_zi_bucket_records(mczi_ctx* ctx, uint32_t records);
 int32_t mczi_read_input_file(const char* path, uint8_t** data, uint64_t* len, char* err, uint64_t err_cap);
 void mczi_free_input(uint8_t* data);
 
+/* Decodes on the device a gzip buffer whose members carry their sizes (BGZF:
+ * the "BC" extra subfield), one warp per member, each member checked against
+ * its ISIZE and CRC-32, and copies the bytes to out (cap bytes; *n_out gets
+ * the decoded length, also when out is too small).  The counting and ZI
+ * entry points take such inputs compressed (and the path-based ones keep such
+ * files compressed) and decode them this way in HBM; other gzip, xz and zstd
+ * inputs are decoded on the host.  The decompression the reference runs in
+ * front of its FASTX parser: src/lib.rs:3127-3143.  Errors:
+ * MCZI_ERR_INVALID_CONFIG (not such a buffer), MCZI_ERR_TOO_LARGE (out too
+ * small), MCZI_ERR_IO (a member is not valid DEFLATE or fails its checks). */
+int32_t mczi_inflate_gzip(mczi_ctx* ctx, const uint8_t* gz, uint64_t len, uint8_t* out, uint64_t cap,
+                          uint64_t* n_out);
+
 /* ------------------------------------------------------------- ZI serving */
 
 /* A resident ZI dictionary answering subtraction requests with continuous

@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-fsigned-char",
               "-I", str(ROOT / "include")] + ARCH
 CUDA_SOURCES = ["mc_pack.cu", "mc_scan.cu", "mc_partition.cu", "mc_count.cu", "mczi_api.cu", "zi.cu",
-                "mc_pack_noalloc.cu", "mc_precount.cu", "simplitig.cu", "exchange.cu"]
+                "mc_pack_noalloc.cu", "mc_precount.cu", "simplitig.cu", "exchange.cu", "inflate.cu"]
 CXX_SOURCES = ["host_io.cpp", "serve.cpp", "decompress.cpp"]
 
 

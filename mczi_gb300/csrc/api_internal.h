@@ -177,6 +177,9 @@ struct mczi_ctx {
   mczi::HostPinned kff_host;     // their host copy, written to the file as is
   mczi::DevBuf sx_keys, sx_tab, sx_rank, sx_ext;  // simplitig writer: sorted keys, key->rank table, extensions
   mczi::DevBuf stream_scratch;     // streamed staging: pack carries, scan tile range
+  // gzip inputs decoded on the device: compressed bytes, member table, work
+  // counter / status / per-input formats, and the output of mczi_inflate_gzip
+  mczi::DevBuf gz_comp, gz_members, gz_scratch, gz_out;
   cudaStream_t copy_stream = nullptr;  // host-to-device copies of the streamed staging
   cudaEvent_t ev_copy = nullptr;       // last copied segment
   int streamed = 1;                    // one-shot counts overlap staging with pack + scan
@@ -270,14 +273,23 @@ struct Pipe {
 
 
 struct InputPlan {
-  std::vector<uint64_t> off, len;  // per input: text offset (tile-aligned), bytes
+  std::vector<uint64_t> off, len;  // per input: text offset (tile-aligned), bytes (decoded)
   std::vector<uint32_t> tinfo;     // per tile
   std::vector<uint64_t> tile0;     // per input: first tile
   uint64_t text_len = 0, n_tiles = 0, skipped = 0, h2d_bytes = 0;
+  // per input: its text on the host (the caller's bytes, or decoded here when
+  // compressed and not decoded on the device); null for an input decoded on
+  // the device
+  std::vector<const uint8_t*> data;
+  std::vector<std::vector<uint8_t>> decoded;
+  // gzip inputs whose members carry their sizes: decoded on the device into
+  // the text (members' out_off relative to their input's text offset)
+  std::vector<mczi::GzMember> gz;
+  std::vector<uint32_t> gz_inputs;
 };
 int32_t plan_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n, InputPlan& pl);
 int32_t stage_layout(mczi_ctx* ctx, const InputPlan& pl, size_t n);
-int32_t copy_text_range(mczi_ctx* ctx, const mczi_input* inputs, size_t n, const InputPlan& pl, uint64_t b0,
+int32_t copy_text_range(mczi_ctx* ctx, const mczi_input* inputs, size_t n, InputPlan& pl, uint64_t b0,
                         uint64_t b1, cudaStream_t s);
 int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n);
 // Streamed staging: the text (laid out by stage_layout) is copied in segments
@@ -286,7 +298,7 @@ int32_t stage_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n);
 // packed and the superkmers in (desc, key), or with *overflow set when they
 // did not fit (then pipe_scan redoes the scan).
 bool streamed_worthwhile(const mczi_ctx* ctx, const InputPlan& pl);
-int32_t stream_pack_scan(mczi_ctx* ctx, const mczi_input* inputs, size_t n, const InputPlan& pl, int k, int m,
+int32_t stream_pack_scan(mczi_ctx* ctx, const mczi_input* inputs, size_t n, InputPlan& pl, int k, int m,
                          Pipe& p, bool* overflow);
 // simplitig.cu: extension table of n sorted distinct keys (lo, hi host arrays)
 // into ext_host (n x SIMPLITIG_STRIDE words; see host_io.h)

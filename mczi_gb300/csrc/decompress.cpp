@@ -305,18 +305,86 @@ bool decompress_buffer(const std::vector<uint8_t>& in, std::vector<uint8_t>* out
   }
 }
 
-bool read_input_file(const std::string& path, std::vector<uint8_t>* out, std::string* err) {
+// RFC 1952 member layout: 10-byte header (magic, CM = 8, FLG, MTIME, XFL,
+// OS), optional FEXTRA (XLEN, subfields SI1 SI2 SLEN data), FNAME and
+// FCOMMENT (zero-terminated), FHCRC (2 bytes), the DEFLATE data, then CRC-32
+// and ISIZE.  BGZF puts the member size minus one in subfield 'B' 'C'.
+bool gzip_sized_members(const uint8_t* p, uint64_t n, std::vector<GzSpan>* members, uint64_t* out_total) {
+  members->clear();
+  uint64_t pos = 0, total = 0;
+  auto u16 = [&](uint64_t at) { return (uint32_t)p[at] | ((uint32_t)p[at + 1] << 8); };
+  auto u32 = [&](uint64_t at) { return u16(at) | (u16(at + 2) << 16); };
+  while (pos < n) {
+    if (p[pos] == 0) {  // zero padding after the last member
+      for (uint64_t i = pos; i < n; i++)
+        if (p[i] != 0) return false;
+      break;
+    }
+    if (n - pos < 18 || p[pos] != 0x1f || p[pos + 1] != 0x8b || p[pos + 2] != 8) return false;
+    const uint32_t flg = p[pos + 3];
+    if (!(flg & 4u)) return false;  // no extra field: no size
+    uint64_t h = pos + 10;
+    const uint32_t xlen = u16(h);
+    h += 2;
+    if (h + xlen > n) return false;
+    uint64_t bsize = 0;
+    bool have = false;
+    for (uint64_t f = h; f + 4 <= h + xlen;) {
+      const uint32_t slen = u16(f + 2);
+      if (f + 4 + slen > h + xlen) return false;
+      if (p[f] == 'B' && p[f + 1] == 'C' && slen == 2) {
+        bsize = u16(f + 4);
+        have = true;
+      }
+      f += 4 + slen;
+    }
+    if (!have) return false;
+    h += xlen;
+    const uint64_t end = pos + bsize + 1;
+    if (end > n) return false;
+    for (uint32_t bit : {8u, 16u}) {  // FNAME, FCOMMENT
+      if (flg & bit) {
+        while (h < end && p[h] != 0) h++;
+        h++;
+      }
+    }
+    if (flg & 2u) h += 2;  // FHCRC
+    if (h + 8 > end) return false;
+    GzSpan m;
+    m.in_off = h;
+    m.in_len = (uint32_t)(end - 8 - h);
+    m.crc = u32(end - 8);
+    m.out_len = u32(end - 4);
+    total += m.out_len;
+    members->push_back(m);
+    pos = end;
+  }
+  if (members->empty()) return false;
+  *out_total = total;
+  return true;
+}
+
+bool read_input_file(const std::string& path, std::vector<uint8_t>* out, std::string* err, bool keep_sized_gzip) {
   std::vector<uint8_t> raw;
   if (!read_file(path, &raw, err)) return false;
-  if (input_format(raw.data(), raw.size()) == InputFormat::Plain) {
+  const InputFormat f = input_format(raw.data(), raw.size());
+  if (f == InputFormat::Plain) {
     out->swap(raw);
     return true;
+  }
+  if (keep_sized_gzip && f == InputFormat::Gzip) {
+    std::vector<GzSpan> m;
+    uint64_t total = 0;
+    if (gzip_sized_members(raw.data(), raw.size(), &m, &total)) {
+      out->swap(raw);
+      return true;
+    }
   }
   return decompress_buffer(raw, out, path, err);
 }
 
 bool read_input_files(const char* const* paths, size_t n, std::vector<std::vector<uint8_t>>* out,
-                      std::string* err) {
+                      std::string* err, bool keep_sized_gzip) {
   out->assign(n, {});
   std::vector<std::string> errs(n);
   std::vector<char> ok(n, 1);
@@ -324,7 +392,8 @@ bool read_input_files(const char* const* paths, size_t n, std::vector<std::vecto
   const size_t hw = std::max(1u, std::thread::hardware_concurrency());
   const size_t nt = std::min(n, hw);
   auto work = [&]() {
-    for (size_t i; (i = next.fetch_add(1)) < n;) ok[i] = read_input_file(paths[i], &(*out)[i], &errs[i]) ? 1 : 0;
+    for (size_t i; (i = next.fetch_add(1)) < n;)
+      ok[i] = read_input_file(paths[i], &(*out)[i], &errs[i], keep_sized_gzip) ? 1 : 0;
   };
   std::vector<std::thread> th;
   for (size_t t = 1; t < nt; t++) th.emplace_back(work);

@@ -44,10 +44,24 @@ enum class InputFormat { Plain, Gzip, Xz, Zstd };
 InputFormat input_format(const uint8_t* p, size_t n);
 bool decompress_buffer(const std::vector<uint8_t>& in, std::vector<uint8_t>* out, const std::string& name,
                        std::string* err);
-// a FASTA/FASTQ file, decompressed when it is gzip, xz or zstd
-bool read_input_file(const std::string& path, std::vector<uint8_t>* out, std::string* err);
+// One gzip member's DEFLATE data (offset and length in the buffer, header and
+// trailer excluded) and its trailer (ISIZE, CRC-32).
+struct GzSpan {
+  uint64_t in_off;
+  uint32_t in_len, out_len, crc;
+};
+// The members of a gzip buffer when every member carries its size in a BGZF
+// "BC" extra subfield (so the boundaries are known without decoding), with
+// their decoded total; false for any other buffer (then it is decoded on the
+// host).  Zero bytes after the last member are allowed.
+bool gzip_sized_members(const uint8_t* p, uint64_t n, std::vector<GzSpan>* members, uint64_t* out_total);
+// a FASTA/FASTQ file, decompressed when it is gzip, xz or zstd; with
+// keep_sized_gzip a gzip file whose members carry their sizes is returned as
+// it is, for decoding on the device
+bool read_input_file(const std::string& path, std::vector<uint8_t>* out, std::string* err,
+                     bool keep_sized_gzip = false);
 // several files, decoded on parallel host threads; the first failure's message
 bool read_input_files(const char* const* paths, size_t n, std::vector<std::vector<uint8_t>>* out,
-                      std::string* err);
+                      std::string* err, bool keep_sized_gzip = false);
 
 }  // namespace mczi

@@ -77,30 +77,61 @@ int detect_format(const uint8_t* d, uint64_t n) {
 
 // Host-side layout of a batch of inputs in HBM: each input starts on a
 // PACK_TILE boundary, the gaps are '\n'; per tile: input << 2 | fastq << 1 |
-// input starts here.
+// input starts here.  Compressed inputs: a gzip input whose members carry
+// their sizes is decoded on the device when the text is copied (its format is
+// checked there); other gzip, xz and zstd inputs are decoded here.
 int32_t plan_inputs(mczi_ctx* ctx, const mczi_input* inputs, size_t n, InputPlan& pl) {
   if (n == 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "at least one input file is required");
   pl.off.assign(n, 0);
   pl.len.assign(n, 0);
+  pl.data.assign(n, nullptr);
+  pl.decoded.clear();
+  pl.decoded.reserve(n);
+  pl.gz.clear();
+  pl.gz_inputs.clear();
   std::vector<int> fmt(n);
   uint64_t pos = 0;
   pl.skipped = 0;
   pl.h2d_bytes = 0;
+  std::vector<GzSpan> spans;
   for (size_t i = 0; i < n; i++) {
     const uint8_t* d = inputs[i].data;
     uint64_t l = d ? inputs[i].len : 0;
-    int f = detect_format(d, l);
-    if (f < 0) {
-      std::fprintf(stderr, "MC_WARN\tskipped_invalid_fastx_input\tinput\t%zu\terror\tInvalid record start\n", i);
-      pl.skipped++;
-      l = 0;
-      f = 0;
+    int f = 0;
+    const InputFormat cf = input_format(d, l);
+    uint64_t total = 0;
+    if (cf == InputFormat::Gzip && gzip_sized_members(d, l, &spans, &total)) {
+      uint64_t o = 0;
+      for (const GzSpan& sp : spans) {
+        pl.gz.push_back(GzMember{sp.in_off, o, sp.in_len, sp.out_len, sp.crc, (uint32_t)i});
+        o += sp.out_len;
+      }
+      pl.gz_inputs.push_back((uint32_t)i);
+      pl.h2d_bytes += l;  // the compressed bytes cross the host link
+      l = total;
+    } else {
+      if (cf != InputFormat::Plain) {
+        std::vector<uint8_t> raw(d, d + l), dec;
+        std::string e;
+        if (!decompress_buffer(raw, &dec, "input " + std::to_string(i), &e)) return fail(ctx, MCZI_ERR_IO, e);
+        pl.decoded.push_back(std::move(dec));
+        d = pl.decoded.back().data();
+        l = pl.decoded.back().size();
+      }
+      pl.data[i] = d;
+      f = detect_format(d, l);
+      if (f < 0) {
+        std::fprintf(stderr, "MC_WARN\tskipped_invalid_fastx_input\tinput\t%zu\terror\tInvalid record start\n", i);
+        pl.skipped++;
+        l = 0;
+        f = 0;
+      }
+      if (f == 2) { l = 0; f = 0; }
+      pl.h2d_bytes += l;
     }
-    if (f == 2) { l = 0; f = 0; }
     pl.off[i] = pos;
     pl.len[i] = l;
     fmt[i] = f;
-    pl.h2d_bytes += l;
     const uint64_t tiles = l == 0 ? 1 : (l + PACK_TILE - 1) / PACK_TILE;  // every input owns >= 1 tile
     pos += tiles * PACK_TILE;
   }
@@ -136,9 +167,102 @@ int32_t stage_layout(mczi_ctx* ctx, const InputPlan& pl, size_t n) {
   return MCZI_OK;
 }
 
+namespace {
+
+// first non-newline byte of each device-decoded input: 0 '>', 1 '@', 2 none
+// (empty), 3 another byte (not a FASTX record start); one CTA per input
+__global__ void k_gz_formats(const uint8_t* __restrict__ text, const uint64_t* __restrict__ span, uint32_t n,
+                             int32_t* __restrict__ fmt) {
+  __shared__ unsigned long long first;
+  if (blockIdx.x >= n) return;
+  const uint64_t o = span[2 * blockIdx.x], len = span[2 * blockIdx.x + 1];
+  if (threadIdx.x == 0) first = ~0ull;
+  __syncthreads();
+  for (uint64_t i0 = 0; i0 < len; i0 += blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    if (i < len && text[o + i] != '\n' && text[o + i] != '\r') atomicMin(&first, (unsigned long long)i);
+    __syncthreads();
+    if (first != ~0ull) break;  // uniform: read after the barrier
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    int32_t f = 2;
+    if (first != ~0ull) {
+      const uint8_t c = text[o + first];
+      f = c == '>' ? 0 : c == '@' ? 1 : 3;
+    }
+    fmt[blockIdx.x] = f;
+  }
+}
+
+// Decodes the plan's device gzip inputs into the text (their bytes cross the
+// host link compressed), then checks each one's first record start and fixes
+// its tiles' format bits (a FASTQ input) or blanks it (not FASTX: skipped with
+// MC's warning, as a plain input would be).
+int32_t inflate_inputs(mczi_ctx* ctx, const mczi_input* inputs, InputPlan& pl, cudaStream_t s) {
+  const size_t ng = pl.gz_inputs.size();
+  std::vector<uint64_t> coff(ng + 1, 0);
+  for (size_t j = 0; j < ng; j++) coff[j + 1] = coff[j] + inputs[pl.gz_inputs[j]].len;
+  CKA(ctx->gz_comp, coff[ng] + 16);
+  uint8_t* comp = ctx->gz_comp.as<uint8_t>();
+  std::vector<uint64_t> slot(pl.off.size(), 0);
+  for (size_t j = 0; j < ng; j++) {
+    const uint32_t i = pl.gz_inputs[j];
+    slot[i] = j;
+    CK(cudaMemcpyAsync(comp + coff[j], inputs[i].data, inputs[i].len, cudaMemcpyHostToDevice, s));
+  }
+  std::vector<GzMember> m(pl.gz);
+  for (GzMember& g : m) {
+    g.in_off += coff[slot[g.input]];
+    g.out_off += pl.off[g.input];
+  }
+  std::vector<uint64_t> span(2 * ng);
+  for (size_t j = 0; j < ng; j++) {
+    span[2 * j] = pl.off[pl.gz_inputs[j]];
+    span[2 * j + 1] = pl.len[pl.gz_inputs[j]];
+  }
+  CKA(ctx->gz_members, m.size() * sizeof(GzMember) + span.size() * 8 + 16);
+  GzMember* dm = ctx->gz_members.as<GzMember>();
+  uint64_t* dspan = reinterpret_cast<uint64_t*>(dm + m.size());
+  CK(cudaMemcpyAsync(dm, m.data(), m.size() * sizeof(GzMember), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dspan, span.data(), span.size() * 8, cudaMemcpyHostToDevice, s));
+  CKA(ctx->gz_scratch, 64 + 4 * ng);
+  uint32_t* scr = ctx->gz_scratch.as<uint32_t>();
+  CK(cudaMemsetAsync(scr, 0, 64 + 4 * ng, s));
+  launch_inflate(comp, dm, (uint32_t)m.size(), ctx->text.as<uint8_t>(), scr, scr + 1, ctx->sm_count * 16, s);
+  k_gz_formats<<<(unsigned)ng, 256, 0, s>>>(ctx->text.as<uint8_t>(), dspan, (uint32_t)ng,
+                                           reinterpret_cast<int32_t*>(scr + 16));
+  CK(cudaGetLastError());
+  std::vector<uint32_t> h(16 + ng);
+  CK(cudaMemcpyAsync(h.data(), scr, (16 + ng) * 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (h[1] & ST_GZ_CORRUPT)
+    return fail(ctx, MCZI_ERR_IO, "gzip input: a member is not valid DEFLATE data or does not match its size or CRC-32");
+  for (size_t j = 0; j < ng; j++) {
+    const uint32_t i = pl.gz_inputs[j];
+    const int32_t f = (int32_t)h[16 + j];
+    const uint64_t t0 = pl.tile0[i], t1 = i + 1 < pl.off.size() ? pl.tile0[i + 1] : pl.n_tiles;
+    if (f == 1) {
+      for (uint64_t t = t0; t < t1; t++) pl.tinfo[t] |= 2u;
+      CK(cudaMemcpyAsync(ctx->tile_info.as<uint32_t>() + t0, pl.tinfo.data() + t0, (t1 - t0) * 4,
+                         cudaMemcpyHostToDevice, s));
+    } else if (f == 3) {
+      std::fprintf(stderr, "MC_WARN\tskipped_invalid_fastx_input\tinput\t%u\terror\tInvalid record start\n", i);
+      pl.skipped++;
+      ctx->skipped = pl.skipped;
+      CK(cudaMemsetAsync(ctx->text.as<uint8_t>() + pl.off[i], '\n', pl.len[i], s));
+    }
+  }
+  CK(cudaStreamSynchronize(s));  // the tile formats were staged from a host vector
+  return MCZI_OK;
+}
+
+}  // namespace
+
 // Copies the text bytes [b0, b1) of the batch (inputs and their '\n' gaps)
-// on stream s.
-int32_t copy_text_range(mczi_ctx* ctx, const mczi_input* inputs, size_t n, const InputPlan& pl, uint64_t b0,
+// on stream s; inputs decoded on the device are decoded when the range
+// covers the whole text (callers that stage in segments never have them).
+int32_t copy_text_range(mczi_ctx* ctx, const mczi_input* inputs, size_t n, InputPlan& pl, uint64_t b0,
                         uint64_t b1, cudaStream_t s) {
   uint8_t* text = ctx->text.as<uint8_t>();
   for (size_t i = 0; i < n; i++) {
@@ -147,9 +271,13 @@ int32_t copy_text_range(mczi_ctx* ctx, const mczi_input* inputs, size_t n, const
     if (end <= b0) continue;
     if (o >= b1) break;
     const uint64_t c0 = std::max(o, b0), c1 = std::min(e, b1);
-    if (c1 > c0) CK(cudaMemcpyAsync(text + c0, inputs[i].data + (c0 - o), c1 - c0, cudaMemcpyHostToDevice, s));
+    if (c1 > c0 && pl.data[i]) CK(cudaMemcpyAsync(text + c0, pl.data[i] + (c0 - o), c1 - c0, cudaMemcpyHostToDevice, s));
     const uint64_t g0 = std::max(e, b0), g1 = std::min(end, b1);
     if (g1 > g0) CK(cudaMemsetAsync(text + g0, '\n', g1 - g0, s));
+  }
+  if (!pl.gz_inputs.empty()) {
+    if (b0 != 0 || b1 != pl.text_len) return fail(ctx, MCZI_ERR_STATE, "device-decoded inputs staged in segments");
+    return inflate_inputs(ctx, inputs, pl, s);
   }
   return MCZI_OK;
 }
@@ -632,10 +760,12 @@ int32_t run_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int mode, uint6
 static uint64_t stream_seg_min(const mczi_ctx* ctx) { return ctx->stream_seg_tiles > 0 ? ctx->stream_seg_tiles : 4096; }
 
 bool streamed_worthwhile(const mczi_ctx* ctx, const InputPlan& pl) {
-  return ctx->streamed && pl.n_tiles >= 2 * stream_seg_min(ctx);
+  // inputs decoded on the device are staged whole (their decoded bytes
+  // appear in no host buffer to copy in segments)
+  return ctx->streamed && pl.gz_inputs.empty() && pl.n_tiles >= 2 * stream_seg_min(ctx);
 }
 
-int32_t stream_pack_scan(mczi_ctx* ctx, const mczi_input* inputs, size_t n, const InputPlan& pl, int k, int m,
+int32_t stream_pack_scan(mczi_ctx* ctx, const mczi_input* inputs, size_t n, InputPlan& pl, int k, int m,
                          Pipe& p, bool* overflow) {
   int32_t rc;
   *overflow = false;
@@ -950,7 +1080,8 @@ int32_t count_paths(mczi_ctx* ctx, const char* const* paths, size_t n, const mcz
   // plain, gzip, xz or zstd files, decoded on parallel host threads
   std::vector<std::vector<uint8_t>> data;
   std::string e;
-  if (!read_input_files(paths, n, &data, &e)) return fail(ctx, MCZI_ERR_IO, e);
+  // (gzip files whose members carry their sizes stay compressed: decoded on the device)
+  if (!read_input_files(paths, n, &data, &e, true)) return fail(ctx, MCZI_ERR_IO, e);
   std::vector<mczi_input> in(n);
   for (size_t i = 0; i < n; i++) {
     in[i].data = data[i].data();
@@ -1138,6 +1269,49 @@ __global__ void k_result_digest(const uint64_t* __restrict__ lo, const uint64_t*
     atomicAdd(&acc[1], (unsigned long long)sum);
     atomicXor(&acc[2], (unsigned long long)x);
   }
+}
+
+int32_t mczi_inflate_gzip(mczi_ctx* ctx, const uint8_t* gz, uint64_t len, uint8_t* out, uint64_t cap,
+                          uint64_t* n_out) {
+  if (!ctx) return MCZI_ERR_STATE;
+  if (!n_out) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "n_out must not be NULL");
+  *n_out = 0;
+  std::vector<GzSpan> spans;
+  uint64_t total = 0;
+  if (!gz || !gzip_sized_members(gz, len, &spans, &total))
+    return fail(ctx, MCZI_ERR_INVALID_CONFIG, "not a gzip buffer whose members carry their sizes (BGZF)");
+  *n_out = total;
+  if (total > cap || (total && !out)) return fail(ctx, MCZI_ERR_TOO_LARGE, "output buffer smaller than the decoded bytes");
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  std::vector<GzMember> m;
+  m.reserve(spans.size());
+  uint64_t o = 0;
+  for (const GzSpan& sp : spans) {
+    m.push_back(GzMember{sp.in_off, o, sp.in_len, sp.out_len, sp.crc, 0});
+    o += sp.out_len;
+  }
+  CKA(ctx->gz_comp, len + 16);
+  CKA(ctx->gz_members, m.size() * sizeof(GzMember));
+  CKA(ctx->gz_out, total + 16);
+  CKA(ctx->gz_scratch, 64);
+  uint32_t* scr = ctx->gz_scratch.as<uint32_t>();
+  CK(cudaMemcpyAsync(ctx->gz_comp.p, gz, len, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ctx->gz_members.p, m.data(), m.size() * sizeof(GzMember), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(scr, 0, 64, s));
+  launch_inflate(ctx->gz_comp.as<uint8_t>(), ctx->gz_members.as<GzMember>(), (uint32_t)m.size(),
+                 ctx->gz_out.as<uint8_t>(), scr, scr + 1, ctx->sm_count * 16, s);
+  CK(cudaGetLastError());
+  uint32_t st = 0;
+  CK(cudaMemcpyAsync(&st, scr + 1, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (st & ST_GZ_CORRUPT)
+    return fail(ctx, MCZI_ERR_IO, "gzip input: a member is not valid DEFLATE data or does not match its size or CRC-32");
+  if (total) {
+    CK(cudaMemcpyAsync(out, ctx->gz_out.p, total, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  return MCZI_OK;
 }
 
 int32_t mczi_result_digest(mczi_ctx* ctx, int32_t unit_counts, uint64_t* out) {

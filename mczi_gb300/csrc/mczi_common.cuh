@@ -25,6 +25,7 @@ enum : uint32_t {
   ST_MINTAB_FULL = 1u << 5,      // minimizer table full
   ST_ZI_OVERFLOW = 1u << 6,      // ZI absent buffer too small
   ST_COUNT_WIDTH = 1u << 7,      // a bucket holds more k-mer windows than its 32-bit counters take
+  ST_GZ_CORRUPT = 1u << 8,       // a gzip member failed to decode, or decoded to another length or CRC
 };
 
 __device__ __forceinline__ void set_status(uint32_t* st, uint32_t bit) { atomicOr(st, bit); }

@@ -55,6 +55,24 @@ void launch_pack(const PackArgs& a, cudaStream_t s);
 void launch_pack_segment(const PackArgs& a, uint64_t t0, uint64_t t1, LineSum* carry_line, BaseSum* carry_base,
                          cudaStream_t s);
 
+// ------------------------------------------------------ gzip on the device
+// One gzip member (RFC 1952) of an input whose members carry their size
+// (BGZF's "BC" extra field): its raw DEFLATE data in the compressed buffer,
+// where its bytes go in the output, and its trailer.
+struct GzMember {
+  uint64_t in_off;   // DEFLATE data offset in the compressed buffer
+  uint64_t out_off;  // offset of the decoded bytes in the output
+  uint32_t in_len;   // DEFLATE data bytes (header and trailer excluded)
+  uint32_t out_len;  // ISIZE: decoded bytes
+  uint32_t crc;      // CRC-32 of the decoded bytes
+  uint32_t input;    // index of the input the member belongs to
+};
+// Decodes every member into out (one warp per member, members taken from
+// *work, which must start at 0); a member that is not valid DEFLATE, decodes
+// to another length or fails its CRC sets ST_GZ_CORRUPT in *status.
+void launch_inflate(const uint8_t* comp, const GzMember* members, uint32_t n_members, uint8_t* out,
+                    unsigned int* work, uint32_t* status, int ctas, cudaStream_t s);
+
 // partition digits of the superkmer key (mix32 of the minimizer value)
 constexpr int P1_BITS = 12;
 constexpr int P2_BITS = 11;
