@@ -148,7 +148,9 @@ int32_t mczi_route_copy(mczi_ctx* ctx, uint32_t dest, uint8_t* out, uint64_t cap
  * [1] only a rescan, if one was needed.  After a ZI query: [0] pack, [1] scan,
  * [2] partition of the absent windows, [3] their deduplication, [4] probe; a
  * query of at least 64 MiB of text is streamed like mczi_count ([0] then
- * spans staging + pack + scan).  Returns the number of phases written. */
+ * spans staging + pack + scan).  [5]: the device gzip decoding of the last
+ * call that decoded gzip members on the device (mczi_inflate_gzip, or inputs
+ * staged compressed), 0 before any.  Returns the number of phases written. */
 int32_t mczi_phase_times(mczi_ctx* ctx, float* ms, int32_t cap);
 /* Statistics of the last run: [0] bases, [1] superkmers, [2] counting rounds,
  * [3] round splits, [4] distinct k-mers inserted, [5] kept records,

@@ -203,6 +203,7 @@ struct mczi_ctx {
   uint64_t n_out = 0;
   int mask_words = 0;  // > 0 when the last result carries per-input masks
   float phase_ms[mczi::N_PHASES] = {0, 0, 0, 0, 0};
+  float inflate_ms = 0.f;  // device gzip decoding of the last call that decoded members
   uint64_t stats[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   cudaEvent_t ev[mczi::N_PHASES + 1] = {};
   cudaEvent_t ev_pre[2] = {};

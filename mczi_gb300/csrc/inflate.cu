@@ -154,14 +154,26 @@ __device__ bool inflate_member(const uint8_t* __restrict__ in, uint32_t in_len, 
   uint32_t q = 0;   // next input byte
   uint32_t pos = 0; // decoded bytes
   bool err = false;
-  // tops the buffer up to >= 57 bits; past the input it feeds zero bytes, and
-  // a member that needs more than 8 of them is corrupt
+  // tops the buffer up to >= 32 bits, four input bytes at a time (two
+  // aligned words and a funnel shift: the bytes after a member's data are
+  // its trailer, so the second word stays inside the member); past the input
+  // it feeds zero bytes, and a member that needs more than 8 of them is
+  // corrupt
   auto refill = [&]() {
-    while (bn <= 56) {
-      const uint64_t b = q < in_len ? (uint64_t)in[q] : 0ull;
-      q++;
-      bb |= b << bn;
-      bn += 8;
+    if (bn < 32) {
+      uint32_t w = 0;
+      if (q + 4u <= in_len) {
+        const uintptr_t a = reinterpret_cast<uintptr_t>(in + q);
+        const uint32_t* p = reinterpret_cast<const uint32_t*>(a & ~(uintptr_t)3);
+        const uint32_t sh = (uint32_t)(a & 3u) * 8u;
+        w = sh ? __funnelshift_r(p[0], p[1], sh) : p[0];
+      } else {
+        for (uint32_t i = 0; i < 4; i++)
+          if (q + i < in_len) w |= (uint32_t)in[q + i] << (8 * i);
+      }
+      bb |= (uint64_t)w << bn;
+      bn += 32;
+      q += 4;
     }
     if (q > in_len + 8u) err = true;
   };
@@ -209,8 +221,8 @@ __device__ bool inflate_member(const uint8_t* __restrict__ in, uint32_t in_len, 
       if (nlit > 286 || ndist > 30) { err = true; break; }
       for (int s = lane; s < 19; s += 32) ws.lens[s] = 0;
       __syncwarp();
-      refill();  // >= 57 bits: up to 19 three-bit lengths
       for (uint32_t i = 0; i < ncl; i++) {
+        refill();
         const uint32_t l = take(3);
         if (lane == 0) ws.lens[CL_ORDER[i]] = (uint8_t)l;
       }
@@ -246,9 +258,10 @@ __device__ bool inflate_member(const uint8_t* __restrict__ in, uint32_t in_len, 
     // the distance lengths follow the literal/length ones in lens
     if (!huff_build(ws.lit, ws.lens, (int)nlit, &ws.bad, lane)) { err = true; break; }
     if (!huff_build(ws.dist, ws.lens + nlit, (int)ndist, &ws.bad, lane)) { err = true; break; }
-    // the block's symbols
+    // the block's symbols: >= 32 bits before a literal/length code and its
+    // extra bits (<= 20), again before a distance code and its extra bits (<= 28)
     for (;;) {
-      refill();  // >= 57 bits: a length code and extra bits, a distance code and extra bits
+      refill();
       if (err) break;
       int sym = huff_decode(ws.lit, bb, bn);
       if (sym < 0) { err = true; break; }
@@ -262,6 +275,7 @@ __device__ bool inflate_member(const uint8_t* __restrict__ in, uint32_t in_len, 
       sym -= 257;
       if (sym >= 29) { err = true; break; }
       const uint32_t len = LEN_BASE[sym] + take(LEN_EXTRA[sym]);
+      refill();
       const int ds = huff_decode(ws.dist, bb, bn);
       if (ds < 0 || ds >= 30) { err = true; break; }
       const uint32_t d = DIST_BASE[ds] + take(DIST_EXTRA[ds]);

@@ -229,13 +229,16 @@ int32_t inflate_inputs(mczi_ctx* ctx, const mczi_input* inputs, InputPlan& pl, c
   CKA(ctx->gz_scratch, 64 + 4 * ng);
   uint32_t* scr = ctx->gz_scratch.as<uint32_t>();
   CK(cudaMemsetAsync(scr, 0, 64 + 4 * ng, s));
+  CK(cudaEventRecord(ctx->ev[0], s));
   launch_inflate(comp, dm, (uint32_t)m.size(), ctx->text.as<uint8_t>(), scr, scr + 1, ctx->sm_count * 16, s);
+  CK(cudaEventRecord(ctx->ev[1], s));
   k_gz_formats<<<(unsigned)ng, 256, 0, s>>>(ctx->text.as<uint8_t>(), dspan, (uint32_t)ng,
                                            reinterpret_cast<int32_t*>(scr + 16));
   CK(cudaGetLastError());
   std::vector<uint32_t> h(16 + ng);
   CK(cudaMemcpyAsync(h.data(), scr, (16 + ng) * 4, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  CK(cudaEventElapsedTime(&ctx->inflate_ms, ctx->ev[0], ctx->ev[1]));
   if (h[1] & ST_GZ_CORRUPT)
     return fail(ctx, MCZI_ERR_IO, "gzip input: a member is not valid DEFLATE data or does not match its size or CRC-32");
   for (size_t j = 0; j < ng; j++) {
@@ -1299,12 +1302,15 @@ int32_t mczi_inflate_gzip(mczi_ctx* ctx, const uint8_t* gz, uint64_t len, uint8_
   CK(cudaMemcpyAsync(ctx->gz_comp.p, gz, len, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(ctx->gz_members.p, m.data(), m.size() * sizeof(GzMember), cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(scr, 0, 64, s));
+  CK(cudaEventRecord(ctx->ev[0], s));
   launch_inflate(ctx->gz_comp.as<uint8_t>(), ctx->gz_members.as<GzMember>(), (uint32_t)m.size(),
                  ctx->gz_out.as<uint8_t>(), scr, scr + 1, ctx->sm_count * 16, s);
   CK(cudaGetLastError());
+  CK(cudaEventRecord(ctx->ev[1], s));
   uint32_t st = 0;
   CK(cudaMemcpyAsync(&st, scr + 1, 4, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  CK(cudaEventElapsedTime(&ctx->inflate_ms, ctx->ev[0], ctx->ev[1]));
   if (st & ST_GZ_CORRUPT)
     return fail(ctx, MCZI_ERR_IO, "gzip input: a member is not valid DEFLATE data or does not match its size or CRC-32");
   if (total) {
@@ -1413,8 +1419,8 @@ int32_t mczi_count_datasets_to_fasta_path(mczi_ctx* ctx, const char* const* inpu
 
 int32_t mczi_phase_times(mczi_ctx* ctx, float* ms, int32_t cap) {
   if (!ctx) return MCZI_ERR_STATE;
-  int32_t n = std::min<int32_t>(cap, N_PHASES);
-  for (int32_t i = 0; i < n; i++) ms[i] = ctx->phase_ms[i];
+  int32_t n = std::min<int32_t>(cap, N_PHASES + 1);
+  for (int32_t i = 0; i < n; i++) ms[i] = i < N_PHASES ? ctx->phase_ms[i] : ctx->inflate_ms;
   return n;
 }
 

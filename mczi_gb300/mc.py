@@ -201,6 +201,19 @@ class Context:
     def write_fasta(self, path: str | os.PathLike) -> None:
         self._ck(self._lib.mczi_result_write_fasta(self._h, os.fsencode(str(path))))
 
+    def inflate_gzip(self, gz) -> bytes:
+        """Decodes a gzip buffer whose members carry their sizes (BGZF, see
+        mczi_gb300.bgzf) on the device; phase_times()[5] is the decode time."""
+        mv = _as_bytes(gz)
+        src = (C.c_char * mv.nbytes).from_buffer_copy(mv) if mv.nbytes else None
+        n = C.c_uint64()
+        rc = self._lib.mczi_inflate_gzip(self._h, src, mv.nbytes, None, 0, C.byref(n))
+        if rc not in (0, N.MCZI_ERR_TOO_LARGE):
+            self._ck(rc)
+        out = np.empty(max(1, n.value), dtype=np.uint8)
+        self._ck(self._lib.mczi_inflate_gzip(self._h, src, mv.nbytes, out.ctypes.data, n.value, C.byref(n)))
+        return out[: n.value].tobytes()
+
     def phase_times(self) -> list[float]:
         buf = (C.c_float * 8)()
         n = self._ck(self._lib.mczi_phase_times(self._h, buf, 8))

@@ -16,7 +16,7 @@ import zlib
 import numpy as np
 import pytest
 
-import bgzf
+from mczi_gb300 import bgzf
 from oracle_ref import parse_kff, to_int
 
 pytestmark = pytest.mark.gpu
