@@ -386,8 +386,8 @@ int32_t mczi_serve_close(mczi_server* srv);
  * first call, with lazy loading) and held until the process exits.  The first
  * call on a device looks its address up (cudaGetSymbolAddress) with that
  * device current and keeps it for the life of the device's primary context
- * (do not call again on a device after cudaDeviceReset); make that first call
- * before any stream capture.  Every call shares the array, so calls that
+ * (do not call again on a device after cudaDeviceReset); that first lookup
+ * may itself load the module on the device.  Every call shares the array, so calls that
  * overlap on the GPU race: issue them one at a time. */
 int32_t mczi_pack_fastx_noalloc(const uint8_t* d_text, uint64_t text_len, int32_t fastq, uint32_t* d_packed,
                                 uint64_t packed_words, uint32_t* d_fbits, uint64_t fbits_words, uint64_t* n_bases,

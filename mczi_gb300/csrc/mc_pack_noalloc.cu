@@ -18,8 +18,8 @@
 // under lazy loading (CUDA_MODULE_LOADING=LAZY, the default since CUDA 12) --
 // and held until the process exits.  Its host-side name is only a stand-in:
 // the device address is looked up with cudaGetSymbolAddress, once per device,
-// with that device current, on the first call on that device (make that
-// first call before any stream capture, since the lookup may load the module).
+// with that device current, on the first call on that device (the lookup
+// may itself load the module there).
 // The cached address is valid for the life of the device's primary context:
 // a caller that ends it (cudaDeviceReset) must not call this entry point on
 // that device again in the same process.  All calls share the array and it
