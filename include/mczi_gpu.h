@@ -165,7 +165,7 @@ int32_t mczi_run_stats(mczi_ctx* ctx, uint64_t* out, int32_t cap);
 int32_t mczi_set_count_tuning(mczi_ctx* ctx, int32_t threads, int32_t table_slots, int32_t ctas_per_sm);
 /* Windows per work item of the counting insert phase (0 = default: 4 for
  * k > 32, else 2) and the target fill of a counting round's table (0 =
- * default: 0.6). */
+ * default: 0.8 for two-pass filtered rounds, 0.6 otherwise; at most 0.85). */
 int32_t mczi_set_count_options(mczi_ctx* ctx, int32_t chunk, float fill);
 
 /* Counting rounds for threshold >= 1: 1 uses two passes over a shared-memory

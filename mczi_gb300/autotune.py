@@ -67,7 +67,7 @@ def cache_key(k: int, mode: int, threshold: int) -> str:
 def candidates(k: int, threshold: int) -> list[Tuning]:
     wide = k > 32
     shapes = [(512, 2), (1024, 1), (384, 2)] if wide else [(512, 2), (1024, 1), (256, 4)]
-    fills = [0.5, 0.6, 0.7]
+    fills = [0.8, 0.7, 0.6]
     chunks = [4, 2] if wide else [2, 4]
     filters = [1, 0] if threshold >= 1 else [0]
     out = [DEFAULT]

@@ -599,7 +599,9 @@ int32_t pipe_count(mczi_ctx* ctx, Pipe& p, int k, uint64_t x, int mode, bool emi
       ca.threads = threads;
       ca.ctas = ctx->sm_count * cps;
       ca.work_counter = reinterpret_cast<unsigned int*>(sc + SC_WORK);
-      ca.fill = ctx->count_fill > 0.f ? ctx->count_fill : 0.6f;
+      // default target fill: filtered rounds (k > 32, x >= 1) measured faster
+      // at 0.8 (fewer, larger rounds), single-pass rounds keep 0.6
+      ca.fill = ctx->count_fill > 0.f ? ctx->count_fill : (fwords > 0 ? 0.8f : 0.6f);
       // default: the fast rounds' chunk for filtered k > 32 counts, else 4
       // (k > 32) or 2 windows per work item
       ca.chunk = ctx->count_chunk > 0 ? (uint32_t)ctx->count_chunk
