@@ -843,7 +843,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the untimed autotuning on a sample")
     ap.add_argument("--no-graph", action="store_true", help="skip the graph-replay timing")
-    ap.add_argument("--workload", default="mc", choices=["mc", "mc-short", "mc-fof", "zi", "zi-serve"])
+    ap.add_argument("--workload", default="mc", choices=["mc", "mc-short", "mc-fof", "zi", "zi-serve", "gzip"])
     ap.add_argument("--zi-files", type=int, default=200)
     ap.add_argument("--zi-one-group", action="store_true",
                     help="run one 50-file group (per input, then union) and exit: the case for ZI kernel profiles")
@@ -868,6 +868,10 @@ def main():
         return run_mc_fof(args)
     if args.workload == "mc-short" and args.impl == "ours":
         return run_mc_short(args)
+    if args.workload == "gzip" and args.impl == "ours":
+        # the default line's gzip key alone (BGZF long reads decoded on the device)
+        print(json.dumps(gzip_measure(args.gzip_scale if args.gzip_scale > 0 else 0.1, 3)), flush=True)
+        return 0
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
