@@ -441,6 +441,41 @@ __device__ __forceinline__ uint32_t dd_digit(uint64_t h, int hi, int n) {
   return n == 0 ? 0u : (uint32_t)(h >> (64 - hi - n)) & ((1u << n) - 1u);
 }
 
+// Level-1 bucket of a rolled window, a function of its canonical k-mer
+// without forming it: for k <= 32 the sum of the two strands' multiplicative
+// hashes (the top half of one 64-bit product each, on the FMA pipe; a sum of
+// two uniform values mod 2^32 stays uniform, their minimum would not), for
+// longer k the strand-symmetric hash.  Level 2 and the dedup take their
+// digits from key_hash of the stored key, an independent hash.
+__device__ __forceinline__ uint32_t dd_level1(const Roll64& r, int n) {
+  const uint32_t a = (uint32_t)((r.fwd * 0x9E3779B97F4A7C15ull) >> 32);
+  const uint32_t b = (uint32_t)((r.rev * 0x9E3779B97F4A7C15ull) >> 32);
+  return n == 0 ? 0u : (a + b) >> (32 - n);
+}
+__device__ __forceinline__ uint32_t dd_level1(const Roll128& r, int n) {
+  return n == 0 ? 0u : (uint32_t)(sym_hash(r) >> (64 - n));
+}
+
+// the bases after position p of the packed stream, one word load per 16
+struct BaseStream {
+  const uint32_t* wp;
+  uint32_t word, q;
+  __device__ __forceinline__ void init(const uint32_t* packed, uint64_t p) {
+    wp = packed + (p >> 4);
+    q = (uint32_t)(p & 15);
+    word = *wp << (2 * q);
+  }
+  __device__ __forceinline__ uint32_t next() {
+    const uint32_t b = word >> 30;
+    word <<= 2;
+    if (++q == 16) {
+      q = 0;
+      word = *++wp;
+    }
+    return b;
+  }
+};
+
 // the input of a run: largest j with input_base[j] <= start; the last answer
 // is kept, as consecutive runs of a slice mostly come from the same input
 struct InputCursor {
@@ -480,10 +515,11 @@ __global__ void __launch_bounds__(DD_THREADS) k_zi_expand_count(ExpandArgs a) {
     const uint32_t nw = (uint32_t)(d & 0xffffffu) + 1u;
     R r;
     roll_set<K, R>(r, a.packed, s0, k);
-    uint64_t p = s0 + (uint64_t)k;
+    BaseStream bs;
+    bs.init(a.packed, s0 + (uint64_t)k);
     for (uint32_t u = 0; u < nw; u++) {
-      if (u > 0) { r.push(base_at(a.packed, p)); p++; }
-      atomicAdd(&c[dd_digit(key_hash(r.canon()), 0, a.bits1)], 1u);
+      if (u > 0) r.push(bs.next());
+      atomicAdd(&c[dd_level1(r, a.bits1)], 1u);
     }
   }
   __syncthreads();
@@ -542,14 +578,15 @@ __global__ void __launch_bounds__(DD_THREADS) k_zi_expand_scatter(ExpandArgs a) 
         const uint16_t ds = (a.with_ids && lng) ? ic.of(a, s0) : 0;
         R r;
         roll_set<K, R>(r, a.packed, s0, k);
-        uint64_t p = s0 + (uint64_t)k;
+        BaseStream bs;
+        bs.init(a.packed, s0 + (uint64_t)k);
         for (uint32_t u = 0; u < nw; u++) {
-          if (u > 0) { r.push(base_at(a.packed, p)); p++; }
-          const K key = r.canon();
-          const uint32_t b = dd_digit(key_hash(key), 0, a.bits1);
+          if (u > 0) r.push(bs.next());
+          const uint32_t b = dd_level1(r, a.bits1);
           if (!lng) {
             atomicAdd(&tcnt[b], 1u);
           } else {
+            const K key = r.canon();
             const uint32_t pos = atomicAdd(&gcur[b], 1u);
             kout[pos] = key;
             if (iout) iout[pos] = ds;
@@ -582,11 +619,12 @@ __global__ void __launch_bounds__(DD_THREADS) k_zi_expand_scatter(ExpandArgs a) 
         const uint16_t ds = a.with_ids ? ic.of(a, s0) : 0;
         R r;
         roll_set<K, R>(r, a.packed, s0, k);
-        uint64_t p = s0 + (uint64_t)k;
+        BaseStream bs;
+        bs.init(a.packed, s0 + (uint64_t)k);
         for (uint32_t u = 0; u < nw; u++) {
-          if (u > 0) { r.push(base_at(a.packed, p)); p++; }
+          if (u > 0) r.push(bs.next());
           const K key = r.canon();
-          const uint32_t b = dd_digit(key_hash(key), 0, a.bits1);
+          const uint32_t b = dd_level1(r, a.bits1);
           const uint32_t pos = atomicAdd(&tcnt[b], 1u);
           skey[pos] = key;
           sid[pos] = ds;
