@@ -200,6 +200,26 @@ struct ProbeArgs {
   uint64_t mf_mask;
 };
 
+// the bases after position p of the packed stream, one word load per 16
+struct BaseStream {
+  const uint32_t* wp;
+  uint32_t word, q;
+  __device__ __forceinline__ void init(const uint32_t* packed, uint64_t p) {
+    wp = packed + (p >> 4);
+    q = (uint32_t)(p & 15);
+    word = *wp << (2 * q);
+  }
+  __device__ __forceinline__ uint32_t next() {
+    const uint32_t b = word >> 30;
+    word <<= 2;
+    if (++q == 16) {
+      q = 0;
+      word = *++wp;
+    }
+    return b;
+  }
+};
+
 template <class K, class R>
 __device__ __forceinline__ void roll_set(R& r, const uint32_t* packed, uint64_t s0, int k) {
   r.init(k);
@@ -299,11 +319,12 @@ __global__ void __launch_bounds__(ZI_THREADS) k_zi_probe(ProbeArgs a) {
         {
           R r;
           roll_set<K, R>(r, a.qpacked, s0 + c0, k);
-          uint64_t p = s0 + c0 + (uint64_t)k;
+          BaseStream bs;
+          bs.init(a.qpacked, s0 + c0 + (uint64_t)k);
 #pragma unroll
           for (int t = 0; t < Q_CHUNK; t++) {
             if (t < (int)cn) {
-              if (t > 0) { r.push(base_at(a.qpacked, p)); p++; }
+              if (t > 0) r.push(bs.next());
               q[t] = r.canon();
             }
           }
@@ -316,9 +337,10 @@ __global__ void __launch_bounds__(ZI_THREADS) k_zi_probe(ProbeArgs a) {
           const uint32_t en = (uint32_t)(e & 0xffffffu) + 1u;
           R r;
           roll_set<K, R>(r, a.ipacked, e0, k);
-          uint64_t p = e0 + (uint64_t)k;
+          BaseStream bs;
+          bs.init(a.ipacked, e0 + (uint64_t)k);
           for (uint32_t u = 0; u < en; u++) {
-            if (u > 0) { r.push(base_at(a.ipacked, p)); p++; }
+            if (u > 0) r.push(bs.next());
             const K ek = r.canon();
 #pragma unroll
             for (int t = 0; t < Q_CHUNK; t++)
@@ -456,25 +478,6 @@ __device__ __forceinline__ uint32_t dd_level1(const Roll128& r, int n) {
   return n == 0 ? 0u : (uint32_t)(sym_hash(r) >> (64 - n));
 }
 
-// the bases after position p of the packed stream, one word load per 16
-struct BaseStream {
-  const uint32_t* wp;
-  uint32_t word, q;
-  __device__ __forceinline__ void init(const uint32_t* packed, uint64_t p) {
-    wp = packed + (p >> 4);
-    q = (uint32_t)(p & 15);
-    word = *wp << (2 * q);
-  }
-  __device__ __forceinline__ uint32_t next() {
-    const uint32_t b = word >> 30;
-    word <<= 2;
-    if (++q == 16) {
-      q = 0;
-      word = *++wp;
-    }
-    return b;
-  }
-};
 
 // the input of a run: largest j with input_base[j] <= start; the last answer
 // is kept, as consecutive runs of a slice mostly come from the same input
