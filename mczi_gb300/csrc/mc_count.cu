@@ -491,6 +491,16 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
     if (b >= (uint32_t)NP1) break;
     const uint64_t lo = a.bucket_off[b], hi = a.bucket_off[b + 1];
     if (hi <= lo) continue;
+    // Descriptors of a batch are loaded ahead of their use: a round's next
+    // batch while the current one's steps run, the next round's first batch
+    // before this round's emission (otherwise every batch starts with the
+    // full latency of its loads in front of a block scan).  pf_base is the
+    // index in desc of the prefetched batch's first descriptor (uniform).
+    uint64_t pf_base = ~0ull, pf_dsc = 0;
+    auto prefetch = [&](uint64_t base) {
+      pf_base = base;
+      pf_dsc = base + (uint64_t)tid < hi ? a.desc[base + (uint64_t)tid] : 0ull;
+    };
 
     // ---- per-bin occupancy and descriptor counts, and the bucket's total
     // windows in 64 bits: every 32-bit counter below (bin occupancy, its
@@ -697,7 +707,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
               uint64_t dsc = 0;
               uint32_t nch = 0;
               if (has) {
-                dsc = a.desc[lo + bb + (uint64_t)tid];
+                dsc = pf_base == lo + bb ? pf_dsc : a.desc[lo + bb + (uint64_t)tid];
                 const uint32_t len = bd_windows(dsc);
                 nch = (len + chunk - 1) / chunk;
                 if (MODE == 1) {
@@ -712,6 +722,8 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
               sh_cpre[tid] = cp;
               if (lane == 0) sh_cpre32[tid >> 5] = cp;
               if (tid == 0) sh_cpre[nth] = total;
+              // the round's next batch is loaded while this one's steps run
+              if (bb + (uint64_t)nth < dhi) prefetch(lo + bb + (uint64_t)nth);
               __syncthreads();
             }
             const int nd = (int)min((uint64_t)nth, dhi - bb);
@@ -933,6 +945,13 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
           }
           __syncthreads();
           continue;
+        }
+        // the next round's first batch (a split sub-round of this range, or
+        // the next planned round), loaded while this round emits
+        {
+          const uint32_t nsp = s_sp;
+          if (nsp > 0) prefetch(lo + dst[stack[nsp - 1].bl]);
+          else if (r + 1 < nrounds) prefetch(lo + dst[rstart[r + 1]]);
         }
         // ---- emit slots with count > threshold.  Each warp counts the
         // emissions of its slots, reserves them with one atomic (whose
