@@ -1523,7 +1523,8 @@ int32_t mczi_zi_build_path(mczi_ctx* ctx, const char* index_path, uint32_t k, ui
   if (!index_path) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "index path must not be NULL");
   std::vector<uint8_t> data;
   std::string e;
-  if (!read_input_file(index_path, &data, &e)) return fail(ctx, MCZI_ERR_IO, e);
+  // (a gzip file whose members carry their sizes stays compressed: decoded on the device)
+  if (!read_input_file(index_path, &data, &e, true)) return fail(ctx, MCZI_ERR_IO, e);
   cudaSetDevice(ctx->device);
   return zi_build(ctx, data.data(), data.size(), k, m);
 }
@@ -1533,7 +1534,7 @@ int32_t mczi_zi_query_paths(mczi_ctx* ctx, const char* const* query_paths, size_
   if (n == 0) return fail(ctx, MCZI_ERR_INVALID_CONFIG, "at least one query FASTA is required");
   std::vector<std::vector<uint8_t>> data;
   std::string e;
-  if (!read_input_files(query_paths, n, &data, &e)) return fail(ctx, MCZI_ERR_IO, e);
+  if (!read_input_files(query_paths, n, &data, &e, true)) return fail(ctx, MCZI_ERR_IO, e);
   std::vector<mczi_input> in(n);
   for (size_t i = 0; i < n; i++) in[i] = mczi_input{data[i].data(), data[i].size()};
   cudaSetDevice(ctx->device);

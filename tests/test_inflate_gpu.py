@@ -159,11 +159,11 @@ def test_count_and_zi_bgzf_paths(gpu_ctx, oracle, tmp_path):
     if head["values"]["data_size"] == 1:  # one-byte counts saturate at x + 1
         exp = {e: min(c, 3) for e, c in exp.items()}
     assert outs[0] == exp
-    # ZI query paths with a BGZF query
+    # ZI build and query paths with BGZF index and query files
     index, query = gen.c4_index_and_query(genome_len=200_000, query_bases=2_000_000, k=31)
-    (tmp_path / "idx.fa").write_bytes(index.tobytes())
+    (tmp_path / "idx.fa.gz").write_bytes(bgzf.compress(index.tobytes()))
     (tmp_path / "q.fa.gz").write_bytes(bgzf.compress(query.tobytes()))
-    assert lib.mczi_zi_build_path(gpu_ctx.handle, str(tmp_path / "idx.fa").encode(), 31, 19) == 0
+    assert lib.mczi_zi_build_path(gpu_ctx.handle, str(tmp_path / "idx.fa.gz").encode(), 31, 19) == 0
     n = C.c_uint64()
     arr = (C.c_char_p * 1)(str(tmp_path / "q.fa.gz").encode())
     rc = lib.mczi_zi_query_paths(gpu_ctx.handle, arr, 1, C.byref(n))
