@@ -74,9 +74,12 @@ int32_t mczi_validate_config(mczi_ctx* ctx, const mczi_counter_config* cfg, int3
 /* count_inputs (src/lib.rs:278) / count_datasets (src/lib.rs:289): counts the
  * canonical k-mers of `inputs` and keeps those with count > threshold.
  * Mode 0 counts occurrences (exact counts); mode 1 counts the inputs
- * (datasets) containing each k-mer (fof, k <= 32).  Inputs that do not start
- * with a FASTA/FASTQ record are skipped with an MC_WARN line, like
- * src/lib.rs:3371-3392.  *n_records receives the number of kept k-mers. */
+ * (datasets) containing each k-mer (fof, k <= 32).  Inputs may be plain or
+ * compressed (gzip, xz, zstd, recognised by their magic bytes): gzip whose
+ * members carry their sizes (BGZF) is decoded on the device, the rest on the
+ * host.  Inputs that do not start with a FASTA/FASTQ record are skipped with
+ * an MC_WARN line, like src/lib.rs:3371-3392.  *n_records receives the number
+ * of kept k-mers. */
 int32_t mczi_count(mczi_ctx* ctx, const mczi_counter_config* cfg, int32_t mode, const mczi_input* inputs,
                    size_t n_inputs, uint64_t* n_records);
 
