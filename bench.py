@@ -853,7 +853,7 @@ def main():
     ap.add_argument("--line-serve-requests", type=int, default=500)
     ap.add_argument("--line-zi-steps", type=int, default=3)
     ap.add_argument("--no-zi", action="store_true", help="MC only: skip the ZI keys of the default line")
-    ap.add_argument("--gzip-scale", type=float, default=0.1,
+    ap.add_argument("--gzip-scale", type=float, default=0.25,
                     help="scale of the long reads for the default line's gzip key (BGZF decoded on the device); "
                          "0 skips it")
     ap.add_argument("--serve-workers", type=int, default=2)
@@ -870,7 +870,7 @@ def main():
         return run_mc_short(args)
     if args.workload == "gzip" and args.impl == "ours":
         # the default line's gzip key alone (BGZF long reads decoded on the device)
-        print(json.dumps(gzip_measure(args.gzip_scale if args.gzip_scale > 0 else 0.1, 3)), flush=True)
+        print(json.dumps(gzip_measure(args.gzip_scale if args.gzip_scale > 0 else 0.25, 3)), flush=True)
         return 0
     if args.warmup < 3 and args.impl == "ours":
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
