@@ -476,6 +476,10 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
   if (MODE == 1) {
     for (int i = tid; i <= a.n_datasets; i += nth) dsbase[i] = a.dataset_base[i];
   }
+  // the table (keys and counts or masks) holds stale slots: true until a
+  // round's emission has cleared every slot it visited, and again after a
+  // round that overflowed (uniform over the CTA)
+  bool table_dirty = true;
 
   for (;;) {
     __syncthreads();
@@ -637,14 +641,18 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
         if (tid == 0) { s_sp--; s_nused = 0; s_over = 0; }
         const uint32_t dlo = dst[rr.bl], dhi = dst[rr.bh];
         if (dhi == dlo) { __syncthreads(); continue; }
-        // clear the table (and the filter bitmap)
-        for (uint32_t i = tid; i < S; i += nth) {
-          keys[i] = EMPTY;
-          if (MODE == 0) cnt[i] = 0;
-          else for (int q = 0; q < W; q++) msk[(size_t)i * W + q] = 0ull;
+        // clear the table unless the last emission left it empty, and the
+        // filter bitmaps (fwords is a multiple of 32 and bmap 16-byte aligned)
+        if (table_dirty) {
+          for (uint32_t i = tid; i < S; i += nth) {
+            keys[i] = EMPTY;
+            if (MODE == 0) cnt[i] = 0;
+            else for (int q = 0; q < W; q++) msk[(size_t)i * W + q] = 0ull;
+          }
         }
-        for (uint32_t i = tid; i < fwords; i += nth) bmap[i] = 0u;
+        for (uint32_t i = tid; i < fwords / 4; i += nth) reinterpret_cast<uint4*>(bmap)[i] = make_uint4(0u, 0u, 0u, 0u);
         __syncthreads();
+        table_dirty = true;
         const bool full_range = (rr.hlo == 0u && rr.hhi == 0xffffffffu);
         uint32_t claimed = 0;  // slots this thread claimed in this round
         // ---- insert.  The round's superkmers are taken in batches of up to
@@ -953,38 +961,55 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
           if (nsp > 0) prefetch(lo + dst[stack[nsp - 1].bl]);
           else if (r + 1 < nrounds) prefetch(lo + dst[rstart[r + 1]]);
         }
-        // ---- emit slots with count > threshold.  Each warp counts the
-        // emissions of its slots, reserves them with one atomic (whose
-        // latency is paid once per warp and round, not once per 32 slots),
-        // then writes them.
+        // ---- emit slots with count > threshold, and empty the table.  A
+        // thread owns slots tid, tid + nth, ... (as in the clear above).  Pass
+        // A tests up to 32 of them, remembers the kept ones in a bit mask and
+        // clears the others; each warp reserves its kept slots with one atomic
+        // (whose latency is paid once per warp and group, not once per 32
+        // slots); pass B writes the kept slots and clears them.
         {
           // the claiming occurrence is implicit except in slow filtered
           // rounds, whose pass 2 counts every occurrence
           const uint32_t implicit = (filtered && !fast) ? 0u : 1u;
-          auto slot_count = [&](uint32_t s, K& key, uint32_t& c) -> bool {
-            if (s >= S) return false;
-            key = keys[s];
-            if (key_eq(key, EMPTY)) return false;
-            c = MODE == 0 ? cnt[s] + implicit : popc_words(&msk[(size_t)s * W], W);
-            return (uint64_t)c > a.threshold;
+          auto slot_count = [&](uint32_t s) -> uint32_t {
+            return MODE == 0 ? cnt[s] + implicit : popc_words(&msk[(size_t)s * W], W);
           };
-          uint32_t mine = 0;  // this warp's emissions (warp-uniform)
-          for (uint32_t base = 0; base < S; base += nth) {
-            K key;
-            uint32_t c;
-            mine += __popc(__ballot_sync(0xffffffffu, slot_count(base + tid, key, c)));
-          }
-          if (mine) {
+          auto slot_clear = [&](uint32_t s) {
+            keys[s] = EMPTY;
+            if (MODE == 0) cnt[s] = 0;
+            else for (int q = 0; q < W; q++) msk[(size_t)s * W + q] = 0ull;
+          };
+          const uint32_t group = 32u * (uint32_t)nth;
+          for (uint32_t g0 = 0; g0 < S; g0 += group) {
+            uint32_t kept = 0;  // bit i: slot g0 + i * nth + tid is emitted
+            for (uint32_t i = 0; i < 32u; i++) {
+              const uint32_t s = g0 + i * (uint32_t)nth + (uint32_t)tid;
+              if (g0 + i * (uint32_t)nth >= S) break;  // uniform
+              if (s < S) {
+                const K key = keys[s];
+                if (!key_eq(key, EMPTY)) {
+                  if ((uint64_t)slot_count(s) > a.threshold) kept |= 1u << i;
+                  else slot_clear(s);
+                }
+              }
+            }
+            // this warp's emissions in the group, and the positions i at
+            // which any of its lanes emits (both warp-uniform)
+            const uint32_t mine = __reduce_add_sync(0xffffffffu, (uint32_t)__popc(kept));
+            if (!mine) continue;
+            uint32_t todo = __reduce_or_sync(0xffffffffu, kept);
             unsigned long long ob = 0;
             if (lane == 0) ob = atomicAdd(a.n_out, (unsigned long long)mine);
             ob = __shfl_sync(0xffffffffu, ob, 0);
-            for (uint32_t base = 0; base < S; base += nth) {
-              const uint32_t s = base + tid;
-              K key = EMPTY;
-              uint32_t c = 0;
-              const bool emit = slot_count(s, key, c);
+            while (todo) {
+              const uint32_t i = (uint32_t)__ffs(todo) - 1u;
+              todo &= todo - 1u;
+              const bool emit = (kept >> i) & 1u;
               const unsigned bal = __ballot_sync(0xffffffffu, emit);
               if (emit) {
+                const uint32_t s = g0 + i * (uint32_t)nth + (uint32_t)tid;
+                const K key = keys[s];
+                const uint32_t c = slot_count(s);
                 const unsigned long long idx = ob + __popc(bal & ((1u << lane) - 1u));
                 if (idx < a.out_cap) {
                   if constexpr (sizeof(K) == 8) {
@@ -999,10 +1024,12 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
                 } else {
                   set_status(a.status, ST_OUT_OVERFLOW);
                 }
+                slot_clear(s);
               }
               ob += __popc(bal);
             }
           }
+          table_dirty = false;
         }
         if (tid == 0) {
           const double frac = ((double)rr.hhi - (double)rr.hlo + 1.0) / 4294967296.0;
