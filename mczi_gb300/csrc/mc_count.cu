@@ -31,6 +31,8 @@ namespace {
 constexpr int MAX_STACK = 48;
 constexpr uint32_t PROBE_LIMIT = 256;
 constexpr int MAX_THREADS = 1024;
+constexpr uint32_t TAIL_PARTS = 4;  // parts of each bucket in the last wave (by p2 bins)
+static_assert(NP2 % TAIL_PARTS == 0, "a part is a whole number of p2 bins");
 
 // exclusive scan of one u32 per thread over the block (<= 1024 threads);
 // `ws` is 32 words of shared scratch.  Ends with a barrier.
@@ -491,8 +493,18 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
       s_rho = rho;
     }
     __syncthreads();
-    const uint32_t b = s_bucket;
-    if (b >= (uint32_t)NP1) break;
+    // Work units: buckets in order, except that the last gridDim.x buckets
+    // are handed out as TAIL_PARTS parts each, part p taking the bucket's p2
+    // bins [p, p + 1) * NP2 / TAIL_PARTS.  Buckets take about equal times,
+    // so whole buckets to the end would leave part of the CTAs idle for up
+    // to one bucket's time while the last wave finishes.
+    const uint32_t tail_from = (uint32_t)NP1 > gridDim.x ? (uint32_t)NP1 - gridDim.x : 0u;
+    const uint32_t unit = s_bucket;
+    if (unit >= tail_from + ((uint32_t)NP1 - tail_from) * TAIL_PARTS) break;
+    const bool whole = unit < tail_from;
+    const uint32_t b = whole ? unit : tail_from + (unit - tail_from) / TAIL_PARTS;
+    const int jlo = whole ? 0 : (int)((unit - tail_from) % TAIL_PARTS) * (NP2 / TAIL_PARTS);
+    const int jhi = whole ? NP2 : jlo + NP2 / TAIL_PARTS;
     const uint64_t lo = a.bucket_off[b], hi = a.bucket_off[b + 1];
     if (hi <= lo) continue;
     // Descriptors of a batch are loaded ahead of their use: a round's next
@@ -579,10 +591,14 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
     if (a.desc_unsorted) {
       // partition pass 2 of this bucket: p2 order into `desc`, the bin starts
       // as cursors (afterwards dst[b] holds the start of bin b + 1)
+      // (a part of a bucket writes only its own bins; every descriptor still
+      // advances its bin's cursor, so the cursors end as in a whole bucket)
       uint64_t* out = const_cast<uint64_t*>(a.desc);
       for (uint64_t i = lo + tid; i < hi; i += nth) {
         const uint64_t bd = src[i];
-        out[lo + atomicAdd(&dst[bd_p2(bd)], 1u)] = bd;
+        const uint32_t bin = bd_p2(bd);
+        const uint32_t at = atomicAdd(&dst[bin], 1u);
+        if ((int)bin >= jlo && (int)bin < jhi) out[lo + at] = bd;
       }
       __syncthreads();
       // shift back by one bin, top chunk first: a chunk reads only entries
@@ -605,11 +621,12 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
     if (tid == 0) s_nrounds = 0;
     __syncthreads();
     {
-      // compaction of round starts, in bin order: warp ballots, chunked
-      for (int base = 0; base < NP2; base += nth) {
+      // compaction of round starts, in bin order: warp ballots, chunked (a
+      // part of a bucket plans its own bins only)
+      for (int base = jlo; base < jhi; base += nth) {
         const int j = base + tid;
         bool st = false;
-        if (j < NP2) st = (j == 0) || (occ[j] / budget != occ[j - 1] / budget);
+        if (j < jhi) st = (j == jlo) || (occ[j] / budget != occ[j - 1] / budget);
         const unsigned bal = __ballot_sync(0xffffffffu, st);
         if (lane == 0) warp_tmp[tid >> 5] = __popc(bal);
         __syncthreads();
@@ -629,7 +646,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
       __syncthreads();
       if (tid == 0) {
         const uint32_t bl = rstart[r];
-        const uint32_t bh = (r + 1 < nrounds) ? rstart[r + 1] : (uint32_t)NP2;
+        const uint32_t bh = (r + 1 < nrounds) ? rstart[r + 1] : (uint32_t)jhi;
         stack[0] = RoundRange{bl, bh, 0u, 0xffffffffu};
         s_sp = 1;
       }
@@ -1032,8 +1049,11 @@ __global__ void __launch_bounds__(MAX_THREADS, 1) k_count(CountArgs a) {
           table_dirty = false;
         }
         if (tid == 0) {
-          const double frac = ((double)rr.hhi - (double)rr.hlo + 1.0) / 4294967296.0;
-          atomicAdd(&a.stats[0], (unsigned long long)((double)(occ[rr.bh] - occ[rr.bl]) * frac));
+          // the round's windows times the share of the key hash range it
+          // covered (span / 2^32; integer arithmetic: FP64 is slow here and
+          // the whole CTA waits for this thread at the next barrier)
+          const uint64_t span = (uint64_t)(rr.hhi - rr.hlo) + 1ull;  // <= 2^32
+          atomicAdd(&a.stats[0], (unsigned long long)(((uint64_t)(occ[rr.bh] - occ[rr.bl]) * span) >> 32));
           atomicAdd(&a.stats[1], (unsigned long long)s_nused);
           atomicAdd(&a.stats[2], 1ull);
         }
