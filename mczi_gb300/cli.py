@@ -84,7 +84,7 @@ def mczi_main(argv: list[str]) -> None:
     from . import mczi
     a = _mczi_parser().parse_args(argv)
     if a.reform_output:
-        raise N.MCZIError(N.MCZI_ERR_INVALID_CONFIG, "--reform-output (the R reformer) is not available in this build")
+        raise N.MCZIError(N.MCZI_ERR_INVALID_CONFIG, "--reform-output (the R unitig reformer) is not part of this library")
     if a.threads is not None and a.threads <= 0:
         raise N.MCZIError(N.MCZI_ERR_INVALID_CONFIG, "--threads must be greater than 0")
     index_inputs = mc.expand_fofns(a.index_input) if a.index_fofn else list(a.index_input)
