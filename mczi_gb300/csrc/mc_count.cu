@@ -6,18 +6,19 @@
 // (src/lib.rs:2400-2425, 3589-3614) and the fof per-dataset dedup + presence
 // table (src/lib.rs:2213-2247, 4450-4522).
 //
-// A persistent CTA takes p1 buckets from a work counter.  For each bucket it
-// histograms the window occupancy of the 4096 p2 bins, cuts the bins into
-// rounds whose expected number of distinct k-mers fits the shared-memory
+// A persistent CTA takes p1 buckets (4096) from a work counter; the last
+// wave of buckets is handed out in parts by p2 bins.  For each bucket (or
+// part) it histograms the window occupancy of the 2048 p2 bins, cuts its bins
+// into rounds whose expected number of stored k-mers fits the shared-memory
 // table (expected = occupancy x the distinct/occurrence ratio measured so far
-// across the grid), and for every round: clears the table, regenerates the
+// across the grid, at the target fill), and for every round: regenerates the
 // canonical k-mers of the round's superkmers on chip (the k-mers never touch
 // HBM), inserts them with shared-memory CAS, and emits the slots whose count
-// passes the threshold.  A round whose table fills past 85 % is abandoned and
-// split -- by bins while it spans several, then by k-mer hash range -- so the
-// result never depends on the estimate.  Every k-mer of a bucket lands in
-// exactly one round because the p2 bin and the hash range are functions of
-// the canonical k-mer.
+// passes the threshold, leaving the table empty.  A round in which a probe
+// run exceeds PROBE_LIMIT slots is abandoned and split -- by bins while it
+// spans several, then by k-mer hash range -- so the result never depends on
+// the estimate.  Every k-mer of a bucket lands in exactly one round because
+// the p2 bin and the hash range are functions of the canonical k-mer.
 //
 // Presence mode (fof): the table holds a bitmask of datasets per k-mer; the
 // dataset of a superkmer is found from its base offset.  count = popcount.
