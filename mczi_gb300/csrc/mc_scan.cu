@@ -4,10 +4,12 @@
 // visitor (src/lib.rs:3694-3789; vendor/simd-minimizers-2.3.1/src/
 // minimizers.rs:259-291, sliding_min.rs:556-593, collect.rs:116-286).
 //
-// Order: every m-mer is hashed as H(min(fwd, rc)); a window's minimizer value
-// is the minimum of the w = k - m + 1 hashes it contains.  Both strands of a
-// k-mer contain the same canonical m-mers, so the minimizer value -- and the
-// partition derived from it -- is a function of the canonical k-mer alone,
+// Order: an m-mer's value is min(H(fwd), H(rc)) for m <= 32 (H multiplicative,
+// see mmer_hash64) and H of a mix of its canonical value for m > 32 -- either
+// way the same for both strands; a window's minimizer value is the minimum of
+// the w = k - m + 1 values it contains.  Both strands of a k-mer contain the
+// same m-mers up to strand, so the minimizer value -- and the partition
+// derived from it -- is a function of the canonical k-mer alone,
 // which is the invariant MC's counting relies on (each k-mer occurrence lands
 // in the partition of its canonical form).  A superkmer is a maximal run of
 // consecutive valid windows with the same minimizer value, cut at tile edges.

@@ -189,12 +189,12 @@ __host__ __device__ __forceinline__ uint64_t bd_start(uint64_t bd) { return bd >
 __host__ __device__ __forceinline__ uint32_t bd_windows(uint64_t bd) { return (uint32_t)((bd >> 11) & 0xfffu) + 1u; }
 __host__ __device__ __forceinline__ uint32_t bd_p2(uint64_t bd) { return (uint32_t)(bd & 0x7ffu); }
 
-// canonical m-mer hash: the minimizer order (strand-symmetric by
-// construction).  Multiplicative hashing (Knuth): the top half of the 64-bit
-// product with an odd constant, one multiply and no shifts of the integer
-// pipe, which bounds the scan.
-__device__ __forceinline__ uint32_t mmer_hash64(uint64_t canon) {
-  return (uint32_t)((canon * 0x9E3779B97F4A7C15ull) >> 32);
+// m-mer hash of the minimizer order, multiplicative (Knuth): the top half of
+// the 64-bit product with an odd constant, one multiply and no shifts of the
+// integer pipe, which bounds the scan.  The scan applies it to both strands of
+// an m-mer and keeps the smaller, so the order is strand-symmetric.
+__device__ __forceinline__ uint32_t mmer_hash64(uint64_t v) {
+  return (uint32_t)((v * 0x9E3779B97F4A7C15ull) >> 32);
 }
 
 }  // namespace mczi
