@@ -13,6 +13,9 @@
 // Concatenated members (multi-member gzip, several xz streams, several zstd
 // frames) decode in sequence, as flate2's MultiGzDecoder and liblzma's
 // LZMA_CONCATENATED do.  Several input files decode on parallel host threads.
+// A gzip file whose members all carry their compressed size (BGZF) can
+// instead be returned as it is (keep_sized_gzip) and decoded on the device
+// (inflate.cu); the path-based entry points do that.
 #include "host_io.h"
 #include "../../include/mczi_gpu.h"
 

@@ -1,8 +1,13 @@
 // host_io.cpp -- host-side output writers for libmczi_gpu.
 //
-// The reference keeps output formatting on the host (src/lib.rs:1190-1676),
-// and so does this library: the device produces (canonical k-mer, count)
-// records, the host serialises them.
+// The reference formats its outputs on the host (src/lib.rs:1190-1676).
+// Here the device produces the (canonical k-mer, count) records and, for KFF,
+// also formats them as the file stores them (k_kff_records in mczi_api.cu);
+// the host writes the KFF header, the values section and the raw section's
+// header before those bytes and the trailer after them (write_kff_records),
+// walks the simplitigs over the device's extension table
+// (write_simplitig_walk), and keeps a self-contained simplitig writer for
+// records already on the host (write_simplitig_file).
 #include "host_io.h"
 
 #include <algorithm>
