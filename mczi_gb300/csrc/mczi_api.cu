@@ -4,6 +4,8 @@
 // The MC pipeline on one GPU (all intermediate data stays in HBM; the
 // reference round-trips it through temporary partition files):
 //   stage   : inputs -> HBM, each at a PACK_TILE-aligned offset
+//   K0 gz   : (BGZF inputs, copied compressed) members decoded in HBM into
+//             their staged places (inflate.cu)
 //   K1 pack : bytes -> 2-bit packed stream + fragment-start bits
 //   K2 scan : minimizer scan -> superkmer descriptors + partition keys
 //   K4 pre  : (optional) pass-1 minimizer table and superkmer filter

@@ -8,8 +8,12 @@ library (``src/lib.rs``): ``CounterConfig`` (:48-53), ``CountedKmer`` (:63-66),
 (:442), ``expand_fofns`` (:242-276), ``decode_kmer`` (:3056-3069).
 
 All counting runs in ``libmczi_gpu.so`` on the GPU; this module only moves
-bytes and records across the C ABI.  Compressed inputs (.gz, .xz) are
-decompressed on the host before they are handed over, as MC's readers do.
+bytes and records across the C ABI.  Input files given by path are read with
+the library's readers (``read_input``): plain, gzip, xz or zstd, decoded on
+host threads, as MC's readers decode them.  Compressed bytes handed to
+``Context.count`` directly, and the C ABI's path entry points, decode BGZF
+gzip on the device instead (``Context.inflate_gzip`` decodes such a buffer
+alone).
 """
 from __future__ import annotations
 

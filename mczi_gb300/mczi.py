@@ -2,8 +2,10 @@
 
 Follows the reference's MCZI run (src/mczi.rs:238-454): the index inputs are
 counted by MC with (k, m, x); the kept canonical k-mers become the
-dictionary's sequences (written as MC simplitigs, as the reference feeds MC's
-k-mer set to its SSHash build); the query inputs are subtracted; the absent
+dictionary's sequences on the device, each k-mer its own sequence
+(``mczi_zi_build_from_result``; the reference writes MC's k-mer set to FASTA
+and compacts it before its SSHash build: the k-mer set is the same); the
+query inputs are subtracted; the absent
 k-mers are written as simplitig FASTA, one file for all queries or, with
 ``query_fofn``, one per query file named ``<stem>.<suffix><ext>`` beside it or
 in the output folder (src/mczi.rs:770-871).  The index stays on the device
