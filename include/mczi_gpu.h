@@ -49,7 +49,11 @@ typedef struct {
   uint32_t partition_count;
 } mczi_counter_config;
 
-/* One FASTA/FASTQ input held in host memory (already decompressed). */
+/* One FASTA/FASTQ input held in host memory.  The entry points that take an
+ * array of them (mczi_count, mczi_stage, mczi_route_superkmers, mczi_zi_query,
+ * mczi_zi_query_per_input) accept each plain or compressed (gzip, xz, zstd,
+ * recognised by their magic bytes): BGZF gzip is decoded on the device, the
+ * rest on the host. */
 typedef struct {
   const uint8_t* data;
   uint64_t len;
