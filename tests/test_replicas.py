@@ -62,3 +62,32 @@ def test_reference_arm_prints_on_rank_zero_only():
     r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1",
                         "--warmup", "1"], cwd=ROOT, env=env, capture_output=True, text=True, timeout=120)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_reference_arm_line_on_rank_zero():
+    """Rank 0 (or a plain run) of the reference arm times the CPU
+    restatement on a sample of the headline workload and prints one JSON line
+    with the keys the benchmark line carries: the same metric and unit as the
+    GPU arm, the sample's scale and bases in `config`, a `cpu_baseline`
+    describing this run and an `e2e` with no host-device copies."""
+    import json
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "LOCAL_RANK", "WORLD_SIZE")}
+    scale = 0.0005  # 2 Mbp of the 4 Gbp long-read workload
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "2",
+                        "--warmup", "1", "--ref-sample-scale", str(scale)], cwd=ROOT, env=env,
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    assert (d["metric"], d["unit"], d["higher_is_better"]) == ("MC Gbases/s", "Gbases/s", True)
+    assert (d["steps"], d["warmup"], d["n_gpus"]) == (2, 1, 1)
+    assert d["value"] > 0
+    cfg = d["config"]
+    assert cfg["workload"] == "mc_abundance_long_reads_4gbp_k63" and (cfg["k"], cfg["m"], cfg["x"]) == (63, 21, 3)
+    assert cfg["scale"] == scale and cfg["bases"] == int(4_000_000_000 * scale)
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["unit"] == d["unit"] and cb["kind"] == "port" and cb["cores"] >= 1
+    assert f"scale {scale}" in cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
