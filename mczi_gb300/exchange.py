@@ -16,6 +16,14 @@ communication:
 5. gather (optional): the union of the ranks' records is the single-GPU
    result, record for record.
 
+fof (presence) mode is the same plan with the dataset carried beside the
+records: every rank takes a share of every dataset, routes each dataset's
+share on its own, and the exchange sends a table of group sizes per
+(destination, dataset) with the bytes, so the receiver rebuilds one input
+per dataset and counts them in presence mode (``count_datasets_sharded``).
+A k-mer's occurrences in one dataset all reach the same rank, so its
+presence count there is its number of datasets, as on one GPU.
+
 The exchange works over any ``torch.distributed`` process group: NCCL on
 GPUs, gloo on the CPU (the tests run the plan with two gloo ranks and a CPU
 stand-in for the routing step).
@@ -110,6 +118,72 @@ def count_sharded(share: Sequence, config, group=None, ctx=None,
     groups = route(share, world)
     received = [b for b in all_to_all_bytes(groups, group) if b.size]
     if not received:  # none of this rank's buckets occurs
+        e = np.empty(0, dtype=np.uint64)
+        return e, (e if config.k > 32 else None), e
+    return count(received)
+
+
+def _empty_groups(world: int) -> list[np.ndarray]:
+    return [np.empty(0, dtype=np.uint8) for _ in range(world)]
+
+
+def all_to_all_datasets(groups: Sequence[Sequence[np.ndarray]], group=None) -> list[np.ndarray]:
+    """Step 3 in fof mode: groups[i][d] holds dataset i's records for rank d.
+    One exchange of the size table (per destination, one size per dataset)
+    and one of the bytes; returns, per dataset, the records this rank
+    received from all ranks, concatenated."""
+    import torch
+    import torch.distributed as dist
+    world = dist.get_world_size(group)
+    n = len(groups)
+    backend = dist.get_backend(group)
+    dev = torch.device("cuda", torch.cuda.current_device()) if backend == "nccl" else torch.device("cpu")
+    table = np.array([[int(groups[i][d].size) for i in range(n)] for d in range(world)], dtype=np.int64)
+    send_tab = torch.from_numpy(table.reshape(-1).copy()).to(dev)
+    recv_tab = torch.empty(world * n, dtype=torch.int64, device=dev)
+    dist.all_to_all_single(recv_tab, send_tab, group=group)  # n sizes to and from every rank
+    rtab = recv_tab.cpu().numpy().reshape(world, n)
+    ss = [int(v) for v in table.sum(axis=1)]
+    rs = [int(v) for v in rtab.sum(axis=1)]
+    parts = [np.asarray(groups[i][d], dtype=np.uint8) for d in range(world) for i in range(n)]
+    payload = np.concatenate(parts) if sum(ss) else np.empty(0, np.uint8)
+    send = torch.from_numpy(payload).to(dev)
+    recv = torch.empty(sum(rs), dtype=torch.uint8, device=dev)
+    dist.all_to_all_single(recv, send, output_split_sizes=rs, input_split_sizes=ss, group=group)
+    r = recv.cpu().numpy()
+    per = [[] for _ in range(n)]
+    off = 0
+    for src in range(world):
+        for i in range(n):
+            ln = int(rtab[src, i])
+            if ln:
+                per[i].append(r[off:off + ln])
+            off += ln
+    return [np.concatenate(p) if p else np.empty(0, np.uint8) for p in per]
+
+
+def count_datasets_sharded(shares: Sequence[Sequence], config, group=None, ctx=None,
+                           route: Callable | None = None, count: Callable | None = None):
+    """fof mode, steps 2-4 on this rank: shares[i] is this rank's share of
+    dataset i (a list of buffers, possibly empty).  Each dataset's share is
+    routed on its own; after the exchange this rank counts, in presence mode,
+    one input per dataset that sent it records (a dataset with none here
+    holds none of this rank's k-mers, so leaving it out changes no count).
+    Returns (lo, hi, counts) of this rank's buckets (hi None for k <= 32).
+    `route(share, world)` and `count(received_datasets)` replace the GPU
+    steps (the CPU tests pass stand-ins)."""
+    import torch.distributed as dist
+    world = dist.get_world_size(group)
+    if route is None:
+        route = lambda s, w: route_superkmers(ctx, s, config, w)  # noqa: E731
+    if count is None:
+        def count(received):
+            n = ctx.count(received, config, N.MODE_PRESENCE)
+            r = ctx.records(n, sorted=True)
+            return r.lo, r.hi, r.count
+    groups = [route(list(share), world) if sum(len(b) for b in share) else _empty_groups(world) for share in shares]
+    received = [b for b in all_to_all_datasets(groups, group) if b.size]
+    if not received:
         e = np.empty(0, dtype=np.uint64)
         return e, (e if config.k > 32 else None), e
     return count(received)

@@ -97,6 +97,68 @@ def test_exchange_plan_two_gloo_ranks(tmp_path, oracle):
     assert all(v > 0 for v in n) and sum(n) == lo.size
 
 
+def _datasets(n=4):
+    """fof inputs: n read samples of one genome (presence counts up to n)."""
+    rng = np.random.default_rng(11)
+    g = rng.choice(np.frombuffer(b"ACGT", dtype=np.uint8), size=1500)
+    out = []
+    for d in range(n):
+        recs = []
+        for i in range(60 + 20 * d):
+            a = int(rng.integers(0, 1400))
+            s = g[a:a + int(rng.integers(20, 120))].copy()
+            if rng.random() < 0.5:
+                s = np.frombuffer(bytes(s)[::-1].translate(bytes.maketrans(b"ACGT", b"TGCA")), dtype=np.uint8)
+            recs.append(b">d%dr%d\n" % (d, i) + s.tobytes() + b"\n")
+        out.append(b"".join(recs))
+    return out
+
+
+def _fof_rank_main(rank: int, world: int, port: int, out_dir: str) -> None:
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    sys.path.insert(0, str(ROOT))
+    sys.path.insert(0, str(ROOT / "tests"))
+    import torch.distributed as dist
+    import oracle_ref
+    from mczi_gb300 import exchange
+    from mczi_gb300.mc import CounterConfig
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    # every rank takes a share of every dataset; rank 1's share of the last
+    # dataset is empty (a dataset need not reach every rank)
+    shares = [[exchange.split_records(ds, world)[rank]] for ds in _datasets()]
+    if rank == 1:
+        shares[-1] = []
+    if rank == 0:
+        shares[-1] = [_datasets()[-1]]
+    lo, hi, cnt = exchange.count_datasets_sharded(
+        shares, CounterConfig(K, 7, X), route=cpu_route,
+        count=lambda received: (lambda r: (r[0], None, r[2]))(oracle_ref.count(received, K, X, 1)))
+    got = exchange.gather_records(lo, hi, cnt)
+    if rank == 0:
+        np.save(Path(out_dir, "lo.npy"), got[0])
+        np.save(Path(out_dir, "cnt.npy"), got[2])
+    Path(out_dir, f"n{rank}").write_text(str(lo.size))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_fof_exchange_plan_two_gloo_ranks(tmp_path, oracle):
+    """fof mode: datasets split over two ranks, each dataset routed on its
+    own, sizes per (destination, dataset) exchanged with the bytes, presence
+    counted per rank; the union equals the oracle's presence count of the
+    whole datasets."""
+    torch = pytest.importorskip("torch")
+    world, port = 2, _free_port()
+    torch.multiprocessing.start_processes(_fof_rank_main, args=(world, port, str(tmp_path)), nprocs=world,
+                                          start_method="spawn")
+    lo, hi, cnt = oracle.count(_datasets(), K, X, 1)
+    assert lo.size > 0 and int(cnt.max()) == 4  # k-mers in every dataset are kept
+    assert np.array_equal(np.load(tmp_path / "lo.npy"), lo)
+    assert np.array_equal(np.load(tmp_path / "cnt.npy"), cnt)
+    n = [int((tmp_path / f"n{r}").read_text()) for r in range(world)]
+    assert all(v > 0 for v in n) and sum(n) == lo.size
+
+
 def test_split_records_cuts_at_record_starts():
     from mczi_gb300 import exchange
     fa = _reads(7, 50)

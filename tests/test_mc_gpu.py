@@ -493,3 +493,34 @@ def test_route_superkmers_union_equals_single(gpu_ctx, oracle):
         assert np.array_equal(lo[order], olo) and np.array_equal(cnt[order], ocnt), k
         if k > 32:
             assert np.array_equal(hi[order], ohi)
+
+
+def test_route_datasets_presence_union_equals_single(gpu_ctx, oracle):
+    """fof mode of the multi-GPU plan on one GPU: every dataset split in
+    three shares, each share routed to three destinations on its own; every
+    destination counts, in presence mode, one input per dataset that sent it
+    records; the union of the three results equals the oracle's presence
+    count of the whole datasets, record for record."""
+    from mczi_gb300 import exchange, gen
+    from mczi_gb300.mc import CounterConfig
+    datasets = gen.c3_datasets(n_datasets=6, genome_len=200_000, coverage=(2.0, 6.0))
+    k, m, x, world = 31, 21, 2, 3
+    cfg = CounterConfig(k, m, x)
+    received = [[[] for _ in datasets] for _ in range(world)]  # [destination][dataset]
+    for i, ds in enumerate(datasets):
+        for share in exchange.split_records(ds, world):
+            for d, g in enumerate(exchange.route_superkmers(gpu_ctx, [share], cfg, world)):
+                if g.size:
+                    received[d][i].append(g)
+    los, cnts = [], []
+    for d in range(world):
+        inputs = [np.concatenate(p) for p in received[d] if p]
+        assert len(inputs) == len(datasets), d  # every dataset reaches every destination here
+        n = gpu_ctx.count(inputs, cfg, 1)
+        r = gpu_ctx.records(n, sorted=True)
+        los.append(r.lo)
+        cnts.append(r.count)
+    lo, cnt = np.concatenate(los), np.concatenate(cnts)
+    order = np.argsort(lo, kind="stable")
+    olo, _, ocnt = oracle.count(datasets, k, x, 1)
+    assert olo.size > 0 and np.array_equal(lo[order], olo) and np.array_equal(cnt[order], ocnt)
