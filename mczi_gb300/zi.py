@@ -81,6 +81,38 @@ def collect_query_kmers_absent_from_index(ctx: Context, queries: Sequence) -> Re
     return ctx.records(n, sorted=True)
 
 
+def collect_absent_sharded(ctx: Context | None, queries: Sequence, group=None, absent=None):
+    """ZI on several GPUs, one process per GPU.  Every rank holds the same
+    dictionary (each builds it from the same index: ZI's index is small, so
+    it is replicated, not split) and takes a share of every query, cut at
+    record boundaries; the ranks' absent sets are gathered and merged at rank
+    0, the only collective.  Whether a k-mer is absent does not depend on the
+    other queries, so the merged set is the single-GPU result.  Returns the
+    sorted distinct (lo, hi) at rank 0 (hi None for k <= 32), None elsewhere.
+    `absent(share)` -> (lo, hi) replaces the GPU query (the CPU tests pass a
+    stand-in)."""
+    import torch.distributed as dist
+    from .exchange import split_records
+    world, rank = dist.get_world_size(group), dist.get_rank(group)
+    share = [s for s in (split_records(_bytes(q), world)[rank] for q in queries) if s.size]
+    if absent is None:
+        def absent(qs):
+            r = collect_query_kmers_absent_from_index(ctx, qs)
+            return r.lo, r.hi
+    lo, hi = absent(share) if share else (np.empty(0, dtype=np.uint64), None)
+    parts = [None] * world
+    dist.all_gather_object(parts, (np.asarray(lo, dtype=np.uint64), hi), group=group)
+    if rank != 0:
+        return None
+    lo = np.concatenate([p[0] for p in parts])
+    if all(p[1] is None for p in parts):
+        return np.unique(lo), None
+    hi = np.concatenate([np.asarray(p[1], dtype=np.uint64) if p[1] is not None else np.zeros(p[0].size, np.uint64)
+                         for p in parts])
+    u = np.unique(np.stack([hi, lo], axis=1), axis=0)  # sorted by (hi, lo), duplicates removed
+    return np.ascontiguousarray(u[:, 1]), np.ascontiguousarray(u[:, 0])
+
+
 def query_per_input(ctx: Context, queries: Sequence) -> int:
     """One batch of independent requests; returns the number of records."""
     data = [_bytes(q) for q in queries]

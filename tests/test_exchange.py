@@ -1,5 +1,7 @@
-"""MC counting on several GPUs (mczi_gb300/exchange.py): the exchange plan
-on two gloo ranks on the CPU, and the record split.
+"""Several GPUs: MC counting's exchange plan (mczi_gb300/exchange.py, in
+abundance and fof presence mode) and ZI's sharded queries
+(mczi_gb300/zi.py::collect_absent_sharded) on two gloo ranks on the CPU, and
+the record split.
 
 The GPU routing step (mczi_route_superkmers) is replaced here by a CPU
 stand-in with the property the plan relies on: every window goes to the rank
@@ -157,6 +159,70 @@ def test_fof_exchange_plan_two_gloo_ranks(tmp_path, oracle):
     assert np.array_equal(np.load(tmp_path / "cnt.npy"), cnt)
     n = [int((tmp_path / f"n{r}").read_text()) for r in range(world)]
     assert all(v > 0 for v in n) and sum(n) == lo.size
+
+
+def _zi_inputs():
+    """A ZI index (one genome) and three query sets: reads of the genome and
+    of foreign sequence, some with an N."""
+    rng = np.random.default_rng(21)
+    acgt = np.frombuffer(b"ACGT", dtype=np.uint8)
+    g = rng.choice(acgt, size=4000)
+    foreign = rng.choice(acgt, size=600)  # absent k-mers that recur across records and ranks
+    index = b">idx\n" + g.tobytes() + b"\n"
+    queries = []
+    for q in range(3):
+        recs = []
+        for i in range(50 + 30 * q):
+            src = g if rng.random() < 0.7 else foreign
+            a = int(rng.integers(0, src.size - 150))
+            s = src[a:a + int(rng.integers(30, 150))].copy()
+            if rng.random() < 0.2:
+                s[int(rng.integers(0, s.size))] = ord("N")
+            recs.append(b">q%dr%d\n" % (q, i) + s.tobytes() + b"\n")
+        queries.append(b"".join(recs))
+    return index, queries
+
+
+def _zi_rank_main(rank: int, world: int, port: int, out_dir: str) -> None:
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    sys.path.insert(0, str(ROOT))
+    sys.path.insert(0, str(ROOT / "tests"))
+    import torch.distributed as dist
+    import oracle_ref
+    from mczi_gb300 import zi
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    index, queries = _zi_inputs()
+    for k in (15, 41):
+        def absent(share):
+            lo, hi = oracle_ref.zi_absent(index, share, k)
+            Path(out_dir, f"n{k}_{rank}").write_text(str(lo.size))
+            return lo, hi
+        got = zi.collect_absent_sharded(None, queries, absent=absent)
+        if rank == 0:
+            np.save(Path(out_dir, f"lo{k}.npy"), got[0])
+            np.save(Path(out_dir, f"hi{k}.npy"), got[1])
+        else:
+            assert got is None
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_zi_sharded_queries_two_gloo_ranks(tmp_path, oracle):
+    """ZI on several GPUs: the index replicated, every query split over two
+    ranks, the absent sets gathered and merged at rank 0; the merged set
+    equals the oracle's absent set of the whole queries (k = 15 and 41)."""
+    torch = pytest.importorskip("torch")
+    world, port = 2, _free_port()
+    torch.multiprocessing.start_processes(_zi_rank_main, args=(world, port, str(tmp_path)), nprocs=world,
+                                          start_method="spawn")
+    index, queries = _zi_inputs()
+    for k in (15, 41):
+        lo, hi = oracle.zi_absent(index, queries, k)
+        assert lo.size > 0
+        # the ranks' sets overlap, so the merge has duplicates to remove
+        assert sum(int((tmp_path / f"n{k}_{r}").read_text()) for r in range(world)) > lo.size, k
+        assert np.array_equal(np.load(tmp_path / f"lo{k}.npy"), lo), k
+        assert np.array_equal(np.load(tmp_path / f"hi{k}.npy"), hi), k
 
 
 def test_split_records_cuts_at_record_starts():
