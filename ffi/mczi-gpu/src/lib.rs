@@ -4,6 +4,7 @@
 //! * `count_inputs` (src/lib.rs:278), `count_datasets` (:289),
 //! * `count_inputs_to_fasta_path` (:427), `count_datasets_to_fasta_path` (:442),
 //! * `count_inputs_to_kff_path` (:457), `count_datasets_to_kff_path` (:509),
+//! * `count_inputs_to_kmer_fasta_path` (:306), `count_datasets_to_kmer_fasta_path` (:357),
 //! * `build_dictionary` (src/zi.rs:114),
 //! * `collect_query_kmers_absent_from_index` (src/zi.rs:152)
 //!
@@ -200,6 +201,41 @@ pub fn count_inputs_to_kff_path(inputs: &[PathBuf], config: CounterConfig, outpu
 
 pub fn count_datasets_to_kff_path(inputs: &[PathBuf], config: CounterConfig, output_path: &Path) -> Result<()> {
     with_gpu(|g| g.count_paths(inputs, config, output_path, true, true))
+}
+
+/// The selected-k-mer FASTA (src/lib.rs:306-311): every kept k-mer as
+/// ">MC_kmer_<i> count=<c>" and its bases, in ascending `encoded` order;
+/// returns the number written.  The `_with_stats` / `_silent_stats` forms
+/// (:314-425, MCZI's index step at src/mczi.rs:340-344) keep their phase
+/// bookkeeping and take `selected_kmers` from here.
+pub fn count_inputs_to_kmer_fasta_path(inputs: &[PathBuf], config: CounterConfig, output_path: &Path) -> Result<u64> {
+    write_kmer_fasta(&count_inputs(inputs, config)?, config.k, output_path)
+}
+
+/// count_datasets_to_kmer_fasta_path (src/lib.rs:357-363): as above with the
+/// number of datasets containing each k-mer as its count.
+pub fn count_datasets_to_kmer_fasta_path(inputs: &[PathBuf], config: CounterConfig, output_path: &Path) -> Result<u64> {
+    write_kmer_fasta(&count_datasets(inputs, config)?, config.k, output_path)
+}
+
+fn write_kmer_fasta(records: &[CountedKmer], k: usize, output: &Path) -> Result<u64> {
+    let out = c_path(output)?;
+    let lo: Vec<u64> = records.iter().map(|r| r.encoded as u64).collect();
+    let hi: Vec<u64> = records.iter().map(|r| (r.encoded >> 64) as u64).collect();
+    let cnt: Vec<u64> = records.iter().map(|r| r.count).collect();
+    let mut err = vec![0 as c_char; 1024];
+    let rc = unsafe {
+        sys::mczi_write_kmer_fasta(out.as_ptr(), lo.as_ptr(), hi.as_ptr(), cnt.as_ptr(), lo.len() as u64,
+                                   u32::try_from(k).unwrap_or(u32::MAX), err.as_mut_ptr(), err.len() as u64)
+    };
+    if rc != sys::MCZI_OK {
+        let msg = unsafe { CStr::from_ptr(err.as_ptr()) }.to_string_lossy().into_owned();
+        if msg.is_empty() {
+            bail!("libmczi_gpu failed with status {rc}");
+        }
+        bail!(msg);
+    }
+    Ok(records.len() as u64)
 }
 
 /// ZI's dictionary, resident on the device in its own context.

@@ -298,6 +298,20 @@ int32_t mczi_set_zi_bucket_records(mczi_ctx* ctx, uint32_t records);
 int32_t mczi_read_input_file(const char* path, uint8_t** data, uint64_t* len, char* err, uint64_t err_cap);
 void mczi_free_input(uint8_t* data);
 
+/* The selected-k-mer FASTA of count_inputs_to_kmer_fasta_path /
+ * count_datasets_to_kmer_fasta_path (src/lib.rs:306-425, records as
+ * write_kmer_fasta_record_u128, src/lib.rs:1535-1544; MCZI writes its index
+ * set this way, src/mczi.rs:340-344): record i (from 1) is
+ * ">MC_kmer_<i> count=<counts[i-1]>" followed by the k-mer's k bases on one
+ * line (MSB-first, A0 C1 G2 T3; 1 <= k <= 64).  Host memory only, no
+ * context: pass the records copied with mczi_result_copy (sorted = 1 gives
+ * ascending encoded order; the reference writes them in its partition
+ * order).  key_hi may be NULL for k <= 32.  Returns MCZI_ERR_IO with the
+ * message in err (err_cap bytes, may be NULL) when the file cannot be
+ * written. */
+int32_t mczi_write_kmer_fasta(const char* path, const uint64_t* key_lo, const uint64_t* key_hi,
+                              const uint64_t* counts, uint64_t n, uint32_t k, char* err, uint64_t err_cap);
+
 /* Decodes on the device a gzip buffer whose members carry their sizes (BGZF:
  * the "BC" extra subfield), one warp per member, each member checked against
  * its ISIZE and CRC-32, and copies the bytes to out (cap bytes; *n_out gets

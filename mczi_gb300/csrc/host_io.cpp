@@ -10,6 +10,8 @@
 // records already on the host (write_simplitig_file).
 #include "host_io.h"
 
+#include "../../include/mczi_gpu.h"
+
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -178,6 +180,32 @@ bool write_kff_records(const std::string& path, int k, int m, uint64_t x, int co
   return true;
 }
 
+bool write_kmer_fasta(const std::string& path, const uint64_t* lo, const uint64_t* hi, const uint64_t* count,
+                      uint64_t n, int k, std::string* err) {
+  File o(path);
+  if (!o.f) {
+    *err = "failed to create " + path;
+    return false;
+  }
+  static const char B[4] = {'A', 'C', 'G', 'T'};
+  char line[64];
+  char seq[72];
+  for (uint64_t i = 0; i < n; i++) {
+    const int l = std::snprintf(line, sizeof line, ">MC_kmer_%llu count=%llu\n", (unsigned long long)(i + 1),
+                                (unsigned long long)count[i]);
+    o.put(line, (size_t)l);
+    const u128 key = ((u128)(hi ? hi[i] : 0) << 64) | lo[i];
+    for (int j = 0; j < k; j++) seq[j] = B[(int)((key >> (2 * (k - 1 - j))) & 3)];
+    seq[k] = '\n';
+    o.put(seq, (size_t)k + 1);
+  }
+  if (!o.close()) {
+    *err = "failed to write " + path;
+    return false;
+  }
+  return true;
+}
+
 bool write_simplitig_file(const std::string& path, const HostRecords& r, int k, std::string* err) {
   File o(path);
   if (!o.f) {
@@ -334,3 +362,14 @@ bool read_file(const std::string& path, std::vector<uint8_t>* out, std::string* 
 }
 
 }  // namespace mczi
+
+extern "C" int32_t mczi_write_kmer_fasta(const char* path, const uint64_t* lo, const uint64_t* hi,
+                                         const uint64_t* counts, uint64_t n, uint32_t k, char* err, uint64_t err_cap) {
+  if (!path || k < 1 || k > 64 || (n && (!lo || !counts)) || (n && k > 32 && !hi)) return MCZI_ERR_INVALID_CONFIG;
+  std::string e;
+  if (!mczi::write_kmer_fasta(path, lo, k > 32 ? hi : nullptr, counts, n, (int)k, &e)) {
+    if (err && err_cap) std::snprintf(err, err_cap, "%s", e.c_str());
+    return MCZI_ERR_IO;
+  }
+  return MCZI_OK;
+}

@@ -17,6 +17,12 @@ struct HostRecords {
 bool write_kff_records(const std::string& path, int k, int m, uint64_t x, int count_size, uint64_t n,
                        const uint8_t* rec, uint64_t rec_bytes, std::string* err);
 
+// Selected k-mer FASTA (src/lib.rs:1535-1544): record i (from 1) is
+// ">MC_kmer_<i> count=<count>" and the k-mer's bases on one line (k <= 64;
+// the reference wraps at 80 columns).  hi may be null for k <= 32.
+bool write_kmer_fasta(const std::string& path, const uint64_t* lo, const uint64_t* hi, const uint64_t* count,
+                      uint64_t n, int k, std::string* err);
+
 // Greedy simplitig FASTA (src/lib.rs:1469-1533).  Returns false on I/O error.
 bool write_simplitig_file(const std::string& path, const HostRecords& r, int k, std::string* err);
 

@@ -5,7 +5,9 @@ library (``src/lib.rs``): ``CounterConfig`` (:48-53), ``CountedKmer`` (:63-66),
 ``count_inputs`` (:278, sorted by encoded k-mer), ``count_datasets`` (:289),
 ``count_inputs_to_kff_path`` (:457), ``count_inputs_to_fasta_path`` (:427),
 ``count_datasets_to_kff_path`` (:509), ``count_datasets_to_fasta_path``
-(:442), ``expand_fofns`` (:242-276), ``decode_kmer`` (:3056-3069).
+(:442), ``count_inputs_to_kmer_fasta_path`` (:306),
+``count_datasets_to_kmer_fasta_path`` (:357), ``expand_fofns`` (:242-276),
+``decode_kmer`` (:3056-3069).
 
 All counting runs in ``libmczi_gpu.so`` on the GPU; this module only moves
 bytes and records across the C ABI.  Input files given by path are read with
@@ -406,3 +408,34 @@ def count_datasets_to_kff_path(inputs, config: CounterConfig, output_path, ctx: 
 def count_datasets_to_fasta_path(inputs, config: CounterConfig, output_path, ctx: Context | None = None) -> None:
     c = _run(inputs, config, N.MODE_PRESENCE, ctx)
     _write_through(output_path, c.write_fasta)
+
+
+def write_kmer_fasta(records: Records, output_path) -> int:
+    """The selected-k-mer FASTA of `records` (src/lib.rs:1535-1544): record i
+    (from 1) is ">MC_kmer_<i> count=<count>" and the k-mer's bases on one
+    line, in the records' order; written by the library
+    (mczi_write_kmer_fasta, host only).  Returns the number of records."""
+    n = len(records)
+    lo = np.ascontiguousarray(records.lo, dtype=np.uint64)
+    cnt = np.ascontiguousarray(records.count, dtype=np.uint64)
+    hi = np.ascontiguousarray(records.hi, dtype=np.uint64) if records.hi is not None else None
+    err = C.create_string_buffer(1024)
+    rc = N.load().mczi_write_kmer_fasta(os.fsencode(str(output_path)), lo.ctypes.data if n else None,
+                                        hi.ctypes.data if hi is not None and n else None,
+                                        cnt.ctypes.data if n else None, n, records.k, err, len(err))
+    if rc < 0:
+        raise N.MCZIError(rc, err.value.decode(errors="replace") or "invalid k-mer FASTA request")
+    return n
+
+
+def count_inputs_to_kmer_fasta_path(inputs, config: CounterConfig, output_path, ctx: Context | None = None) -> int:
+    """Every kept k-mer as a FASTA record (src/lib.rs:306-311), in ascending
+    encoded order (the reference writes its partitions' order); returns the
+    number of selected k-mers."""
+    return write_kmer_fasta(_run(inputs, config, N.MODE_ABUNDANCE, ctx).records(sorted=True), output_path)
+
+
+def count_datasets_to_kmer_fasta_path(inputs, config: CounterConfig, output_path, ctx: Context | None = None) -> int:
+    """fof mode of count_inputs_to_kmer_fasta_path (src/lib.rs:357-363): the
+    count of a k-mer is the number of datasets containing it."""
+    return write_kmer_fasta(_run(inputs, config, N.MODE_PRESENCE, ctx).records(sorted=True), output_path)

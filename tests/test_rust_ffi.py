@@ -117,6 +117,10 @@ def test_shim_keeps_reference_signatures():
         "pub fn count_datasets_to_fasta_path(inputs: &[PathBuf], config: CounterConfig, output_path: &Path) -> Result<()>",
         "pub fn count_inputs_to_kff_path(inputs: &[PathBuf], config: CounterConfig, output_path: &Path) -> Result<()>",
         "pub fn count_datasets_to_kff_path(inputs: &[PathBuf], config: CounterConfig, output_path: &Path) -> Result<()>",
+        "pub fn count_inputs_to_kmer_fasta_path(inputs: &[PathBuf], config: CounterConfig, output_path: &Path) "
+        "-> Result<u64>",
+        "pub fn count_datasets_to_kmer_fasta_path(inputs: &[PathBuf], config: CounterConfig, output_path: &Path) "
+        "-> Result<u64>",
         "pub fn build_dictionary(index_path: &Path, k: usize, m: usize, _threads: usize, _ram_limit_gib: usize, "
         "_tmp_dir: &Path) -> Result<Dictionary>",
         "pub fn collect_query_kmers_absent_from_index(dictionary: &Dictionary, query_inputs: &[PathBuf]) "
