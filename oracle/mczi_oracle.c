@@ -611,7 +611,9 @@ static void absent_probe(void *c, u128 key) {
     if (!table_contains(a->index, key)) table_add(a->absent, key);
 }
 
-/* ZI: canonical query k-mers absent from the index, sorted, count = 1. */
+/* ZI: canonical query k-mers absent from the index, sorted; count = the
+ * k-mer's absent occurrences in the queries (the sum over the set is MCZI's
+ * not_filtered_kmers, src/mczi.rs:1661-1720, 1895-1914). */
 void *oracle_zi_absent(const uint8_t *index_buf, uint64_t index_len,
                        const uint8_t *const *qbufs, const uint64_t *qlens, int n_queries, int k) {
     result_t *r = (result_t *)calloc(1, sizeof(result_t));
@@ -636,7 +638,7 @@ void *oracle_zi_absent(const uint8_t *index_buf, uint64_t index_len,
     for (uint64_t i = 0; i < absent.cap; i++) {
         if (absent.keys[i] == EMPTY_KEY) continue;
         r->recs[r->n].key = absent.keys[i];
-        r->recs[r->n].count = 1;
+        r->recs[r->n].count = absent.counts[i];
         r->n++;
     }
     qsort(r->recs, r->n, sizeof(rec_t), rec_cmp);

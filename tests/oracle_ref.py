@@ -89,11 +89,18 @@ def count(bufs, k: int, x: int, mode: int = 0, threads: int = 4):
     return _take(h)
 
 
-def zi_absent(index, queries, k: int):
+def zi_absent_counts(index, queries, k: int):
+    """Sorted (lo, hi, count) of the canonical query k-mers absent from the
+    index; count = the k-mer's absent occurrences over the queries."""
     ia = np.frombuffer(index, dtype=np.uint8) if not isinstance(index, np.ndarray) else index
     arrs, ptrs, lens = _arrays(queries)
     h = load().oracle_zi_absent(ia.ctypes.data if ia.size else None, ia.size, ptrs, lens, len(arrs), k)
-    lo, hi, _ = _take(h)
+    return _take(h)
+
+
+def zi_absent(index, queries, k: int):
+    """Sorted (lo, hi) of the canonical query k-mers absent from the index."""
+    lo, hi, _ = zi_absent_counts(index, queries, k)
     return lo, hi
 
 

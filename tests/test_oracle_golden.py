@@ -103,6 +103,23 @@ def test_zi_subtract(oracle, golden):
     assert to_int(lo, hi) == [encode("CCC")]
 
 
+def test_mczi_subtraction_statistics(oracle, golden):
+    """MCZI's scan statistics: every query window is scanned; the absent
+    records' counts are their absent occurrences, so their sum is the number
+    of windows not found in the index (the first case's index is MC's x = 0
+    set of AAACG, i.e. all its k-mers)."""
+    for c in golden["mczi_stats"]["cases"]:
+        queries = [q.encode() for q in c["queries"]]
+        scanned = 0
+        for q in queries:
+            _, offs, _ = oracle.fragments(q, c["k"])
+            scanned += sum(int(offs[i + 1] - offs[i]) - c["k"] + 1 for i in range(len(offs) - 1))
+        lo, hi, cnt = oracle.zi_absent_counts(c["index"].encode(), queries, c["k"])
+        assert scanned == c["scanned_kmers"]
+        assert int(cnt.sum()) == c["not_filtered_kmers"]
+        assert scanned - int(cnt.sum()) == c["filtered_kmers"]
+
+
 def test_zi_subtract_fasta_text(oracle, golden, tmp_path):
     z = golden["zi"]["subtract"]
     lo, hi = oracle.zi_absent(z["index"].encode(), [z["query"].encode()], 3)
