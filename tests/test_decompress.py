@@ -7,7 +7,8 @@ mczi_read_input_file is the host-only entry point these tests call (no
 device needed).  Covered: plain, multi-member gzip, concatenated xz streams,
 multi-frame zstd, a compressed file with a misleading name, an empty file,
 and truncated or corrupt streams, which must fail with MCZI_ERR_IO and a
-message, not return partial data.
+message, not return partial data; and the reference's own gzip, xz and
+invalid-input cases counted by the oracle.
 """
 import ctypes as C
 import ctypes.util
@@ -106,3 +107,24 @@ def test_missing_file(tmp_path):
     from mczi_gb300 import MCZIError
     with pytest.raises(MCZIError, match="failed to open"):
         read(tmp_path / "nope.fa")
+
+
+def test_reference_compressed_and_invalid_inputs(tmp_path, oracle):
+    """The reference's own cases (src/lib.rs:5609-5740): ACGTACGT through
+    gzip and xz counts to ACG:4, GTA:2 at k=3 x=1; an input that is not
+    FASTA/FASTQ, plain or gzip-compressed, is skipped, not an error."""
+    from oracle_ref import encode
+    fa = b">read\nACGTACGT\n"
+    want = {encode("ACG"): 4, encode("GTA"): 2}
+    (tmp_path / "r.fa.gz").write_bytes(gzip.compress(fa))
+    (tmp_path / "r.fa.xz").write_bytes(lzma.compress(fa))
+    (tmp_path / "bad.txt").write_bytes(b"not a FASTA or FASTQ file\n")
+    (tmp_path / "bad.fa.gz").write_bytes(gzip.compress(b"not a FASTA or FASTQ file\n"))
+    for name in ("r.fa.gz", "r.fa.xz"):
+        lo, hi, cnt = oracle.count([read(tmp_path / name)], 3, 1)
+        assert dict(zip((int(v) for v in lo), (int(c) for c in cnt))) == want, name
+    for bad in ("bad.txt", "bad.fa.gz"):
+        data = [read(tmp_path / bad), read(tmp_path / "r.fa.gz")]
+        assert data[0] == b"not a FASTA or FASTQ file\n"  # decoded, then skipped by the parser
+        lo, hi, cnt = oracle.count(data, 3, 1)
+        assert dict(zip((int(v) for v in lo), (int(c) for c in cnt))) == want, bad
