@@ -128,3 +128,19 @@ def test_reference_compressed_and_invalid_inputs(tmp_path, oracle):
         assert data[0] == b"not a FASTA or FASTQ file\n"  # decoded, then skipped by the parser
         lo, hi, cnt = oracle.count(data, 3, 1)
         assert dict(zip((int(v) for v in lo), (int(c) for c in cnt))) == want, bad
+
+
+@pytest.mark.parametrize("ext", [".gz", ".gzip", ".xz", ".zst", ".zstd", ".fa"])
+def test_outputs_compressed_by_extension(tmp_path, ext):
+    """Outputs are compressed by their extension as MC's output writer does
+    (src/lib.rs:1355-1405); each reads back through the library's readers."""
+    from mczi_gb300.mc import _write_through
+    d = payload(3, 60_000)
+    out = tmp_path / ("out.fa" + ext if ext != ".fa" else "out.fa")
+    _write_through(out, lambda p: p.write_bytes(d))
+    raw = out.read_bytes()
+    magic = {".gz": b"\x1f\x8b", ".gzip": b"\x1f\x8b", ".xz": b"\xfd7zXZ\x00", ".zst": b"\x28\xb5\x2f\xfd",
+             ".zstd": b"\x28\xb5\x2f\xfd", ".fa": b">"}[ext]
+    assert raw.startswith(magic)
+    assert read(out) == d
+    assert not list(tmp_path.glob("*.tmp-plain"))
