@@ -115,6 +115,8 @@ extern "C" {
     pub fn mczi_read_input_file(path: *const c_char, data: *mut *mut u8, len: *mut u64, err: *mut c_char,
                                 err_cap: u64) -> i32;
     pub fn mczi_free_input(data: *mut u8);
+    pub fn mczi_compress_output(plain_path: *const c_char, output_path: *const c_char, err: *mut c_char,
+                                err_cap: u64) -> i32;
     pub fn mczi_write_kmer_fasta(path: *const c_char, key_lo: *const u64, key_hi: *const u64, counts: *const u64,
                                  n: u64, k: u32, err: *mut c_char, err_cap: u64) -> i32;
     pub fn mczi_inflate_gzip(ctx: *mut mczi_ctx, gz: *const u8, len: u64, out: *mut u8, cap: u64, n_out: *mut u64)

@@ -77,8 +77,26 @@ impl Gpu {
         bail!(text)
     }
 
+    /// The path entry points.  As the reference's (e.g. src/lib.rs:466-480),
+    /// a compressed output (.gz, .gzip, .xz, .zst, .zstd) is written plain
+    /// first and then compressed (compress_existing_file, src/lib.rs:1397).
     fn count_paths(&self, inputs: &[PathBuf], config: CounterConfig, output: &Path, datasets: bool,
                    kff: bool) -> Result<()> {
+        if !output_compressed(output) {
+            return self.count_paths_plain(inputs, config, output, datasets, kff);
+        }
+        let mut tmp = output.as_os_str().to_owned();
+        tmp.push(".tmp-plain");
+        let tmp = PathBuf::from(tmp);
+        let result = self
+            .count_paths_plain(inputs, config, &tmp, datasets, kff)
+            .and_then(|_| compress_output(&tmp, output));
+        let _ = std::fs::remove_file(&tmp);
+        result
+    }
+
+    fn count_paths_plain(&self, inputs: &[PathBuf], config: CounterConfig, output: &Path, datasets: bool,
+                         kff: bool) -> Result<()> {
         let cfg = c_config(&config)?;
         let (_keep, ptrs) = c_paths(inputs)?;
         let out = c_path(output)?;
@@ -158,6 +176,24 @@ fn c_paths(paths: &[PathBuf]) -> Result<(Vec<CString>, Vec<*const c_char>)> {
     let owned = paths.iter().map(|p| c_path(p)).collect::<Result<Vec<_>>>()?;
     let ptrs = owned.iter().map(|c| c.as_ptr()).collect();
     Ok((owned, ptrs))
+}
+
+fn output_compressed(path: &Path) -> bool {
+    matches!(
+        path.extension().and_then(|e| e.to_str()).map(str::to_ascii_lowercase).as_deref(),
+        Some("gz" | "gzip" | "xz" | "zst" | "zstd")
+    )
+}
+
+fn compress_output(plain: &Path, output: &Path) -> Result<()> {
+    let (p, o) = (c_path(plain)?, c_path(output)?);
+    let mut err = vec![0 as c_char; 1024];
+    let rc = unsafe { sys::mczi_compress_output(p.as_ptr(), o.as_ptr(), err.as_mut_ptr(), err.len() as u64) };
+    if rc != sys::MCZI_OK {
+        let msg = unsafe { CStr::from_ptr(err.as_ptr()) }.to_string_lossy().into_owned();
+        bail!(msg);
+    }
+    Ok(())
 }
 
 fn read_input(path: &Path) -> Result<Vec<u8>> {

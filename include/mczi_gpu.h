@@ -298,6 +298,20 @@ int32_t mczi_set_zi_bucket_records(mczi_ctx* ctx, uint32_t records);
 int32_t mczi_read_input_file(const char* path, uint8_t** data, uint64_t* len, char* err, uint64_t err_cap);
 void mczi_free_input(uint8_t* data);
 
+/* compress_existing_file (src/lib.rs:1397-1405) with MC's output writer
+ * (src/lib.rs:1355-1395): writes the bytes of plain_path to output_path,
+ * compressed as output_path's extension says (.gz / .gzip: gzip at level 1;
+ * .xz: xz preset 6; .zst / .zstd: zstd level 1; case-insensitive), or as
+ * they are for any other extension.  The reference's path entry points write
+ * a compressed output this way (a plain file first, then this step, e.g.
+ * src/lib.rs:466-480); the ones here write the plain file, so a caller
+ * wanting the reference's behaviour adds this step (the Rust crate does).
+ * Host only, no context; the codecs are the system's zlib / liblzma /
+ * libzstd loaded at run time.  MCZI_ERR_IO with the message in err (err_cap
+ * bytes, may be NULL) on an unreadable input, a missing codec or a write
+ * failure. */
+int32_t mczi_compress_output(const char* plain_path, const char* output_path, char* err, uint64_t err_cap);
+
 /* The selected-k-mer FASTA of count_inputs_to_kmer_fasta_path /
  * count_datasets_to_kmer_fasta_path (src/lib.rs:306-425, records as
  * write_kmer_fasta_record_u128, src/lib.rs:1535-1544; MCZI writes its index

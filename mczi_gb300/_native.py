@@ -96,6 +96,7 @@ SIGNATURES = [
     ("mczi_read_input_file", C.c_int32, [C.c_char_p, C.POINTER(C.c_void_p), C.POINTER(C.c_uint64), C.c_char_p,
                                          C.c_uint64]),
     ("mczi_free_input", None, [C.c_void_p]),
+    ("mczi_compress_output", C.c_int32, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_uint64]),
     ("mczi_write_kmer_fasta", C.c_int32, [C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32,
                                           C.c_char_p, C.c_uint64]),
     ("mczi_inflate_gzip", C.c_int32, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_uint64,

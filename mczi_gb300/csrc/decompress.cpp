@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cctype>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -51,7 +52,7 @@ struct ZStream {
   unsigned long adler;
   unsigned long reserved;
 };
-constexpr int Z_OK = 0, Z_STREAM_END = 1, Z_BUF_ERROR = -5, Z_NO_FLUSH = 0;
+constexpr int Z_OK = 0, Z_STREAM_END = 1, Z_BUF_ERROR = -5, Z_NO_FLUSH = 0, Z_FINISH = 4, Z_DEFLATED = 8;
 
 struct ZLib {
   bool ok = false;
@@ -60,6 +61,11 @@ struct ZLib {
   int (*inflate)(ZStream*, int) = nullptr;
   int (*reset)(ZStream*) = nullptr;
   int (*end)(ZStream*) = nullptr;
+  // encoder (outputs)
+  bool enc = false;
+  int (*dinit2)(ZStream*, int, int, int, int, int, const char*, int) = nullptr;
+  int (*deflate)(ZStream*, int) = nullptr;
+  int (*dend)(ZStream*) = nullptr;
 };
 
 // ------------------------------------------------------------ liblzma (xz)
@@ -81,12 +87,14 @@ struct LzmaStream {
 };
 constexpr int LZMA_OK = 0, LZMA_STREAM_END = 1, LZMA_RUN = 0, LZMA_FINISH = 3;
 constexpr uint32_t LZMA_CONCATENATED = 0x08;
+constexpr int LZMA_CHECK_CRC64 = 4;
 
 struct Lzma {
   bool ok = false;
   int (*stream_decoder)(LzmaStream*, uint64_t, uint32_t) = nullptr;
   int (*code)(LzmaStream*, int) = nullptr;
   void (*end)(LzmaStream*) = nullptr;
+  int (*easy_encoder)(LzmaStream*, uint32_t, int) = nullptr;  // outputs
 };
 
 // ------------------------------------------------------------ libzstd
@@ -106,6 +114,9 @@ struct Zstd {
   size_t (*free_ds)(void*) = nullptr;
   unsigned (*is_error)(size_t) = nullptr;
   const char* (*error_name)(size_t) = nullptr;
+  // one-shot encoder (outputs)
+  size_t (*bound)(size_t) = nullptr;
+  size_t (*compress)(void*, size_t, const void*, size_t, int) = nullptr;
 };
 
 void* open_any(const char* const* names) {
@@ -129,16 +140,24 @@ void load_decoders() {
   static const char* zn[] = {"libz.so.1", "libz.so", nullptr};
   static const char* xn[] = {"liblzma.so.5", "liblzma.so", nullptr};
   static const char* sn[] = {"libzstd.so.1", "libzstd.so", nullptr};
-  if (void* h = open_any(zn))
+  if (void* h = open_any(zn)) {
     g_z.ok = sym(h, "zlibVersion", &g_z.version) && sym(h, "inflateInit2_", &g_z.init2) &&
              sym(h, "inflate", &g_z.inflate) && sym(h, "inflateReset", &g_z.reset) && sym(h, "inflateEnd", &g_z.end);
-  if (void* h = open_any(xn))
+    g_z.enc = g_z.ok && sym(h, "deflateInit2_", &g_z.dinit2) && sym(h, "deflate", &g_z.deflate) &&
+              sym(h, "deflateEnd", &g_z.dend);
+  }
+  if (void* h = open_any(xn)) {
     g_x.ok = sym(h, "lzma_stream_decoder", &g_x.stream_decoder) && sym(h, "lzma_code", &g_x.code) &&
              sym(h, "lzma_end", &g_x.end);
-  if (void* h = open_any(sn))
+    sym(h, "lzma_easy_encoder", &g_x.easy_encoder);
+  }
+  if (void* h = open_any(sn)) {
     g_zs.ok = sym(h, "ZSTD_createDStream", &g_zs.create) && sym(h, "ZSTD_initDStream", &g_zs.init) &&
               sym(h, "ZSTD_decompressStream", &g_zs.decompress) && sym(h, "ZSTD_freeDStream", &g_zs.free_ds) &&
               sym(h, "ZSTD_isError", &g_zs.is_error) && sym(h, "ZSTD_getErrorName", &g_zs.error_name);
+    sym(h, "ZSTD_compressBound", &g_zs.bound);
+    sym(h, "ZSTD_compress", &g_zs.compress);
+  }
 }
 
 // output grows in steps; `hint` is an estimate of the decompressed size
@@ -287,6 +306,111 @@ bool unzstd(const std::vector<uint8_t>& in, std::vector<uint8_t>* out, const std
   return ok;
 }
 
+// ------------------------------------------------------------ outputs
+// MC's output writer (src/lib.rs:1355-1405): gzip at the fast level, xz at
+// preset 6 with a CRC64 check, zstd at level 1, chosen by the extension.
+enum class OutputCodec { Plain, Gzip, Xz, Zstd };
+
+OutputCodec output_codec(const std::string& path) {
+  const size_t slash = path.find_last_of('/');
+  const size_t dot = path.find_last_of('.');
+  if (dot == std::string::npos || (slash != std::string::npos && dot < slash)) return OutputCodec::Plain;
+  std::string ext = path.substr(dot + 1);
+  for (char& c : ext) c = (char)std::tolower((unsigned char)c);
+  if (ext == "gz" || ext == "gzip") return OutputCodec::Gzip;
+  if (ext == "xz") return OutputCodec::Xz;
+  if (ext == "zst" || ext == "zstd") return OutputCodec::Zstd;
+  return OutputCodec::Plain;
+}
+
+bool gzip_encode(const std::vector<uint8_t>& in, std::vector<uint8_t>* out, std::string* err) {
+  if (!g_z.enc) {
+    *err = "gzip output needs zlib (libz.so.1), which could not be loaded";
+    return false;
+  }
+  ZStream zs;
+  std::memset(&zs, 0, sizeof zs);
+  // level 1, 15 + 16: 32 KiB window with a gzip wrapper, memLevel 8, default strategy
+  if (g_z.dinit2(&zs, 1, Z_DEFLATED, 15 + 16, 8, 0, g_z.version(), (int)sizeof(ZStream)) != Z_OK) {
+    *err = "zlib could not start an encoder";
+    return false;
+  }
+  size_t used = 0, pos = 0;
+  out->clear();
+  bool ok = true;
+  for (;;) {
+    grow(out, used, in.size() / 2);
+    const size_t in_chunk = std::min<size_t>(in.size() - pos, 1u << 30);
+    const size_t out_chunk = std::min<size_t>(out->size() - used, 1u << 30);
+    zs.next_in = in.data() + pos;
+    zs.avail_in = (unsigned)in_chunk;
+    zs.next_out = out->data() + used;
+    zs.avail_out = (unsigned)out_chunk;
+    const int rc = g_z.deflate(&zs, pos + in_chunk == in.size() ? Z_FINISH : Z_NO_FLUSH);
+    pos += in_chunk - zs.avail_in;
+    used += out_chunk - zs.avail_out;
+    if (rc == Z_STREAM_END) break;
+    if (rc != Z_OK && rc != Z_BUF_ERROR) {
+      *err = "zlib failed to compress (error " + std::to_string(rc) + ")";
+      ok = false;
+      break;
+    }
+  }
+  g_z.dend(&zs);
+  out->resize(used);
+  return ok;
+}
+
+bool xz_encode(const std::vector<uint8_t>& in, std::vector<uint8_t>* out, std::string* err) {
+  if (!g_x.ok || !g_x.easy_encoder) {
+    *err = "xz output needs liblzma (liblzma.so.5), which could not be loaded";
+    return false;
+  }
+  LzmaStream s;
+  std::memset(&s, 0, sizeof s);
+  if (g_x.easy_encoder(&s, 6, LZMA_CHECK_CRC64) != LZMA_OK) {
+    *err = "liblzma could not start an encoder";
+    return false;
+  }
+  s.next_in = in.data();
+  s.avail_in = in.size();
+  size_t used = 0;
+  out->clear();
+  bool ok = true;
+  for (;;) {
+    grow(out, used, in.size() / 3);
+    s.next_out = out->data() + used;
+    s.avail_out = out->size() - used;
+    const size_t before = s.avail_out;
+    const int rc = g_x.code(&s, LZMA_FINISH);  // all input is given: finish from the first call
+    used += before - s.avail_out;
+    if (rc == LZMA_STREAM_END) break;
+    if (rc != LZMA_OK) {
+      *err = "liblzma failed to compress (error " + std::to_string(rc) + ")";
+      ok = false;
+      break;
+    }
+  }
+  g_x.end(&s);
+  out->resize(used);
+  return ok;
+}
+
+bool zstd_encode(const std::vector<uint8_t>& in, std::vector<uint8_t>* out, std::string* err) {
+  if (!g_zs.ok || !g_zs.bound || !g_zs.compress) {
+    *err = "zstd output needs libzstd (libzstd.so.1), which could not be loaded";
+    return false;
+  }
+  out->resize(g_zs.bound(in.size()));
+  const size_t n = g_zs.compress(out->data(), out->size(), in.data(), in.size(), 1);
+  if (g_zs.is_error(n)) {
+    *err = std::string("libzstd failed to compress: ") + g_zs.error_name(n);
+    return false;
+  }
+  out->resize(n);
+  return true;
+}
+
 }  // namespace
 
 InputFormat input_format(const uint8_t* p, size_t n) {
@@ -433,5 +557,38 @@ int32_t mczi_read_input_file(const char* path, uint8_t** data, uint64_t* len, ch
 }
 
 void mczi_free_input(uint8_t* data) { std::free(data); }
+
+int32_t mczi_compress_output(const char* plain_path, const char* output_path, char* err, uint64_t err_cap) {
+  if (!plain_path || !output_path) return MCZI_ERR_INVALID_CONFIG;
+  std::call_once(mczi::g_once, mczi::load_decoders);
+  std::string e;
+  std::vector<uint8_t> plain, packed;
+  auto fail = [&](const std::string& m) {
+    if (err && err_cap) std::snprintf(err, err_cap, "%s", m.c_str());
+    return MCZI_ERR_IO;
+  };
+  FILE* f = std::fopen(plain_path, "rb");
+  if (!f) return fail(std::string("failed to open ") + plain_path);
+  uint8_t buf[1 << 16];
+  size_t got;
+  while ((got = std::fread(buf, 1, sizeof buf, f)) > 0) plain.insert(plain.end(), buf, buf + got);
+  const bool bad = std::ferror(f) != 0;
+  std::fclose(f);
+  if (bad) return fail(std::string("failed to read ") + plain_path);
+  const std::vector<uint8_t>* data = &plain;
+  bool ok = true;
+  switch (mczi::output_codec(output_path)) {
+    case mczi::OutputCodec::Gzip: ok = mczi::gzip_encode(plain, &packed, &e); data = &packed; break;
+    case mczi::OutputCodec::Xz: ok = mczi::xz_encode(plain, &packed, &e); data = &packed; break;
+    case mczi::OutputCodec::Zstd: ok = mczi::zstd_encode(plain, &packed, &e); data = &packed; break;
+    case mczi::OutputCodec::Plain: break;
+  }
+  if (!ok) return fail(e);
+  FILE* o = std::fopen(output_path, "wb");
+  if (!o) return fail(std::string("failed to create ") + output_path);
+  const bool wrote = data->empty() || std::fwrite(data->data(), 1, data->size(), o) == data->size();
+  if (std::fclose(o) != 0 || !wrote) return fail(std::string("failed to compress ") + output_path);
+  return MCZI_OK;
+}
 
 }  // extern "C"

@@ -20,8 +20,6 @@ alone).
 from __future__ import annotations
 
 import ctypes as C
-import gzip
-import lzma
 import os
 from dataclasses import dataclass
 from pathlib import Path
@@ -349,53 +347,22 @@ def _compressed_output(path: Path) -> str | None:
     return None
 
 
-def _zstd_compress(data: bytes, level: int = 1) -> bytes:
-    """One zstd frame of `data` through the host's libzstd (loaded at run
-    time, as the library loads it for zstd inputs)."""
-    import ctypes.util
-    lib = None
-    for name in [ctypes.util.find_library("zstd"), "libzstd.so.1", "libzstd.so"]:
-        if not name:
-            continue
-        try:
-            lib = C.CDLL(name)
-            break
-        except OSError:
-            continue
-    if lib is None:
-        raise N.MCZIError(N.MCZI_ERR_IO, "zstd output needs libzstd on the host")
-    lib.ZSTD_compressBound.restype = C.c_size_t
-    lib.ZSTD_compressBound.argtypes = [C.c_size_t]
-    lib.ZSTD_compress.restype = C.c_size_t
-    lib.ZSTD_compress.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_int]
-    lib.ZSTD_isError.restype = C.c_uint
-    lib.ZSTD_isError.argtypes = [C.c_size_t]
-    cap = lib.ZSTD_compressBound(len(data))
-    out = C.create_string_buffer(max(cap, 1))
-    n = lib.ZSTD_compress(out, cap, data, len(data), level)
-    if lib.ZSTD_isError(n):
-        raise N.MCZIError(N.MCZI_ERR_IO, "zstd compression failed")
-    return out.raw[:n]
-
-
 def _write_through(path: str | os.PathLike, writer) -> None:
     """Writes through `writer` and compresses by the output's extension as
-    MC's output writer does (src/lib.rs:1355-1405): .gz/.gzip at gzip's fast
-    level, .xz at preset 6, .zst/.zstd at level 1."""
+    MC's output writer does (src/lib.rs:1355-1405): .gz/.gzip gzip level 1,
+    .xz preset 6, .zst/.zstd level 1 -- the plain file first, then the
+    library's mczi_compress_output (compress_existing_file, :1397)."""
     p = Path(path)
-    comp = _compressed_output(p)
-    if comp is None:
+    if _compressed_output(p) is None:
         writer(p)
         return
     tmp = p.with_name(p.name + ".tmp-plain")
     try:
         writer(tmp)
-        data = tmp.read_bytes()
-        if comp == "zst":
-            p.write_bytes(_zstd_compress(data, 1))
-            return
-        with (gzip.open(p, "wb", compresslevel=1) if comp == "gz" else lzma.open(p, "wb", preset=6)) as f:
-            f.write(data)
+        err = C.create_string_buffer(1024)
+        rc = N.load().mczi_compress_output(os.fsencode(str(tmp)), os.fsencode(str(p)), err, len(err))
+        if rc < 0:
+            raise N.MCZIError(rc, err.value.decode(errors="replace"))
     finally:
         tmp.unlink(missing_ok=True)
 

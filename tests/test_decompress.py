@@ -144,3 +144,37 @@ def test_outputs_compressed_by_extension(tmp_path, ext):
     assert raw.startswith(magic)
     assert read(out) == d
     assert not list(tmp_path.glob("*.tmp-plain"))
+
+
+@pytest.mark.parametrize("ext", [".gz", ".GZIP", ".xz", ".zst", ".zstd", ".kff"])
+@pytest.mark.parametrize("size", [0, 1, 3_000_000])
+def test_native_compress_output(tmp_path, ext, size):
+    """mczi_compress_output, the reference's compress_existing_file step
+    (src/lib.rs:1355-1405): the output reads back through the library's own
+    readers to the plain bytes, whatever its size."""
+    from mczi_gb300 import _native as N
+    lib = N.load()
+    d = payload(5, max(size, 150))[:size]
+    plain, out = tmp_path / "plain.bin", tmp_path / ("out" + ext)
+    plain.write_bytes(d)
+    err = C.create_string_buffer(512)
+    assert lib.mczi_compress_output(str(plain).encode(), str(out).encode(), err, len(err)) == 0, err.value
+    raw = out.read_bytes()
+    magic = {".gz": b"\x1f\x8b", ".GZIP": b"\x1f\x8b", ".xz": b"\xfd7zXZ\x00", ".zst": b"\x28\xb5\x2f\xfd",
+             ".zstd": b"\x28\xb5\x2f\xfd", ".kff": d[:1]}[ext]
+    assert raw.startswith(magic)
+    if ext == ".kff":
+        assert raw == d
+    assert read(out) == d
+
+
+def test_native_compress_output_errors(tmp_path):
+    from mczi_gb300 import _native as N
+    lib = N.load()
+    err = C.create_string_buffer(512)
+    rc = lib.mczi_compress_output(str(tmp_path / "missing").encode(), str(tmp_path / "o.gz").encode(), err, len(err))
+    assert rc == N.MCZI_ERR_IO and b"failed to open" in err.value
+    (tmp_path / "p").write_bytes(b">r\nACGT\n")
+    rc = lib.mczi_compress_output(str(tmp_path / "p").encode(), str(tmp_path / "no" / "o.xz").encode(), err,
+                                  len(err))
+    assert rc == N.MCZI_ERR_IO and b"failed to create" in err.value
