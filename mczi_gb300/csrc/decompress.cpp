@@ -16,6 +16,9 @@
 // A gzip file whose members all carry their compressed size (BGZF) can
 // instead be returned as it is (keep_sized_gzip) and decoded on the device
 // (inflate.cu); the path-based entry points do that.
+//
+// The same libraries compress outputs (mczi_compress_output): MC's output
+// writer picks gzip, xz or zstd by the output's extension.
 #include "host_io.h"
 #include "../../include/mczi_gpu.h"
 
