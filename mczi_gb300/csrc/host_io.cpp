@@ -180,26 +180,71 @@ bool write_kff_records(const std::string& path, int k, int m, uint64_t x, int co
   return true;
 }
 
+namespace {
+
+// decimal digits of v at p; returns the end
+inline char* put_dec(char* p, uint64_t v) {
+  char t[20];
+  int n = 0;
+  do {
+    t[n++] = (char)('0' + v % 10);
+    v /= 10;
+  } while (v);
+  while (n) *p++ = t[--n];
+  return p;
+}
+
+// records [b, e) of the selected-k-mer FASTA into buf (enough room: 58 + k
+// bytes a record: a header of at most 9 + 20 + 7 + 20 + 1, the bases and a
+// newline); returns the bytes written
+size_t format_kmer_records(char* buf, const uint64_t* lo, const uint64_t* hi, const uint64_t* count, uint64_t b,
+                           uint64_t e, int k) {
+  static const char B[4] = {'A', 'C', 'G', 'T'};
+  char* p = buf;
+  for (uint64_t i = b; i < e; i++) {
+    std::memcpy(p, ">MC_kmer_", 9);
+    p = put_dec(p + 9, i + 1);
+    std::memcpy(p, " count=", 7);
+    p = put_dec(p + 7, count[i]);
+    *p++ = '\n';
+    const u128 key = ((u128)(hi ? hi[i] : 0) << 64) | lo[i];
+    for (int j = 0; j < k; j++) p[j] = B[(int)((key >> (2 * (k - 1 - j))) & 3)];
+    p[k] = '\n';
+    p += k + 1;
+  }
+  return (size_t)(p - buf);
+}
+
+}  // namespace
+
 bool write_kmer_fasta(const std::string& path, const uint64_t* lo, const uint64_t* hi, const uint64_t* count,
                       uint64_t n, int k, std::string* err) {
-  File o(path);
-  if (!o.f) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) {
     *err = "failed to create " + path;
     return false;
   }
-  static const char B[4] = {'A', 'C', 'G', 'T'};
-  char line[64];
-  char seq[72];
-  for (uint64_t i = 0; i < n; i++) {
-    const int l = std::snprintf(line, sizeof line, ">MC_kmer_%llu count=%llu\n", (unsigned long long)(i + 1),
-                                (unsigned long long)count[i]);
-    o.put(line, (size_t)l);
-    const u128 key = ((u128)(hi ? hi[i] : 0) << 64) | lo[i];
-    for (int j = 0; j < k; j++) seq[j] = B[(int)((key >> (2 * (k - 1 - j))) & 3)];
-    seq[k] = '\n';
-    o.put(seq, (size_t)k + 1);
+  // blocks of records formatted on the host's threads, written in order
+  const int threads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  constexpr uint64_t PER = 1u << 17;  // records a thread formats per block
+  const size_t cap = (size_t)PER * (58 + (size_t)k);
+  std::vector<std::vector<char>> bufs((size_t)threads, std::vector<char>(n ? cap : 0));
+  std::vector<size_t> len((size_t)threads);
+  bool ok = true;
+  for (uint64_t b0 = 0; b0 < n && ok; b0 += PER * (uint64_t)threads) {
+    auto part = [&](int t) {
+      const uint64_t b = std::min(n, b0 + PER * (uint64_t)t), e = std::min(n, b + PER);
+      len[(size_t)t] = b < e ? format_kmer_records(bufs[(size_t)t].data(), lo, hi, count, b, e, k) : 0;
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < threads; t++) th.emplace_back(part, t);
+    part(0);
+    for (auto& x : th) x.join();
+    for (int t = 0; t < threads && ok; t++)
+      if (len[(size_t)t] && std::fwrite(bufs[(size_t)t].data(), 1, len[(size_t)t], f) != len[(size_t)t]) ok = false;
   }
-  if (!o.close()) {
+  if (std::fclose(f) != 0) ok = false;
+  if (!ok) {
     *err = "failed to write " + path;
     return false;
   }

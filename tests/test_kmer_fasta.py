@@ -76,3 +76,25 @@ def test_empty_set_and_errors(tmp_path):
         _write(tmp_path, Records(one, None, one, 65))  # k beyond 64
     with pytest.raises(N.MCZIError):
         _write(tmp_path, Records(one, None, one, 33))  # k > 32 needs the high words
+
+
+def test_many_records_across_blocks(tmp_path):
+    """More records than one block of every host thread: the file is the
+    records in order, each formatted as the reference formats it."""
+    from mczi_gb300.mc import Records, write_kmer_fasta
+    n = 700_001
+    rng = np.random.default_rng(3)
+    lo = rng.integers(0, 2**62, size=n, dtype=np.uint64)
+    hi = rng.integers(0, 2**60, size=n, dtype=np.uint64)
+    cnt = rng.integers(0, 2**64 - 1, size=n, dtype=np.uint64, endpoint=True)
+    cnt[:3] = [0, 1, 2**64 - 1]
+    k = 63
+    out = tmp_path / "many.fa"
+    assert write_kmer_fasta(Records(lo, hi, cnt, k), out) == n
+    lines = out.read_bytes().split(b"\n")
+    assert len(lines) == 2 * n + 1 and lines[-1] == b""
+    for i in [0, 1, 2, 3, 131071, 131072, 131073, 262144, 699_999, n - 1] + list(rng.integers(0, n, size=200)):
+        i = int(i)
+        assert lines[2 * i] == b">MC_kmer_%d count=%d" % (i + 1, int(cnt[i]))
+        v = (int(hi[i]) << 64) | int(lo[i])
+        assert lines[2 * i + 1] == bytes(b"ACGT"[(v >> (2 * (k - 1 - j))) & 3] for j in range(k))
